@@ -1,0 +1,186 @@
+/*
+ * sampo.h - C ABI of the GB300 implementation of SAMPO's per-step agent
+ * update (libsampo_cuda.so). Plain C types only; every call returns an int
+ * status (SAMPO_OK = 0, negative on error) and never exits the process.
+ * Handles are not thread-safe; one handle drives one simulation on one GPU.
+ *
+ * The reference crosses its host/device boundary through the OpenCL wrapper
+ * lib_icl (include/lib_icl.h:100-159) and the scan driver
+ * (include/scan.h:5-11), called from src/abms.c. Its per-step sequence
+ * calcStats -> generateSeeds -> update -> createNewAgents -> swap
+ * (src/abms.c:502-529) becomes one sampo_step / sampo_run call here. Each
+ * declaration below names the reference code it replaces.
+ */
+#ifndef SAMPO_H
+#define SAMPO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SAMPO_ABI_VERSION 1
+
+/* ---- status codes ---- */
+#define SAMPO_OK 0
+#define SAMPO_ERR_ARG -1          /* invalid argument */
+#define SAMPO_ERR_CUDA -2         /* CUDA runtime error (see sampo_last_error) */
+#define SAMPO_ERR_CAPACITY -3     /* the next layout does not fit the pool */
+#define SAMPO_ERR_TEMPERATURE -4  /* T >= 44 C: the reference reads past devRates (include/properties.h:105-109) */
+#define SAMPO_ERR_STATE -5        /* call out of order (no population yet, inputs missing) */
+#define SAMPO_ERR_INTERNAL -6     /* a device-side consistency check failed */
+#define SAMPO_ERR_IO -7           /* input file missing or short */
+
+/* ---- device error bits (sampo_device_status) ---- */
+#define SAMPO_DEV_ERR_CAPACITY   0x1u
+#define SAMPO_DEV_ERR_DEVRATES   0x2u
+#define SAMPO_DEV_ERR_TILECOUNT  0x4u
+#define SAMPO_DEV_ERR_LARVATABLE 0x8u
+/* warning bit: the step ran on the reference's initial layout with shared
+ * empty ranges and produced agents in the ranges whose ends coincide; the
+ * reference's compaction would have read one prefix-sum entry for several
+ * ends (kernel/oldToNewAgents.cl:270,279,288) and created agents from
+ * uninitialised memory. This implementation counts them correctly. */
+#define SAMPO_DEV_WARN_REF_LAYOUT 0x100u
+
+/* State order of the ranges (enum State, include/agent.h:54-63). */
+enum { SAMPO_EGG = 0, SAMPO_LARVA, SAMPO_PUPA, SAMPO_IMMATURE, SAMPO_MATESEEKING,
+       SAMPO_BMS, SAMPO_BMD, SAMPO_GRAVID, SAMPO_NSTATES };
+
+/* struct AgentRange / struct Population (include/agent.h:104-123). */
+typedef struct { uint32_t start, end; } sampo_range;
+typedef struct {
+  sampo_range r[SAMPO_NSTATES];
+  uint32_t numLarvae1DayEquiv, numFemale, numPotentiallyInfective;
+} sampo_population;
+
+/* struct Environment (include/agent.h:22-35), same field order. */
+typedef struct {
+  float bloodmealSuccess, ITNValue, IRSValue, carryingCapacity, larvacideValue, oviTrapValue;
+} sampo_environment;
+
+/* struct Seeds (include/agent.h:145-150). Four per step (src/abms.c:145-150). */
+typedef struct { uint32_t z1, z2, z3, z4; } sampo_seeds;
+
+/* struct BitesNcycles (include/agent.h:44-50). */
+typedef struct { uint32_t numCyclesReported, sumCyclesReported, numBitesReported, numInfectBitesReported; } sampo_bites_cycles;
+
+/* What src/abms.c reads back each step (pop[0] at :280 and bnc at :506):
+ * the population at the START of a step and the counters of the previous
+ * step's update. */
+typedef struct { sampo_population pop; sampo_bites_cycles bnc; } sampo_stats_row;
+
+/* Host SoA view of a pool; slots [0, pop.r[GRAVID].end). state is 0..7.
+ * The union field of struct Agent (cumulativeLarvalDelay as float bits for
+ * larvae, ovipositionAttemps for gravids) is carried as raw 32 bits. */
+typedef struct {
+  float* ageInHours; float* hoursInState; float* delay; float* cumulativeSporogonicDevelopment;
+  uint32_t* larvalDelayOrOviAttempts; uint32_t* availableEggs; uint32_t* cycleLength;
+  uint32_t* humanBloodmealCount; uint32_t* numEggBatches;
+  uint8_t* isFemale; uint8_t* state;
+} sampo_pool_view;
+
+typedef struct {
+  uint64_t capacity;          /* slots per pool buffer (reference: maxAgents, include/abms.h:16) */
+  float carrying_capacity;    /* reference: carryingCapacity (src/abms.c:19) */
+  int device;                 /* CUDA device ordinal */
+  uint32_t max_steps;         /* length of the per-step input arrays (reference: maxSteps) */
+} sampo_config;
+
+typedef struct sampo_sim sampo_sim;
+
+/* Replaces icl_init_devices/icl_get_device and the buffer creation of
+ * src/abms.c:614-654, 466-474. Allocates both pool buffers and the step
+ * state on the device. */
+int sampo_create(const sampo_config* cfg, sampo_sim** out);
+/* Replaces icl_release_buffers/icl_release_kernel/icl_release_devices
+ * (src/abms.c:543-554, 694). */
+int sampo_destroy(sampo_sim* s);
+/* Text of the last error on this handle (replaces ICL_ASSERT's message,
+ * include/lib_icl.h:19-25). */
+const char* sampo_last_error(const sampo_sim* s);
+
+/* Per-step inputs: temperature and Environment rows for steps
+ * [0, nsteps) (replaces readSingleValFile/readEnvironment, src/abms.c:94-137,
+ * and the by-value kernel arguments at :319-340). */
+int sampo_set_inputs(sampo_sim* s, const float* temperature, const sampo_environment* env, uint32_t nsteps);
+/* Seeds for steps [first, first+nsteps): 4 per step, in the order
+ * generateSeeds draws them (src/abms.c:145-150). */
+int sampo_set_seeds(sampo_sim* s, uint32_t first, const sampo_seeds* seeds, uint32_t nsteps);
+
+/* createInitialPopulation (src/abms.c:185-228, kernel/initAgents.cl:26-65):
+ * n eggs at [0, n) from init_seeds and temperature[0]. age_days_max < 0
+ * keeps the reference's ages (0) and its initial ranges ([n+1, n+1) for
+ * every empty state); age_days_max >= 0 (an extension) sets ageInHours =
+ * hoursInState = 24*U{0..age_days_max} per slot from splitmix64(age_seed)
+ * and uses the padded layout a compaction produces. */
+int sampo_init_population(sampo_sim* s, uint32_t n, const sampo_seeds init_seeds[4], int age_days_max, uint64_t age_seed);
+/* Uploads a prepared pool (an extension: mixed-stage initial populations). */
+int sampo_load_pool(sampo_sim* s, const sampo_population* pop, const sampo_pool_view* pool);
+
+/* One hourly step with explicit inputs - the body of the reference's loop
+ * (src/abms.c:503-521: calcStats, update = killAgents + updateAgents,
+ * createNewAgents = initAgents + preScan/scan x3 + oldToNewAgents, swap).
+ * *row receives the stats at the START of the step (what printStats shows).
+ * Synchronous. */
+int sampo_step(sampo_sim* s, const sampo_environment* env, float temperature, uint32_t world_time,
+               const sampo_seeds seeds[4], sampo_stats_row* row);
+/* nsteps steps from the arrays given to sampo_set_inputs/sampo_set_seeds,
+ * starting at the simulation's current step; world time = step % 24.
+ * Days are replayed as CUDA graphs of 24 steps. rows (may be NULL)
+ * receives nsteps stats rows. */
+int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows);
+/* Stats at the start of the current (next) step. */
+int sampo_current_row(sampo_sim* s, sampo_stats_row* row);
+/* Index of the next step. */
+int sampo_get_step(sampo_sim* s, uint32_t* step);
+
+/* storeHistogram (src/abms.c:160-183, kernel/ageHistogram.cl:13-35):
+ * 100 bins of min(floor(age/24), 99) over adults of the current pool. */
+int sampo_histogram(sampo_sim* s, uint32_t out[100]);
+
+/* Copies the current pool to the host (replaces icl_read_buffer of the
+ * agent buffers; used for parity tests). The view's arrays must hold
+ * pop.r[GRAVID].end entries; pass NULL to read the ranges only. */
+int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_view* pool);
+/* Sticky device status bits (SAMPO_DEV_*) since creation or the last clear. */
+int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear);
+
+/* Per-kernel timing (the reference's TIMING build: CUDA events replace
+ * icl_profile_event, src/abms.c:522-528). With timing on, sampo_run launches
+ * every kernel on its own between events instead of replaying day graphs.
+ * Turning it on or off clears the sums. */
+int sampo_set_timing(sampo_sim* s, int on);
+/* Sums since sampo_set_timing, in milliseconds: out[0] count pass,
+ * out[1] update+scatter pass, out[2] both; *launches = kernels launched. */
+int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launches);
+
+/* ---- host helpers ---- */
+/* glibc-compatible rand() stream (srand/rand as used by src/abms.c:611,
+ * 145-150) with private state, so replicates can run side by side. */
+typedef struct { uint32_t r[31]; uint32_t i; } sampo_rand_state;
+void sampo_rand_seed(sampo_rand_state* st, uint32_t seed);
+uint32_t sampo_rand_next(sampo_rand_state* st);
+/* Fills 4*nsteps seeds: the draws of nsteps generateSeeds calls. */
+void sampo_rand_seeds(sampo_rand_state* st, sampo_seeds* out, uint32_t nsteps);
+
+/* readSingleValFile / readEnvironment (src/abms.c:94-137), same fscanf
+ * formats; env[i].carryingCapacity = carrying_capacity. */
+int sampo_read_temperature_file(const char* path, float* out, uint32_t nsteps);
+int sampo_read_environment_file(const char* path, sampo_environment* out, uint32_t nsteps, float carrying_capacity);
+
+/* Diagnostic: evaluates the model's deterministic transcendentals on the
+ * device (fn 0 exp(x), 1 log(x), 2 sin(x), 3 pow(x, y)); they must equal the
+ * host definitions bit for bit. No counterpart in the reference, whose
+ * OpenCL built-ins are implementation-defined. */
+int sampo_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, int device);
+
+/* Library version and build information. */
+int sampo_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,42 @@
+/*
+ * ref_main.c - entry point of the ref-as-C oracle (TEST INFRASTRUCTURE ONLY).
+ *
+ * Runs the reference's own src/abms.c (compiled unmodified with its main()
+ * renamed to abms_main) after setting the run parameters that abms.c keeps
+ * in file-scope globals (src/abms.c:15-19): maxSteps, initialAgentCount and
+ * carryingCapacity. The srand() seed and the pinning hooks are set through
+ * the emulator (icl_emul.cpp).
+ *
+ *   sampo_ref [--seed S] [--initial N] [--cc CC] [--steps K]
+ *             [--age-days D --age-seed A] [--hash-file F] TEMP ENV
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+extern long long maxSteps;
+extern unsigned int initialAgentCount;
+extern float carryingCapacity;
+extern unsigned sampo_ref_seed;
+extern int sampo_ref_age_days;
+extern unsigned long long sampo_ref_age_seed;
+extern const char* sampo_ref_hash_file;
+int abms_main(int argc, char** argv);
+
+int main(int argc, char** argv) {
+  char* pos[3] = {argv[0], NULL, NULL};
+  int np = 1;
+  for (int i = 1; i < argc; i++) {
+    if (!strcmp(argv[i], "--seed") && i + 1 < argc) sampo_ref_seed = (unsigned)strtoul(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--initial") && i + 1 < argc) initialAgentCount = (unsigned)strtoul(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--cc") && i + 1 < argc) carryingCapacity = strtof(argv[++i], 0);
+    else if (!strcmp(argv[i], "--steps") && i + 1 < argc) maxSteps = strtoll(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--age-days") && i + 1 < argc) sampo_ref_age_days = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--age-seed") && i + 1 < argc) sampo_ref_age_seed = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--hash-file") && i + 1 < argc) sampo_ref_hash_file = argv[++i];
+    else if (np < 3) pos[np++] = argv[i];
+    else { fprintf(stderr, "sampo_ref: unexpected argument %s\n", argv[i]); return 2; }
+  }
+  if (np != 3) { fprintf(stderr, "usage: sampo_ref [options] TEMP ENV\n"); return 2; }
+  return abms_main(3, pos);
+}

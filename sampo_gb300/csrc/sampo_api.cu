@@ -1,0 +1,534 @@
+// sampo_api.cu - host side of the C ABI declared in include/sampo.h.
+//
+// One handle owns one simulation on one GPU: two pool buffers, the device
+// step state, the per-tile look-back arrays and rings of per-step inputs and
+// stats rows. No call exits the process; errors come back as status codes
+// with a message in sampo_last_error.
+#include <cuda_runtime.h>
+#include <string.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string>
+#include <vector>
+#include "sampo_model.cuh"
+#include "sampo_kernels.cuh"
+
+using namespace sampo;
+
+struct sampo_sim {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t capacity = 0;
+  uint32_t ring = 0;
+  float cc = 0.0f;
+  void* pool_mem[2] = {nullptr, nullptr};
+  DevPool pool[2];
+  SimDev* sim_dev = nullptr;
+  uint32_t* tile_mem = nullptr;
+  uint32_t max_tiles = 0;
+  float* T_dev = nullptr;
+  sampo_environment* env_dev = nullptr;
+  sampo_seeds* seeds_dev = nullptr;
+  uint32_t* wt_dev = nullptr;
+  sampo_stats_row* rows_dev = nullptr;
+  sampo_stats_row* rows_pinned = nullptr;
+  sampo_seeds* init_seeds_dev = nullptr;
+  uint32_t* hist_dev = nullptr;
+  std::vector<float> T_host;           // inputs as set (for temperature[0] and checks)
+  std::vector<uint8_t> have_inputs;    // per ring slot: inputs present for absolute step
+  std::vector<uint32_t> input_step;    // absolute step whose inputs occupy the slot
+  std::vector<uint32_t> seed_step;     // absolute step whose seeds occupy the slot
+  SimDev host_state;                   // template for (re)initialisation
+  uint32_t step = 0;                   // host mirror of the device step index
+  uint32_t epoch = 1;                  // host mirror of the device epoch
+  bool have_pop = false;
+  int grid_count = 0, grid_scatter = 0;
+  cudaGraphExec_t day_graph = nullptr;
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_count = 0, t_scatter = 0, t_total = 0;
+  uint64_t launches = 0;
+  std::string err;
+};
+
+static int fail(sampo_sim* s, int code, const std::string& msg) {
+  if (s) s->err = msg;
+  return code;
+}
+static int cuda_fail(sampo_sim* s, cudaError_t e, const char* what) {
+  return fail(s, SAMPO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(s, e_, what); \
+  } while (0)
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static KParams make_params(sampo_sim* s) {
+  KParams p;
+  p.sim = s->sim_dev;
+  p.pool[0] = s->pool[0];
+  p.pool[1] = s->pool[1];
+  p.tileAgg = s->tile_mem;
+  p.tileIncl = s->tile_mem + (size_t)s->max_tiles * 8;
+  p.tileFlag = s->tile_mem + (size_t)s->max_tiles * 16;
+  p.T = s->T_dev;
+  p.env = s->env_dev;
+  p.seeds = s->seeds_dev;
+  p.wt = s->wt_dev;
+  p.rows = s->rows_dev;
+  p.ring = s->ring;
+  p.maxTiles = s->max_tiles;
+  return p;
+}
+
+// Hourly mortality tables that do not change during a run
+// (kernel/killAgents.cl:84-115,135-147), computed on the host with the same
+// deterministic functions the device uses.
+static void fill_constant_tables(SimDev& h) {
+  for (int d = 0; d < 100; d++) {
+    const float a = 0.1f, B = 25.0f, sg = 0.1f;
+    float e = sampo_expf((float)(uint32_t)d / B);
+    float dmr = (a * e) / (1.0f + (a * B * sg * (e - 1.0f)));
+    float dsr = 1.0f - dmr;
+    float hsr = sampo_powf(dsr, 1.0f / 24.0f);
+    h.adultHMR[d] = 1.0f - hsr;
+    h.larvaHMR[d] = SAMPO_NAN_F;
+  }
+  float dmr = 0.1f;
+  float dsr = 1.0f - dmr;
+  h.aquaticHMR = 1.0f - sampo_powf(dsr, 1.0f / 24.0f);
+}
+
+extern "C" int sampo_abi_version(void) { return SAMPO_ABI_VERSION; }
+
+extern "C" const char* sampo_last_error(const sampo_sim* s) { return s ? s->err.c_str() : "null handle"; }
+
+extern "C" int sampo_destroy(sampo_sim* s) {
+  if (!s) return SAMPO_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->day_graph) cudaGraphExecDestroy(s->day_graph);
+  for (auto& e : s->ev) if (e) cudaEventDestroy(e);
+  cudaFree(s->pool_mem[0]); cudaFree(s->pool_mem[1]);
+  cudaFree(s->sim_dev); cudaFree(s->tile_mem);
+  cudaFree(s->T_dev); cudaFree(s->env_dev); cudaFree(s->seeds_dev); cudaFree(s->wt_dev);
+  cudaFree(s->rows_dev); cudaFree(s->init_seeds_dev); cudaFree(s->hist_dev);
+  if (s->rows_pinned) cudaFreeHost(s->rows_pinned);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
+  if (!cfg || !out) return SAMPO_ERR_ARG;
+  *out = nullptr;
+  if (cfg->capacity < 128 || cfg->capacity > 0xFFFFFF00ull) return SAMPO_ERR_ARG;
+  if (!(cfg->carrying_capacity > 0.0f)) return SAMPO_ERR_ARG;
+  sampo_sim* s = new sampo_sim();
+  s->device = cfg->device;
+  s->capacity = cfg->capacity;
+  s->ring = cfg->max_steps >= 2 ? cfg->max_steps : 8760;
+  s->cc = cfg->carrying_capacity;
+  int rc = SAMPO_OK;
+  do {
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) { rc = cuda_fail(s, e, "cudaSetDevice"); break; }
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(s, e, "stream"); break; }
+    const size_t C = s->capacity;
+    const size_t col4 = align256(C * 4), col1 = align256(C);
+    const size_t bytes = 9 * col4 + col1;
+    for (int b = 0; b < 2; b++) {
+      if ((e = cudaMalloc(&s->pool_mem[b], bytes)) != cudaSuccess) { rc = cuda_fail(s, e, "pool allocation"); break; }
+      char* m = (char*)s->pool_mem[b];
+      DevPool& P = s->pool[b];
+      P.age = (float*)(m + 0 * col4); P.his = (float*)(m + 1 * col4); P.delay = (float*)(m + 2 * col4);
+      P.sporo = (float*)(m + 3 * col4); P.uni = (uint32_t*)(m + 4 * col4); P.avail = (uint32_t*)(m + 5 * col4);
+      P.cycle = (uint32_t*)(m + 6 * col4); P.hbc = (uint32_t*)(m + 7 * col4); P.batches = (uint32_t*)(m + 8 * col4);
+      P.flags = (uint8_t*)(m + 9 * col4);
+    }
+    if (rc) break;
+    s->max_tiles = (uint32_t)((C + kTile - 1) / kTile);
+    if ((e = cudaMalloc(&s->tile_mem, (size_t)s->max_tiles * 17 * 4)) != cudaSuccess) { rc = cuda_fail(s, e, "tile arrays"); break; }
+    cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream);
+    if ((e = cudaMalloc(&s->sim_dev, sizeof(SimDev))) != cudaSuccess) { rc = cuda_fail(s, e, "state"); break; }
+    const size_t R = s->ring;
+    if ((e = cudaMalloc(&s->T_dev, R * sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(&s->env_dev, R * sizeof(sampo_environment))) != cudaSuccess ||
+        (e = cudaMalloc(&s->seeds_dev, R * 4 * sizeof(sampo_seeds))) != cudaSuccess ||
+        (e = cudaMalloc(&s->wt_dev, R * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc(&s->rows_dev, R * sizeof(sampo_stats_row))) != cudaSuccess ||
+        (e = cudaMalloc(&s->init_seeds_dev, 4 * sizeof(sampo_seeds))) != cudaSuccess ||
+        (e = cudaMalloc(&s->hist_dev, 100 * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMallocHost(&s->rows_pinned, R * sizeof(sampo_stats_row))) != cudaSuccess) {
+      rc = cuda_fail(s, e, "input rings");
+      break;
+    }
+    s->T_host.assign(R, 0.0f);
+    s->have_inputs.assign(R, 0);
+    s->input_step.assign(R, 0xffffffffu);
+    s->seed_step.assign(R, 0xffffffffu);
+    memset(&s->host_state, 0, sizeof(SimDev));
+    s->host_state.capacity = (uint32_t)C;
+    s->host_state.cc = s->cc;
+    s->host_state.acc_dmin = 0xffffffffu;
+    s->host_state.epoch = 1;
+    fill_constant_tables(s->host_state);
+    if ((e = cudaMemcpyAsync(s->sim_dev, &s->host_state, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess) {
+      rc = cuda_fail(s, e, "state upload");
+      break;
+    }
+    s->grid_count = grid_blocks_count();
+    s->grid_scatter = grid_blocks_scatter();
+    for (auto& ev : s->ev) cudaEventCreate(&ev);
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_fail(s, e, "create"); break; }
+  } while (0);
+  if (rc) {
+    fprintf(stderr, "sampo_create: %s\n", s->err.c_str());
+    sampo_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_set_inputs(sampo_sim* s, const float* temperature, const sampo_environment* env, uint32_t nsteps) {
+  if (!s || !temperature || !env) return SAMPO_ERR_ARG;
+  if (nsteps == 0 || nsteps > s->ring) return fail(s, SAMPO_ERR_ARG, "nsteps exceeds the input ring (config.max_steps)");
+  for (uint32_t i = 0; i < nsteps; i++)
+    if (env[i].carryingCapacity != s->cc)
+      return fail(s, SAMPO_ERR_ARG, "environment carryingCapacity differs from the configured carrying capacity");
+  cudaSetDevice(s->device);
+  std::vector<uint32_t> wt(nsteps);
+  for (uint32_t i = 0; i < nsteps; i++) {
+    wt[i] = i % 24u;  // (UINT)(currentStep * hoursInTimeStep) % 24u, src/abms.c:514
+    s->T_host[i] = temperature[i];
+    s->have_inputs[i] = 1;
+    s->input_step[i] = i;
+  }
+  CK(cudaMemcpyAsync(s->T_dev, temperature, nsteps * sizeof(float), cudaMemcpyHostToDevice, s->stream), "inputs");
+  CK(cudaMemcpyAsync(s->env_dev, env, nsteps * sizeof(sampo_environment), cudaMemcpyHostToDevice, s->stream), "inputs");
+  CK(cudaMemcpyAsync(s->wt_dev, wt.data(), nsteps * sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream), "inputs");
+  CK(cudaStreamSynchronize(s->stream), "inputs");
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_set_seeds(sampo_sim* s, uint32_t first, const sampo_seeds* seeds, uint32_t nsteps) {
+  if (!s || !seeds) return SAMPO_ERR_ARG;
+  if (nsteps == 0 || nsteps > s->ring) return fail(s, SAMPO_ERR_ARG, "nsteps exceeds the seed ring (config.max_steps)");
+  cudaSetDevice(s->device);
+  uint32_t done = 0;
+  while (done < nsteps) {
+    uint32_t step = first + done;
+    uint32_t slot = step % s->ring;
+    uint32_t n = std::min(nsteps - done, s->ring - slot);
+    CK(cudaMemcpyAsync(s->seeds_dev + (size_t)slot * 4, seeds + (size_t)done * 4, (size_t)n * 4 * sizeof(sampo_seeds),
+                       cudaMemcpyHostToDevice, s->stream), "seeds");
+    for (uint32_t i = 0; i < n; i++) s->seed_step[slot + i] = step + i;
+    done += n;
+  }
+  CK(cudaStreamSynchronize(s->stream), "seeds");
+  return SAMPO_OK;
+}
+
+static int reset_state(sampo_sim* s, const sampo_population& pop) {
+  SimDev h = s->host_state;
+  h.pop = pop;
+  h.step = 0;
+  h.cur = 0;
+  h.epoch = ++s->epoch;
+  CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state reset");
+  s->step = 0;
+  return SAMPO_OK;
+}
+
+static int publish_initial(sampo_sim* s) {
+  KParams p = make_params(s);
+  CK(launch_publish_start(p, s->stream), "initial statistics");
+  CK(cudaStreamSynchronize(s->stream), "initial statistics");
+  s->have_pop = true;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_init_population(sampo_sim* s, uint32_t n, const sampo_seeds init_seeds[4], int age_days_max, uint64_t age_seed) {
+  if (!s || !init_seeds) return SAMPO_ERR_ARG;
+  if (!s->have_inputs[0] || s->input_step[0] != 0)
+    return fail(s, SAMPO_ERR_STATE, "set the inputs first: the initial eggs use temperature[0] (src/abms.c:198)");
+  cudaSetDevice(s->device);
+  sampo_population pop;
+  memset(&pop, 0, sizeof(pop));
+  pop.r[0].start = 0;
+  pop.r[0].end = n;
+  if (age_days_max < 0) {
+    for (int k = 1; k < 8; k++) { pop.r[k].start = n + 1; pop.r[k].end = n + 1; }  // src/abms.c:204-219
+  } else {
+    for (int k = 1; k < 8; k++) {
+      pop.r[k].start = ((pop.r[k - 1].end + kLayoutAlign) / kLayoutAlign) * kLayoutAlign;
+      pop.r[k].end = pop.r[k].start;
+    }
+  }
+  if ((uint64_t)pop.r[7].end > s->capacity) return fail(s, SAMPO_ERR_CAPACITY, "initial population exceeds the capacity");
+  int rc = reset_state(s, pop);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(s->init_seeds_dev, init_seeds, 4 * sizeof(sampo_seeds), cudaMemcpyHostToDevice, s->stream), "seeds");
+  KParams p = make_params(s);
+  CK(launch_init_eggs(p, n, s->T_host[0], s->init_seeds_dev, age_days_max, age_seed, s->stream), "initAgents");
+  return publish_initial(s);
+}
+
+extern "C" int sampo_load_pool(sampo_sim* s, const sampo_population* pop, const sampo_pool_view* v) {
+  if (!s || !pop || !v) return SAMPO_ERR_ARG;
+  if (pop->r[0].start != 0) return fail(s, SAMPO_ERR_ARG, "the egg range must start at slot 0");
+  for (int k = 0; k < 8; k++) {
+    if (pop->r[k].end < pop->r[k].start) return fail(s, SAMPO_ERR_ARG, "range end before start");
+    if (k > 0 && pop->r[k].start <= pop->r[k - 1].end) return fail(s, SAMPO_ERR_ARG, "ranges must be ordered with a gap");
+  }
+  const uint32_t n = pop->r[7].end;
+  if ((uint64_t)n > s->capacity) return fail(s, SAMPO_ERR_CAPACITY, "pool exceeds the capacity");
+  cudaSetDevice(s->device);
+  sampo_population p0 = *pop;
+  int rc = reset_state(s, p0);
+  if (rc) return rc;
+  const DevPool& P = s->pool[0];
+  const size_t b4 = (size_t)n * 4;
+  CK(cudaMemcpyAsync(P.age, v->ageInHours, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.his, v->hoursInState, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.delay, v->delay, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.sporo, v->cumulativeSporogonicDevelopment, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.uni, v->larvalDelayOrOviAttempts, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.avail, v->availableEggs, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.cycle, v->cycleLength, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.hbc, v->humanBloodmealCount, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaMemcpyAsync(P.batches, v->numEggBatches, b4, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  std::vector<uint8_t> flags(n);
+  for (uint32_t i = 0; i < n; i++) flags[i] = (uint8_t)((v->state[i] & 7u) | ((v->isFemale[i] ? 1u : 0u) << 3));
+  CK(cudaMemcpyAsync(P.flags, flags.data(), n, cudaMemcpyHostToDevice, s->stream), "pool upload");
+  CK(cudaStreamSynchronize(s->stream), "pool upload");
+  return publish_initial(s);
+}
+
+static int check_device(sampo_sim* s) {
+  uint32_t st[2];
+  CK(cudaMemcpyAsync(st, &s->sim_dev->error, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream), "status");
+  CK(cudaStreamSynchronize(s->stream), "status");
+  if (st[0] & SAMPO_DEV_ERR_CAPACITY) return fail(s, SAMPO_ERR_CAPACITY, "not enough capacity for the next layout");
+  if (st[0] & SAMPO_DEV_ERR_DEVRATES) return fail(s, SAMPO_ERR_TEMPERATURE, "temperature >= 44 C: the reference reads past devRates");
+  if (st[0]) return fail(s, SAMPO_ERR_INTERNAL, "device consistency check failed (bits " + std::to_string(st[0]) + ")");
+  return SAMPO_OK;
+}
+
+static cudaError_t launch_step(sampo_sim* s, const KParams& p) {
+  cudaError_t e = launch_count(p, s->grid_count, s->stream);
+  if (e != cudaSuccess) return e;
+  return launch_scatter(p, s->grid_scatter, s->stream);
+}
+
+extern "C" int sampo_step(sampo_sim* s, const sampo_environment* env, float temperature, uint32_t world_time,
+                          const sampo_seeds seeds[4], sampo_stats_row* row) {
+  if (!s || !env || !seeds) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population: call sampo_init_population or sampo_load_pool");
+  if (env->carryingCapacity != s->cc) return fail(s, SAMPO_ERR_ARG, "environment carryingCapacity differs from the configured carrying capacity");
+  cudaSetDevice(s->device);
+  const uint32_t slot = s->step % s->ring;
+  CK(cudaMemcpyAsync(s->T_dev + slot, &temperature, sizeof(float), cudaMemcpyHostToDevice, s->stream), "step inputs");
+  CK(cudaMemcpyAsync(s->env_dev + slot, env, sizeof(sampo_environment), cudaMemcpyHostToDevice, s->stream), "step inputs");
+  CK(cudaMemcpyAsync(s->wt_dev + slot, &world_time, sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream), "step inputs");
+  CK(cudaMemcpyAsync(s->seeds_dev + (size_t)slot * 4, seeds, 4 * sizeof(sampo_seeds), cudaMemcpyHostToDevice, s->stream), "step inputs");
+  s->T_host[slot] = temperature;
+  s->have_inputs[slot] = 1;
+  s->input_step[slot] = s->step;
+  s->seed_step[slot] = s->step;
+  if (row) CK(cudaMemcpyAsync(row, s->rows_dev + slot, sizeof(sampo_stats_row), cudaMemcpyDeviceToHost, s->stream), "row");
+  KParams p = make_params(s);
+  CK(launch_step(s, p), "step kernels");
+  s->launches += 2;
+  s->step++;
+  return check_device(s);
+}
+
+static int build_day_graph(sampo_sim* s) {
+  if (s->day_graph) return SAMPO_OK;
+  KParams p = make_params(s);
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture");
+  cudaError_t e = cudaSuccess;
+  for (int h = 0; h < 24 && e == cudaSuccess; h++) e = launch_step(s, p);
+  cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+  if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(s, e, "capture launch"); }
+  if (e2 != cudaSuccess) return cuda_fail(s, e2, "end capture");
+  e = cudaGraphInstantiate(&s->day_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { s->day_graph = nullptr; return cuda_fail(s, e, "graph instantiate"); }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_set_timing(sampo_sim* s, int on) {
+  if (!s) return SAMPO_ERR_ARG;
+  s->timing = on != 0;
+  s->t_count = s->t_scatter = s->t_total = 0;
+  s->launches = 0;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
+  if (!s) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population: call sampo_init_population or sampo_load_pool");
+  if (nsteps == 0) return SAMPO_OK;
+  cudaSetDevice(s->device);
+  for (uint32_t i = 0; i < nsteps; i++) {
+    uint32_t st = s->step + i, slot = st % s->ring;
+    if (!s->have_inputs[slot] || s->input_step[slot] != st) return fail(s, SAMPO_ERR_STATE, "no inputs for step " + std::to_string(st));
+    if (s->seed_step[slot] != st) return fail(s, SAMPO_ERR_STATE, "no seeds for step " + std::to_string(st));
+  }
+  KParams p = make_params(s);
+  uint32_t done = 0;
+  // rows of steps [s->step, s->step + n) are read back in chunks no longer than the ring allows
+  const uint32_t chunk_max = s->ring - 1;
+  while (done < nsteps) {
+    const uint32_t n = std::min(nsteps - done, chunk_max);
+    const uint32_t first = s->step;
+    if (s->timing) {
+      for (uint32_t i = 0; i < n; i++) {
+        CK(cudaEventRecord(s->ev[0], s->stream), "event");
+        CK(launch_count(p, s->grid_count, s->stream), "count kernel");
+        CK(cudaEventRecord(s->ev[1], s->stream), "event");
+        CK(launch_scatter(p, s->grid_scatter, s->stream), "scatter kernel");
+        CK(cudaEventRecord(s->ev[2], s->stream), "event");
+        CK(cudaEventSynchronize(s->ev[2]), "event");
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, s->ev[0], s->ev[1]);
+        cudaEventElapsedTime(&b, s->ev[1], s->ev[2]);
+        s->t_count += a; s->t_scatter += b; s->t_total += a + b;
+        s->launches += 2;
+      }
+    } else {
+      uint32_t i = 0;
+      if (n >= 24) {
+        int rc = build_day_graph(s);
+        if (rc) return rc;
+        for (; i + 24 <= n; i += 24) {
+          CK(cudaGraphLaunch(s->day_graph, s->stream), "day graph");
+          s->launches += 48;
+        }
+      }
+      for (; i < n; i++) {
+        CK(launch_step(s, p), "step kernels");
+        s->launches += 2;
+      }
+    }
+    if (rows) {
+      // rows[first .. first+n) live in ring slots first % ring ...
+      uint32_t c = 0;
+      while (c < n) {
+        uint32_t slot = (first + c) % s->ring;
+        uint32_t m = std::min(n - c, s->ring - slot);
+        CK(cudaMemcpyAsync(rows + done + c, s->rows_dev + slot, (size_t)m * sizeof(sampo_stats_row), cudaMemcpyDeviceToHost, s->stream), "rows");
+        c += m;
+      }
+    }
+    s->step += n;
+    done += n;
+    int rc = check_device(s);
+    if (rc) return rc;
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_current_row(sampo_sim* s, sampo_stats_row* row) {
+  if (!s || !row) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
+  cudaSetDevice(s->device);
+  CK(cudaMemcpyAsync(row, s->rows_dev + s->step % s->ring, sizeof(sampo_stats_row), cudaMemcpyDeviceToHost, s->stream), "row");
+  CK(cudaStreamSynchronize(s->stream), "row");
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_get_step(sampo_sim* s, uint32_t* step) {
+  if (!s || !step) return SAMPO_ERR_ARG;
+  *step = s->step;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_histogram(sampo_sim* s, uint32_t out[100]) {
+  if (!s || !out) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
+  cudaSetDevice(s->device);
+  CK(cudaMemsetAsync(s->hist_dev, 0, 100 * sizeof(uint32_t), s->stream), "histogram");
+  KParams p = make_params(s);
+  CK(launch_histogram(p, s->hist_dev, s->stream), "histogram");
+  CK(cudaMemcpyAsync(out, s->hist_dev, 100 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream), "histogram");
+  CK(cudaStreamSynchronize(s->stream), "histogram");
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_view* v) {
+  if (!s || !pop) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
+  cudaSetDevice(s->device);
+  SimDev h;
+  CK(cudaMemcpyAsync(&h, s->sim_dev, sizeof(SimDev), cudaMemcpyDeviceToHost, s->stream), "state");
+  CK(cudaStreamSynchronize(s->stream), "state");
+  *pop = h.pop;
+  if (!v) return SAMPO_OK;
+  const uint32_t n = h.pop.r[7].end;
+  const DevPool& P = s->pool[h.cur & 1u];
+  const size_t b4 = (size_t)n * 4;
+  CK(cudaMemcpyAsync(v->ageInHours, P.age, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->hoursInState, P.his, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->delay, P.delay, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->cumulativeSporogonicDevelopment, P.sporo, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->larvalDelayOrOviAttempts, P.uni, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->availableEggs, P.avail, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->cycleLength, P.cycle, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->humanBloodmealCount, P.hbc, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaMemcpyAsync(v->numEggBatches, P.batches, b4, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  std::vector<uint8_t> flags(n);
+  CK(cudaMemcpyAsync(flags.data(), P.flags, n, cudaMemcpyDeviceToHost, s->stream), "pool read");
+  CK(cudaStreamSynchronize(s->stream), "pool read");
+  for (uint32_t i = 0; i < n; i++) {
+    v->state[i] = flags[i] & 7u;
+    v->isFemale[i] = (flags[i] >> 3) & 1u;
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear) {
+  if (!s || !bits) return SAMPO_ERR_ARG;
+  cudaSetDevice(s->device);
+  uint32_t st[2];
+  CK(cudaMemcpyAsync(st, &s->sim_dev->error, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream), "status");
+  CK(cudaStreamSynchronize(s->stream), "status");
+  *bits = st[0] | st[1];
+  if (clear) {
+    uint32_t z[2] = {0, 0};
+    CK(cudaMemcpyAsync(&s->sim_dev->error, z, sizeof(z), cudaMemcpyHostToDevice, s->stream), "status");
+    CK(cudaStreamSynchronize(s->stream), "status");
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launches) {
+  if (!s || !out) return SAMPO_ERR_ARG;
+  out[0] = s->t_count; out[1] = s->t_scatter; out[2] = s->t_total;
+  if (launches) *launches = s->launches;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, int device) {
+  if (!x || !out || fn < 0 || fn > 3 || (fn == 3 && !y)) return SAMPO_ERR_ARG;
+  if (n == 0) return SAMPO_OK;
+  sampo_sim* s = nullptr;  // CK() reports through a null handle
+  CK(cudaSetDevice(device), "device");
+  float *dx = nullptr, *dy = nullptr, *dout = nullptr;
+  CK(cudaMalloc(&dx, (size_t)n * 4 * 3), "eval buffers");
+  dy = dx + n;
+  dout = dx + 2 * (size_t)n;
+  cudaError_t e = cudaMemcpy(dx, x, (size_t)n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && y) e = cudaMemcpy(dy, y, (size_t)n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_eval_math(fn, dx, dy, dout, n, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  return e == cudaSuccess ? SAMPO_OK : SAMPO_ERR_CUDA;
+}

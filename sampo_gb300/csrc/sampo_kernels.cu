@@ -1,0 +1,656 @@
+// sampo_kernels.cu - the SAMPO hourly step on GB300 (sm_103a).
+//
+// A step is two persistent-CTA kernels over the current pool buffer:
+//
+//  k_count   reads the ~12 bytes per agent that decide survival, the next
+//            state and the eggs laid (killAgents + the decision part of
+//            updateAgents), and publishes per 1024-slot tile the number of
+//            survivors per next state plus the step's newEggs total.
+//  k_scatter recomputes the same decisions with the complete record,
+//            obtains each survivor's stable rank within its next state
+//            (warp match/popc + a block scan + a decoupled look-back over
+//            the tile counts that k_count already published, so no CTA ever
+//            waits on another), writes the updated record to its slot in the
+//            other buffer (the reference's oldToNewAgents layout,
+//            kernel/oldToNewAgents.cl:57-95,126-226), writes the new eggs at
+//            [0, newEggs) (initAgents, kernel/initAgents.cl:26-65), and
+//            accumulates the next step's statistics (calcL1de.cl,
+//            calcGender.cl). The last CTA to finish publishes the next
+//            population, the stats row and the larval mortality table.
+//
+// This replaces the reference's 19 kernels per step (killAgents,
+// updateAgents, initAgents, 3 x preScan + 3 x Bolt scan-by-key,
+// oldToNewAgents, calcL1de x2, calcFemales x2) and its blocking transfers.
+#include <cuda_runtime.h>
+#include "sampo_model.cuh"
+#include "sampo_kernels.cuh"
+
+namespace sampo {
+
+// include/properties.h:94-98 (double literals stored as float, as there)
+__device__ const float kDevRates[32] = {
+    0.000175044, 0.000549094, 0.00109031, 0.001494158, 0.001752487, 0.001962866, 0.002171238, 0.002392989,
+    0.002633689, 0.00289619, 0.003182685, 0.003495287, 0.003836204, 0.004207789, 0.004612566, 0.005053243,
+    0.005532729, 0.006054144, 0.006620836, 0.007236393, 0.007904657, 0.008629745, 0.009416051, 0.010267388,
+    0.011113704, 0.011960019, 0.012806335, 0.010401163, 0.007995991, 0.00033845, 0.00000533086, 0.0000000840986};
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint4 ld_cg_v4(const uint32_t* p) {
+  uint4 v;
+  asm volatile("ld.global.cg.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_cg_v4(uint32_t* p, uint4 v) {
+  asm volatile("st.global.cg.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Range of slot g in the current layout, -1 for gaps and the tail
+// (the validity test of every reference kernel, e.g. kernel/killAgents.cl:28-35).
+__device__ __forceinline__ int range_of(const sampo_population& pop, uint32_t g) {
+  if (g < pop.r[0].end) return 0;
+#pragma unroll
+  for (int k = 1; k < 8; k++) {
+    if (g < pop.r[k].start) return -1;
+    if (g < pop.r[k].end) return k;
+  }
+  return -1;
+}
+
+// Layout of the next pool from the survivor counts (kernel/oldToNewAgents.cl:57-95).
+__device__ __forceinline__ void next_layout(const uint32_t cnt[8], uint32_t newEggs, sampo_population& np, uint32_t base[8]) {
+  np.r[0].start = 0;
+  np.r[0].end = newEggs + cnt[0];
+  base[0] = newEggs;
+#pragma unroll
+  for (int k = 1; k < 8; k++) {
+    np.r[k].start = ((np.r[k - 1].end + kLayoutAlign) / kLayoutAlign) * kLayoutAlign;
+    np.r[k].end = np.r[k].start + cnt[k];
+    base[k] = np.r[k].start;
+  }
+  np.numLarvae1DayEquiv = 0; np.numFemale = 0; np.numPotentiallyInfective = 0;
+}
+
+struct alignas(16) SharedCtx {
+  StepCtx c;
+  sampo_population pop;
+  uint32_t cur, epoch, step;
+};
+
+__device__ void load_ctx(const KParams& p, SharedCtx& s) {
+  SimDev* sim = p.sim;
+  if (threadIdx.x == 0) {
+    StepCtx& c = s.c;
+    uint32_t step = sim->step;
+    uint32_t i = step % p.ring;
+    const sampo_seeds* sd = p.seeds + (size_t)i * 4;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      c.rng_c13[k] = taus_step(sd[k].z1 + 128u, 13, 19, 12, 4294967294u) ^ taus_step(sd[k].z3 + 128u, 3, 11, 17, 4294967280u);
+      c.rng_z2[k] = sd[k].z2 + 128u;
+      c.rng_z4[k] = sd[k].z4;
+    }
+    c.env = p.env[i];
+    float T = p.T[i];
+    c.T = T;
+    c.wt = p.wt[i];
+    s.pop = sim->pop;
+    c.totalBiomass = s.pop.numLarvae1DayEquiv + s.pop.r[EGG].end + (s.pop.r[PUPA].end - s.pop.r[PUPA].start);
+    c.aquaticHMR = sim->aquaticHMR;
+    c.eggIncubation = -0.923f * T + 60.923f;                           // include/properties.h:29-31
+    float cl = sampo_fminf(sampo_fmaxf(T, 12.0f), 48.0f);               // :105-109
+    int di = (int)cl - 12;
+    c.devOOB = di > 31;
+    c.larvaDev = di > 31 ? 0.0f : kDevRates[di];
+    c.pupaDelay = __double2float_rn(__dadd_rn(__dmul_rn(-0.923, (double)T), 60.923));  // :133-135
+    c.immatureDelay = -2.667f * T + 120.0f;                            // :159-161
+    c.bmdDelay = -1.231f * T + 77.231f;                                // :239-241
+    c.sporoOn = T > 16.0f;                                             // kernel/updateAgents.cl:69-70
+    c.sporoInc = __ddiv_rn(1.0, __dmul_rn((double)(111.0f / (T - 16.0f)), 14.0));
+    s.cur = sim->cur;
+    s.epoch = sim->epoch;
+    s.step = step;
+  }
+  for (int k = threadIdx.x; k < 100; k += blockDim.x) {
+    s.c.adultHMR[k] = sim->adultHMR[k];
+    s.c.larvaHMR[k] = sim->larvaHMR[k];
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------
+// Count pass
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_count(KParams p) {
+  __shared__ SharedCtx S;
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_wcnt[kWarps][8];
+  load_ctx(p, S);
+  const StepCtx& c = S.c;
+  const DevPool src = p.pool[S.cur];
+  const uint32_t end = S.pop.r[GRAVID].end;
+  const uint32_t ntiles = (end + kTile - 1) / kTile;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  Acc acc = {0, 0, 0, 0, 0, 0};
+  uint32_t cta_cnt = 0;  // thread b < 8: this CTA's survivors of next state b
+  uint32_t devoob = 0;
+
+  for (;;) {
+    if (tid == 0) s_tile = atomicAdd(&p.sim->ticket1, 1u);
+    __syncthreads();
+    const uint32_t t = s_tile;
+    if (t >= ntiles) break;
+    uint32_t pk0 = 0, pk1 = 0;  // 8-bit survivor counters: buckets 0-3, 4-7
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      const uint32_t g = t * kTile + k * kBlock + tid;
+      int rg = g < end ? range_of(S.pop, g) : -1;
+      if (rg >= 0) {
+        Rec a;
+        a.age = (rg == LARVA || rg >= IMMATURE) ? src.age[g] : 0.0f;
+        a.his = rg != GRAVID ? src.his[g] : 0.0f;
+        a.delay = rg != GRAVID ? src.delay[g] : 0.0f;
+        a.uni = (rg == LARVA || rg == GRAVID) ? src.uni[g] : 0u;
+        a.avail = rg == GRAVID ? src.avail[g] : 0u;
+        a.female = rg == MATESEEKING ? (src.flags[g] >> 3) & 1u : 0u;
+        a.sporo = 0.0f; a.cycle = 0u; a.hbc = 0u; a.batches = 0u;
+        devoob |= (rg == LARVA) & c.devOOB;
+        int ns = update_agent<false>(c, rg, g, a, acc);
+        if (ns >= 0) {
+          if (ns < 4) pk0 += 1u << (8 * ns);
+          else pk1 += 1u << (8 * (ns - 4));
+        }
+      }
+    }
+    pk0 = __reduce_add_sync(0xffffffffu, pk0);
+    pk1 = __reduce_add_sync(0xffffffffu, pk1);
+    if (lane < 8) s_wcnt[warp][lane] = ((lane < 4 ? pk0 : pk1) >> (8 * (lane & 3))) & 0xffu;
+    __syncthreads();
+    if (tid < 8) {
+      uint32_t sum = 0;
+#pragma unroll
+      for (int w = 0; w < kWarps; w++) sum += s_wcnt[w][tid];
+      p.tileAgg[(size_t)t * 8 + tid] = sum;
+      cta_cnt += sum;
+    }
+    __syncthreads();
+  }
+  if (tid < 8 && cta_cnt) atomicAdd(&p.sim->cnt[tid], cta_cnt);
+  uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
+  if (lane == 0 && ne) atomicAdd(&p.sim->newEggs, ne);
+  uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
+  if (lane == 0 && bad) atomicOr(&p.sim->error, bad);
+}
+
+// ------------------------------------------------------------------------
+// Publishing the statistics of the pool a step starts from: L1de, female and
+// infective counts (calcStats, src/abms.c:230-310), the stats row, and the
+// larval hourly mortality for every larva age present this step
+// (kernel/killAgents.cl:117-133 depends on the age and L1de only). Run by one
+// CTA, all threads. Reads and clears the acc_* accumulators.
+// ------------------------------------------------------------------------
+__device__ void publish_start(const KParams& p, const sampo_population& ranges, bool count_bnc) {
+  SimDev* sim = p.sim;
+  __shared__ uint32_t s_l1, s_dmin, s_dmax;
+  __shared__ float s_cc;
+  if (threadIdx.x == 0) {
+    volatile SimDev* vs = sim;
+    sampo_population np = ranges;
+    uint32_t l1 = vs->acc_L1de;
+    np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? l1 : 0u;  // kernel/calcL1de.cl:259-280
+    np.numFemale = vs->acc_fem;
+    np.numPotentiallyInfective = vs->acc_inf;
+    sim->pop = np;
+    if (count_bnc) {
+      sim->bnc.numCyclesReported = vs->acc_bnc[0];
+      sim->bnc.sumCyclesReported = vs->acc_bnc[1];
+      sim->bnc.numBitesReported = vs->acc_bnc[2];
+      sim->bnc.numInfectBitesReported = vs->acc_bnc[3];
+    }
+    sampo_stats_row row;
+    row.pop = np;
+    row.bnc = sim->bnc;
+    p.rows[sim->step % p.ring] = row;
+    s_l1 = np.numLarvae1DayEquiv;
+    s_dmin = vs->acc_dmin;
+    s_dmax = vs->acc_dmax;
+    s_cc = sim->cc;
+    sim->acc_L1de = 0; sim->acc_fem = 0; sim->acc_inf = 0;
+    sim->acc_dmin = 0xffffffffu; sim->acc_dmax = 0;
+    sim->acc_bnc[0] = sim->acc_bnc[1] = sim->acc_bnc[2] = sim->acc_bnc[3] = 0;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 100; d += blockDim.x) {
+    float hmr = SAMPO_NAN_F;
+    if ((uint32_t)d >= s_dmin && (uint32_t)d <= s_dmax) {
+      // kernel/killAgents.cl:117-125
+      float dmr = 0.1f * sampo_expf((float)s_l1 / ((float)(uint32_t)d * s_cc * 1.0f));
+      dmr = sampo_fminf(dmr, 0.8f);
+      float dsr = 1.0f - dmr;
+      float hsr = sampo_powf(dsr, 1.0f / 24.0f);
+      hmr = 1.0f - hsr;
+    }
+    sim->larvaHMR[d] = hmr;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Update + scatter pass
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
+  __shared__ SharedCtx S;
+  __shared__ sampo_population s_np;
+  __shared__ uint32_t s_base[8], s_prefix[8], s_newEggs, s_tile, s_ok, s_last;
+  __shared__ uint32_t s_off[kItems][kWarps][8];
+  __shared__ uint32_t s_red[kWarps][8];
+  load_ctx(p, S);
+  const StepCtx& c = S.c;
+  SimDev* sim = p.sim;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    uint32_t cnt[8];
+    for (int k = 0; k < 8; k++) cnt[k] = sim->cnt[k];
+    s_newEggs = sim->newEggs;
+    next_layout(cnt, s_newEggs, s_np, s_base);
+    uint64_t tot = (uint64_t)s_newEggs + cnt[0];
+    bool ok = tot <= 0xffffffffull;
+    uint64_t e = tot;
+    for (int k = 1; k < 8; k++) e = ((e + kLayoutAlign) / kLayoutAlign) * kLayoutAlign + cnt[k];
+    ok = ok && e <= (uint64_t)sim->capacity;
+    s_ok = ok;
+    if (!ok && blockIdx.x == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
+  }
+  __syncthreads();
+  const DevPool src = p.pool[S.cur];
+  const DevPool dst = p.pool[S.cur ^ 1];
+  const uint32_t end = S.pop.r[GRAVID].end;
+  const uint32_t nold = s_ok ? (end + kTile - 1) / kTile : 0u;
+  const uint32_t negg = s_ok ? (s_newEggs + kTile - 1) / kTile : 0u;
+  const uint32_t epoch = S.epoch;
+
+  Acc acc = {0, 0, 0, 0, 0, 0};
+  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0;
+
+  for (;;) {
+    if (tid == 0) s_tile = atomicAdd(&sim->ticket2, 1u);
+    for (int q = tid; q < kItems * kWarps * 8; q += kBlock) (&s_off[0][0][0])[q] = 0u;
+    __syncthreads();
+    const uint32_t t = s_tile;
+    if (t >= nold + negg) break;
+    if (t < nold) {
+      // ---- decoupled look-back over the count pass's tile aggregates ----
+      if (warp == 0) {
+        uint32_t ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        int64_t pos = (int64_t)t - 1;
+        while (pos >= 0) {
+          const int64_t idx = pos - lane;
+          const bool valid = idx >= 0;
+          const uint32_t f = valid ? ld_acquire_u32(&p.tileFlag[idx]) : 0u;
+          const uint32_t m = __ballot_sync(0xffffffffu, !valid || f == epoch);
+          const int stop = m ? __ffs(m) - 1 : 32;
+          uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
+          if (valid && lane <= stop) {
+            const uint32_t* q = (lane == stop ? p.tileIncl : p.tileAgg) + (size_t)idx * 8;
+            v0 = ld_cg_v4(q);
+            v1 = ld_cg_v4(q + 4);
+          }
+          ex[0] += __reduce_add_sync(0xffffffffu, v0.x); ex[1] += __reduce_add_sync(0xffffffffu, v0.y);
+          ex[2] += __reduce_add_sync(0xffffffffu, v0.z); ex[3] += __reduce_add_sync(0xffffffffu, v0.w);
+          ex[4] += __reduce_add_sync(0xffffffffu, v1.x); ex[5] += __reduce_add_sync(0xffffffffu, v1.y);
+          ex[6] += __reduce_add_sync(0xffffffffu, v1.z); ex[7] += __reduce_add_sync(0xffffffffu, v1.w);
+          if (m) break;
+          pos -= 32;
+        }
+        if (lane == 0) {
+          const uint32_t* ag = p.tileAgg + (size_t)t * 8;
+          uint4 a0 = ld_cg_v4(ag), a1 = ld_cg_v4(ag + 4);
+          st_cg_v4(p.tileIncl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
+          st_cg_v4(p.tileIncl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
+          st_release_u32(&p.tileFlag[t], epoch);
+#pragma unroll
+          for (int b = 0; b < 8; b++) s_prefix[b] = ex[b];
+        }
+      }
+      // ---- recompute the step for the tile's agents ----
+      Rec a[kItems];
+      int nb[kItems];
+      uint32_t rk[kItems];
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        const uint32_t g = t * kTile + k * kBlock + tid;
+        int rg = g < end ? range_of(S.pop, g) : -1;
+        nb[k] = 8;
+        if (rg >= 0) {
+          a[k].age = src.age[g]; a[k].his = src.his[g]; a[k].delay = src.delay[g]; a[k].sporo = src.sporo[g];
+          a[k].uni = src.uni[g]; a[k].avail = src.avail[g]; a[k].cycle = src.cycle[g]; a[k].hbc = src.hbc[g];
+          a[k].batches = src.batches[g];
+          a[k].female = (src.flags[g] >> 3) & 1u;
+          int ns = update_agent<true>(c, rg, g, a[k], acc);
+          if (ns >= 0) nb[k] = ns;
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
+        rk[k] = __popc(peers & lanemask_lt());
+        if (nb[k] < 8 && lane == __ffs(peers) - 1) s_off[k][warp][nb[k]] = __popc(peers);
+      }
+      __syncthreads();
+      // ---- exclusive scan of the (round, warp) counts, one warp per state ----
+      if (warp < 8) {
+        const int b = warp;
+        uint32_t v = (&s_off[0][0][0])[lane * 8 + b];  // entry (round, warp) = lane, kItems*kWarps == 32
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        (&s_off[0][0][0])[lane * 8 + b] = incl - v;
+        if (lane == 31 && incl != p.tileAgg[(size_t)t * 8 + b]) tilebad = 1;
+      }
+      __syncthreads();
+      // ---- write survivors to their new slots ----
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        const int b = nb[k];
+        if (b < 8) {
+          const uint32_t d = s_base[b] + s_prefix[b] + s_off[k][warp][b] + rk[k];
+          dst.age[d] = a[k].age; dst.his[d] = a[k].his; dst.delay[d] = a[k].delay; dst.sporo[d] = a[k].sporo;
+          dst.uni[d] = a[k].uni; dst.avail[d] = a[k].avail; dst.cycle[d] = a[k].cycle; dst.hbc[d] = a[k].hbc;
+          dst.batches[d] = a[k].batches;
+          dst.flags[d] = (uint8_t)(b | (a[k].female << 3));
+          // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
+          if (b == LARVA) {
+            l1 += sampo_f2u_sat(a[k].age / 24.0f);
+            const uint32_t dd = age_days(a[k].age);
+            dmin = min(dmin, dd); dmax = max(dmax, dd);
+          } else if (b >= IMMATURE && a[k].female) {
+            fem += 1u;
+            inf += a[k].sporo >= 1.0f ? 1u : 0u;
+          }
+        }
+      }
+    } else {
+      // ---- new eggs at [0, newEggs) of the next buffer ----
+      const uint32_t e0 = (t - nold) * kTile;
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        const uint32_t id = e0 + k * kBlock + tid;
+        if (id < s_newEggs) {
+          Rec a;
+          new_egg(c, id, a);
+          dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
+          dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
+          dst.batches[id] = a.batches;
+          dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- per-CTA reduction of the accumulators, one atomic each ----
+  {
+    uint32_t v[8] = {l1, fem, inf, acc.cycles, acc.sumCycles, acc.bites, acc.infectBites,
+                     (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u)};
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = j == 7 ? __reduce_or_sync(0xffffffffu, v[j]) : __reduce_add_sync(0xffffffffu, v[j]);
+    uint32_t mn = __reduce_min_sync(0xffffffffu, dmin), mx = __reduce_max_sync(0xffffffffu, dmax);
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) s_red[warp][j] = v[j];
+    }
+    __shared__ uint32_t s_mn[kWarps], s_mx[kWarps];
+    if (lane == 0) { s_mn[warp] = mn; s_mx[warp] = mx; }
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0}, rmn = 0xffffffffu, rmx = 0;
+      for (int w = 0; w < kWarps; w++) {
+        for (int j = 0; j < 7; j++) r[j] += s_red[w][j];
+        r[7] |= s_red[w][7];
+        rmn = min(rmn, s_mn[w]); rmx = max(rmx, s_mx[w]);
+      }
+      if (r[0]) atomicAdd(&sim->acc_L1de, r[0]);
+      if (r[1]) atomicAdd(&sim->acc_fem, r[1]);
+      if (r[2]) atomicAdd(&sim->acc_inf, r[2]);
+      if (r[3]) atomicAdd(&sim->acc_bnc[0], r[3]);
+      if (r[4]) atomicAdd(&sim->acc_bnc[1], r[4]);
+      if (r[5]) atomicAdd(&sim->acc_bnc[2], r[5]);
+      if (r[6]) atomicAdd(&sim->acc_bnc[3], r[6]);
+      if (r[7]) atomicOr(&sim->error, r[7]);
+      if (rmn != 0xffffffffu) { atomicMin(&sim->acc_dmin, rmn); atomicMax(&sim->acc_dmax, rmx); }
+      __threadfence();
+      s_last = atomicAdd(&sim->done2, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+  }
+  if (!s_last) return;
+
+  // ---- epilogue: the last CTA publishes the next step's start ----
+  __threadfence();
+  if (tid == 0) {
+    // the reference's shared empty initial ranges (src/abms.c:204-219) make
+    // oldToNewAgents read one prefix-sum entry for several range ends
+    const sampo_population& op = S.pop;
+    bool shared_end = false;
+    for (int k = 1; k < 8; k++) shared_end |= op.r[k].end == op.r[k - 1].end;
+    uint32_t moved = 0;
+    for (int k = 1; k < 8; k++) moved += sim->cnt[k];
+    if (shared_end && moved) atomicOr(&sim->warn, SAMPO_DEV_WARN_REF_LAYOUT);
+    if (s_ok) {
+      sim->cur = S.cur ^ 1u;
+    }
+    sim->step = S.step + 1u;
+    sim->epoch = S.epoch + 1u;
+    for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
+    sim->newEggs = 0;
+    sim->ticket1 = 0;
+    sim->ticket2 = 0;
+    sim->done2 = 0;
+  }
+  __syncthreads();
+  if (s_ok) publish_start(p, s_np, true);
+  else publish_start(p, S.pop, true);
+}
+
+// ------------------------------------------------------------------------
+// Initial population: initAgents over [0, n) (kernel/initAgents.cl:26-65),
+// optionally with ages 24*U{0..age_days_max} from splitmix64 (an extension).
+// ------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_init_eggs(KParams p, uint32_t n, float T0, const sampo_seeds* seeds, int age_days_max, uint64_t age_seed) {
+  __shared__ StepCtx c;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 4; k++) {
+      c.rng_c13[k] = taus_step(seeds[k].z1 + 128u, 13, 19, 12, 4294967294u) ^ taus_step(seeds[k].z3 + 128u, 3, 11, 17, 4294967280u);
+      c.rng_z2[k] = seeds[k].z2 + 128u;
+      c.rng_z4[k] = seeds[k].z4;
+    }
+    c.eggIncubation = -0.923f * T0 + 60.923f;
+  }
+  __syncthreads();
+  const DevPool dst = p.pool[0];
+  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+    Rec a;
+    new_egg(c, id, a);
+    if (age_days_max >= 0) {
+      uint64_t z = mix64(age_seed ^ mix64((uint64_t)id));
+      float h = 24.0f * (float)(uint32_t)((z >> 32) % ((uint64_t)age_days_max + 1));
+      a.age = h; a.his = h;
+    }
+    dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
+    dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
+    dst.batches[id] = a.batches;
+    dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
+  }
+}
+
+// Statistics of the current pool (grid-stride), accumulated into acc_*.
+__global__ void k_pool_stats(KParams p) {
+  SimDev* sim = p.sim;
+  const sampo_population pop = sim->pop;
+  const DevPool src = p.pool[sim->cur];
+  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0;
+  const uint32_t end = pop.r[GRAVID].end;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < end; g += gridDim.x * blockDim.x) {
+    int rg = range_of(pop, g);
+    if (rg == LARVA) {
+      float age = src.age[g];
+      l1 += sampo_f2u_sat(age / 24.0f);
+      uint32_t dd = age_days(age);
+      dmin = min(dmin, dd); dmax = max(dmax, dd);
+    } else if (rg >= IMMATURE) {
+      if ((src.flags[g] >> 3) & 1u) { fem++; inf += src.sporo[g] >= 1.0f ? 1u : 0u; }
+    }
+  }
+  l1 = __reduce_add_sync(0xffffffffu, l1);
+  fem = __reduce_add_sync(0xffffffffu, fem);
+  inf = __reduce_add_sync(0xffffffffu, inf);
+  dmin = __reduce_min_sync(0xffffffffu, dmin);
+  dmax = __reduce_max_sync(0xffffffffu, dmax);
+  if ((threadIdx.x & 31) == 0) {
+    if (l1) atomicAdd(&sim->acc_L1de, l1);
+    if (fem) atomicAdd(&sim->acc_fem, fem);
+    if (inf) atomicAdd(&sim->acc_inf, inf);
+    if (dmin != 0xffffffffu) { atomicMin(&sim->acc_dmin, dmin); atomicMax(&sim->acc_dmax, dmax); }
+  }
+}
+
+__global__ void k_publish_start(KParams p) {
+  __shared__ sampo_population ranges;
+  if (threadIdx.x == 0) ranges = p.sim->pop;
+  __syncthreads();
+  publish_start(p, ranges, false);
+}
+
+// ageHistogram (kernel/ageHistogram.cl:13-35) with warp-aggregated shared
+// atomics: lanes that fall in the same bin add once.
+__global__ void k_histogram(KParams p, uint32_t* hist) {
+  __shared__ uint32_t h[100];
+  for (int k = threadIdx.x; k < 100; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  SimDev* sim = p.sim;
+  const sampo_population pop = sim->pop;
+  const DevPool src = p.pool[sim->cur];
+  const uint32_t lo = pop.r[IMMATURE].start, hi = pop.r[GRAVID].end;
+  const uint32_t span = hi > lo ? hi - lo : 0u;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < span; base += stride) {
+    const uint32_t g = lo + base + threadIdx.x;
+    int rg = (base + threadIdx.x < span) ? range_of(pop, g) : -1;
+    uint32_t bin = 0xffffffffu;
+    if (rg >= IMMATURE) {
+      bin = sampo_f2u_sat(src.age[g] / 24.0f);
+      bin = bin < 99u ? bin : 99u;
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, bin);
+    if (bin != 0xffffffffu && (threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&h[bin], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < 100; k += blockDim.x)
+    if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
+__global__ void k_pack_flags(KParams p, const uint8_t* state, const uint8_t* female, uint32_t n) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x)
+    p.pool[0].flags[g] = (uint8_t)((state[g] & 7u) | ((female[g] ? 1u : 0u) << 3));
+}
+__global__ void k_unpack_flags(KParams p, uint8_t* state, uint8_t* female, uint32_t n) {
+  const DevPool src = p.pool[p.sim->cur];
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    uint8_t f = src.flags[g];
+    state[g] = f & 7u;
+    female[g] = (f >> 3) & 1u;
+  }
+}
+
+// ------------------------------------------------------------------------
+static int g_sms = 0;
+static int sm_count() {
+  if (!g_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 1;
+  }
+  return g_sms;
+}
+int grid_blocks_count() {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_count, kBlock, 0);
+  return sm_count() * (per > 0 ? per : 1);
+}
+int grid_blocks_scatter() {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kBlock, 0);
+  return sm_count() * (per > 0 ? per : 1);
+}
+cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
+  k_count<<<grid, kBlock, 0, st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
+  k_scatter<<<grid, kBlock, 0, st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev, int age_days_max,
+                             uint64_t age_seed, cudaStream_t st) {
+  int grid = sm_count() * 4;
+  k_init_eggs<<<grid, 256, 0, st>>>(p, n, T0, seeds_dev, age_days_max, age_seed);
+  return cudaGetLastError();
+}
+cudaError_t launch_publish_start(const KParams& p, cudaStream_t st) {
+  k_pool_stats<<<sm_count() * 4, 256, 0, st>>>(p);
+  k_publish_start<<<1, 128, 0, st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st) {
+  k_histogram<<<sm_count() * 4, 256, 0, st>>>(p, hist_dev);
+  return cudaGetLastError();
+}
+cudaError_t launch_pack_pool(const KParams& p, const uint8_t* state, const uint8_t* female, uint32_t n, cudaStream_t st) {
+  k_pack_flags<<<sm_count() * 4, 256, 0, st>>>(p, state, female, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_unpack_flags(const KParams& p, uint8_t* state, uint8_t* female, uint32_t n, cudaStream_t st) {
+  k_unpack_flags<<<sm_count() * 4, 256, 0, st>>>(p, state, female, n);
+  return cudaGetLastError();
+}
+
+}  // namespace sampo
+
+namespace sampo {
+// Diagnostic: the model's transcendental definitions evaluated on the device.
+__global__ void k_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float v = 0.0f;
+    switch (fn) {
+      case 0: v = sampo_expf(x[i]); break;
+      case 1: v = sampo_logf(x[i]); break;
+      case 2: v = sampo_sinf(x[i]); break;
+      case 3: v = sampo_powf(x[i], y[i]); break;
+      default: break;
+    }
+    out[i] = v;
+  }
+}
+cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {
+  k_eval_math<<<sm_count() * 2, 256, 0, st>>>(fn, x, y, out, n);
+  return cudaGetLastError();
+}
+}  // namespace sampo

@@ -1,0 +1,70 @@
+// sampo_kernels.cuh - device state shared by the kernels and the host API.
+#pragma once
+#include <stdint.h>
+#include "../../include/sampo.h"
+
+namespace sampo {
+
+constexpr int kBlock = 256;                 // threads per CTA
+constexpr int kItems = 4;                   // slots per thread per tile (striped by kBlock)
+constexpr int kTile = kBlock * kItems;      // slots per tile
+constexpr int kWarps = kBlock / 32;
+
+// One pool buffer: structure of arrays, one column per agent field.
+struct DevPool {
+  float* age; float* his; float* delay; float* sporo;
+  uint32_t* uni; uint32_t* avail; uint32_t* cycle; uint32_t* hbc; uint32_t* batches;
+  uint8_t* flags;   // bits 0-2 state (0..7), bit 3 isFemale
+};
+
+// Device-resident state of one simulation.
+struct SimDev {
+  sampo_population pop;       // ranges + stats of the current pool (reference pop[0] at step start)
+  sampo_bites_cycles bnc;     // counters of the last update (printed with the next row)
+  uint32_t step;              // index of the next step
+  uint32_t cur;               // current pool buffer (0/1)
+  uint32_t epoch;             // look-back flag value of the running step (never reused)
+  uint32_t cnt[8];            // count pass: survivors by next state
+  uint32_t newEggs;           // count pass: eggs laid (EggsNbiomass.newEggs)
+  uint32_t ticket1;           // count pass tile ticket
+  uint32_t ticket2, done2;    // scatter pass tile ticket / finished CTAs
+  uint32_t acc_bnc[4];        // scatter pass: numCycles, sumCycles, numBites, numInfectBites
+  uint32_t acc_L1de, acc_fem, acc_inf, acc_dmin, acc_dmax;  // stats of the next pool
+  uint32_t error;             // sticky SAMPO_DEV_ERR_* bits
+  uint32_t warn;              // sticky SAMPO_DEV_WARN_* bits
+  uint32_t capacity;
+  float cc;                   // carrying capacity (constant per run, src/abms.c:19,132)
+  float aquaticHMR;
+  float adultHMR[100];
+  float larvaHMR[100];        // for the current step; NaN outside the larvae's age range
+};
+
+struct KParams {
+  SimDev* sim;
+  DevPool pool[2];
+  uint32_t* tileAgg;          // [maxTiles][8] per-tile survivor counts (count pass)
+  uint32_t* tileIncl;         // [maxTiles][8] inclusive prefixes (scatter pass)
+  uint32_t* tileFlag;         // [maxTiles] epoch when tileIncl is valid
+  const float* T;             // [ring] temperature per step
+  const sampo_environment* env;  // [ring]
+  const sampo_seeds* seeds;   // [ring][4]
+  const uint32_t* wt;         // [ring] world time per step
+  sampo_stats_row* rows;      // [ring] stats at the start of each step
+  uint32_t ring;
+  uint32_t maxTiles;
+};
+
+// Launch helpers (sampo_kernels.cu).
+int grid_blocks_count();
+int grid_blocks_scatter();
+cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st);
+cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st);
+cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev,
+                             int age_days_max, uint64_t age_seed, cudaStream_t st);
+cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
+cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
+cudaError_t launch_pack_pool(const KParams& p, const uint8_t* state, const uint8_t* female, uint32_t n, cudaStream_t st);
+cudaError_t launch_unpack_flags(const KParams& p, uint8_t* state, uint8_t* female, uint32_t n, cudaStream_t st);
+cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
+
+}  // namespace sampo

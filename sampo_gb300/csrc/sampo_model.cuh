@@ -1,0 +1,239 @@
+// sampo_model.cuh - the per-agent SAMPO model on the GPU (sm_103a).
+//
+// One hourly step of one agent: killAgents (kernel/killAgents.cl:24-148)
+// followed by updateAgents (kernel/updateAgents.cl:39-270) with the species
+// functions of include/properties.h and the generator of include/gpuRand.h.
+// Float expressions are written in the reference's operation order and the
+// file is compiled with --fmad=false, so every product and sum rounds exactly
+// as the reference's C semantics say; the two places where the reference
+// promotes to double (include/properties.h:134, kernel/updateAgents.cl:69-70)
+// stay double.
+//
+// update_agent<FULL> is used twice per step: FULL=false by the counting pass
+// (only the fields that decide survival, the next state and the number of
+// eggs laid) and FULL=true by the scatter pass (the complete record). Both
+// instantiations run the same decision code on the same inputs, so they
+// agree bit for bit.
+#pragma once
+#include <stdint.h>
+#include "sampo_math.h"
+#include "../../include/sampo.h"
+
+namespace sampo {
+
+enum : int { EGG = 0, LARVA, PUPA, IMMATURE, MATESEEKING, BMS, BMD, GRAVID, NSTATE };
+constexpr uint32_t kLayoutAlign = 64;  // LOCAL_SIZE (include/agent.h:9-17): a layout constant
+
+// One agent record in registers (the SoA columns of the pool).
+struct Rec {
+  float age, his, delay, sporo;
+  uint32_t uni;      // cumulativeLarvalDelay (float bits) for larvae, ovipositionAttemps for gravids
+  uint32_t avail, cycle, hbc, batches;
+  uint32_t female;   // 0/1
+};
+
+// Per-step constants shared by every agent of a step (lives in shared memory).
+struct StepCtx {
+  // HybridTaus (include/gpuRand.h:33-50): z1 and z3 do not depend on the
+  // work-item, so their Tausworthe steps are folded per seed slot.
+  uint32_t rng_c13[4], rng_z2[4], rng_z4[4];
+  sampo_environment env;
+  float T;
+  uint32_t wt;                 // world time = step % 24
+  uint32_t totalBiomass;       // kernel/killAgents.cl:42-43
+  float aquaticHMR;            // eggs and pupae (kernel/killAgents.cl:103-115,135-147)
+  float eggIncubation;         // eggsIncubation(T)
+  float larvaDev;              // larvaDevelopment(T)
+  float pupaDelay, immatureDelay, bmdDelay;
+  double sporoInc;             // 1/((111/(T-16))*14) in double, used when T > 16 and bitten
+  uint32_t sporoOn;            // T > 16
+  uint32_t devOOB;             // T >= 44: the reference reads past devRates
+  float adultHMR[100];
+  float larvaHMR[100];
+};
+
+// Counters an agent update contributes to (BitesNcycles, EggsNbiomass).
+struct Acc {
+  uint32_t newEggs, bites, infectBites, cycles, sumCycles;
+  uint32_t bad;                // larva table miss (must stay 0)
+};
+
+__host__ __device__ __forceinline__ uint32_t taus_step(uint32_t z, int S1, int S2, int S3, uint32_t M) {
+  uint32_t b = (((z << S1) ^ z) >> S2);
+  return (((z & M) << S3) ^ b);
+}
+
+__device__ __forceinline__ float rng(const StepCtx& c, int slot, uint32_t gid) {
+  uint32_t v = c.rng_c13[slot] ^ taus_step(c.rng_z2[slot] + gid, 2, 25, 4, 4294967288u) ^
+               (1664525u * (c.rng_z4[slot] * gid) + 1013904223u);
+  return 2.3283064365387e-10f * __uint2float_rn(v);
+}
+
+// BoxMuller(seeds+1, ...) (include/gpuRand.h:56-63): u0 from slot 1, u1 from slot 2.
+__device__ __forceinline__ float box_muller(const StepCtx& c, uint32_t gid, float mean, float sd) {
+  float u0 = rng(c, 1, gid), u1 = rng(c, 2, gid);
+  float r = __fsqrt_rn(-2.0f * sampo_logf(u0));
+  float theta = (2.0f * 3.14159274101257f) * u1;
+  return (r * sampo_sinf(theta)) * sd + mean;
+}
+
+// eggsHatching (include/properties.h:39-60)
+__host__ __device__ __forceinline__ float eggs_hatching(float p) {
+  float m, b;
+  if (p < 0.5f) { m = 48.0f; b = 0.0f; }
+  else if (p < 0.85f) { m = 68.5714f; b = -10.2857f; }
+  else if (p < 0.90f) { m = 480.0f; b = -360.0f; }
+  else if (p < 0.94f) { m = 600.00f; b = -468.0f; }
+  else { m = 2400.0f; b = -2160.0f; }
+  return (float)sampo_f2u_sat(m * p + b + 0.5f);
+}
+
+__host__ __device__ __forceinline__ bool night(uint32_t wt) { return wt <= 6u || wt >= 18u; }
+
+__device__ __forceinline__ uint32_t age_days(float age) {
+  return sampo_f2u_sat(sampo_fminf(age / 24.0f, 99.0f));  // kernel/killAgents.cl:55
+}
+
+// Kill then update one valid agent of range rg at slot gid.
+// Returns the next state (0..7), or -1 when the agent dies this step.
+template <bool FULL>
+__device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t gid, Rec& a, Acc& acc) {
+  // ---- killAgents (kernel/killAgents.cl:52-147) ----
+  {
+    float prob = rng(c, 0, gid);
+    float hmr;
+    if (rg >= IMMATURE) {
+      hmr = c.adultHMR[age_days(a.age)];
+    } else if (rg == LARVA) {
+      hmr = c.larvaHMR[age_days(a.age)];
+      if (hmr != hmr) acc.bad = 1;  // table entry not prepared
+    } else {
+      hmr = c.aquaticHMR;
+    }
+    if (prob <= hmr) return -1;
+  }
+  // ---- updateAgents (kernel/updateAgents.cl:57-270), elapsedTimeInHours = 1.0f ----
+  a.age = a.age + 1.0f;
+  a.his = a.his + 1.0f;
+  if (FULL && c.sporoOn && a.hbc > 0u)  // kernel/updateAgents.cl:69-70, in double
+    a.sporo = __double2float_rn(__dadd_rn((double)a.sporo, c.sporoInc));
+  switch (rg) {
+    case EGG:
+      if (a.his >= a.delay) {
+        if (FULL) {
+          a.age = 24.0f; a.his = 0.0f;
+          a.delay = box_muller(c, gid, 1.0f, 0.1f);  // larvaDelay (include/properties.h:87-91)
+        }
+        return LARVA;
+      }
+      return EGG;
+    case LARVA: {
+      if (c.env.larvacideValue > 0.0f && a.his == 1.0f) {
+        if (rng(c, 2, gid) <= c.env.larvacideValue) return -1;
+      }
+      float cld = __uint_as_float(a.uni) + c.larvaDev;
+      if (FULL) a.uni = __float_as_uint(cld);
+      if (cld >= a.delay && night(c.wt)) {
+        if (FULL) { a.his = 0.0f; a.delay = c.pupaDelay; }
+        return PUPA;
+      }
+      return LARVA;
+    }
+    case PUPA:
+      if (a.his >= a.delay && night(c.wt)) {
+        if (FULL) { a.age = 0.0f; a.his = 0.0f; a.delay = c.immatureDelay; }
+        return IMMATURE;
+      }
+      return PUPA;
+    case IMMATURE:
+      if (a.his >= a.delay) {
+        if (FULL) { a.delay = 1.0f; a.his = 0.0f; }  // mateSeekingDelay
+        return MATESEEKING;
+      }
+      return IMMATURE;
+    case MATESEEKING:
+      if (a.his >= a.delay && a.female && c.wt == 18u) {
+        if (FULL) { a.his = 0.0f; a.delay = 0.0f; }   // bloodMealSeekingDelay
+        return BMS;
+      }
+      return MATESEEKING;
+    case BMS:
+      if (FULL) a.cycle += 1u;
+      if (a.his >= a.delay && night(c.wt)) {
+        if (rng(c, 1, gid) <= c.env.bloodmealSuccess) {
+          if (c.env.ITNValue * 1.0f * 1.0f > 0.0f) {
+            if (rng(c, 2, gid) <= c.env.ITNValue * 1.0f * 1.0f) return -1;
+          }
+          if (FULL) {
+            a.hbc += 1u;
+            acc.bites += 1u;
+            a.his = 0.0f; a.delay = c.bmdDelay;
+            if (a.sporo >= 1.0f) acc.infectBites += 1u;
+          }
+          return BMD;
+        }
+      }
+      return BMS;
+    case BMD:
+      if (c.env.IRSValue * 1.0f > 0.0f) {
+        if (rng(c, 2, gid) <= c.env.IRSValue * 1.0f) return -1;
+      }
+      if (FULL) a.cycle += 1u;
+      if (a.his >= a.delay) {
+        if (FULL) {
+          if (a.avail <= 0u && a.female) {
+            // generateEggs (include/properties.h:257-266)
+            uint32_t eggs = sampo_f2u_sat(box_muller(c, gid, 170.0f, 30.0f) + 0.5f);
+            eggs = sampo_f2u_sat((float)eggs * sampo_powf(0.8f, (float)a.batches) + 0.5f);
+            a.batches += 1u;
+            a.avail = eggs;
+          }
+          a.his = 0.0f; a.uni = 0u;
+        }
+        return GRAVID;
+      }
+      return BMD;
+    default: {  // GRAVID
+      if (FULL) a.cycle += 1u;
+      if (night(c.wt)) {
+        if (rng(c, 1, gid) < 0.25f) {
+          uint32_t avail = a.avail;
+          bool trapped = false;
+          if (c.env.oviTrapValue > 0.0f) {
+            if (rng(c, 2, gid) <= c.env.oviTrapValue) { trapped = true; avail = 0u; }
+          }
+          if (!trapped) {
+            // layEggs (include/properties.h:296-307)
+            float nbm = (float)c.totalBiomass / (((float)a.uni + 1.0f) * c.env.carryingCapacity);
+            float pbm = sampo_fmaxf(0.0f, 1.0f - nbm);
+            uint32_t pe = sampo_f2u_sat(ceilf((float)avail * pbm));
+            if (!FULL) acc.newEggs += pe;
+            avail = avail - pe;
+          }
+          if (FULL) { a.uni += 1u; a.avail = avail; }
+          if (avail == 0u) {
+            if (FULL) {
+              acc.cycles += 1u; acc.sumCycles += a.cycle;
+              a.cycle = 0u; a.his = 0.0f; a.delay = 0.0f;
+            }
+            if (trapped) return -1;
+            return BMS;
+          }
+        }
+      }
+      return GRAVID;
+    }
+  }
+}
+
+// initAgents (kernel/initAgents.cl:34-64) for new slot id.
+__device__ __forceinline__ void new_egg(const StepCtx& c, uint32_t id, Rec& a) {
+  a.age = 0.0f; a.his = 0.0f;
+  a.female = rng(c, 3, id) <= 0.5f ? 1u : 0u;
+  a.sporo = 0.0f;
+  a.hbc = 0u; a.avail = 0u; a.cycle = 0u; a.uni = 0u;
+  a.delay = c.eggIncubation + eggs_hatching(rng(c, 2, id));
+  a.batches = 0u;
+}
+
+}  // namespace sampo
