@@ -1,0 +1,392 @@
+#!/usr/bin/env python
+"""Throughput of SAMPO's simulated day on GB300, in agent-days per second.
+
+A bench step is one simulated day: 24 hourly steps of the hot path (count
+pass + update/scatter pass each), replayed as one CUDA graph. The default
+workload is the large plain run: 1e6 initial agents in the egg / larva /
+pupa / adult ratio 40/30/10/20, a 2^27-slot pool, seasonal weather
+(26 + 4 sin(2 pi d/365) + N(0, 0.5^2) C, seed 2) for 730 days, carrying
+capacity 5 x 1e6. agent-days = sum over hourly steps of the live agents at
+the step's start / 24.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload plain-large|roofline|plain-small]
+
+--impl reference times the reference's own per-step algorithm on the host
+cores (the CPU restatement in oracle/, pinned to the reference's code by the
+golden traces) over a bounded sample of the same workload.
+Under torchrun (N > 1) every rank runs its own replicate (replicas only:
+a simulation does not shard), rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    # BASELINE config 1: the headline
+    "plain-large": dict(name="plain large run: 1e6 agents (egg/larva/pupa/adult 40/30/10/20), 2^27 slots, 730 days, seasonal weather seed 2",
+                        counts=(400_000, 300_000, 100_000, 200_000), capacity=1 << 27, days=730, seed=2,
+                        cc=5_000_000.0, weather=("seasonal", 2, 26.0, 4.0, 0.5)),
+    # BASELINE config 2: the bandwidth-roofline run
+    "roofline": dict(name="roofline run: 5e7 preloaded agents (uniform over 4 stages, 50/50 gender), 1e8 slots, 28 C constant, 90 days, seed 3",
+                     counts=(12_500_000,) * 4, capacity=100_000_000, days=90, seed=3, cc=3_000_000.0,
+                     weather=("constant", 28.0)),
+    # BASELINE config 0 with its mixed-stage analogue off: the CPU-runnable case
+    "plain-small": dict(name="plain single run: 10,000 eggs aged U{0..3} days, 2^20 slots, 365 days, seed 1",
+                        eggs=10_000, capacity=1 << 20, days=365, seed=1, cc=50_000.0,
+                        weather=("seasonal", 1, 26.0, 4.0, 0.5)),
+}
+
+# algorithmic bytes per live agent read by the count pass, by state of its range
+# (the fields that decide survival, the next state and eggs laid)
+COUNT_BYTES = np.array([8, 12, 8, 12, 13, 12, 12, 12], dtype=np.float64)
+RECORD_BYTES = 37.0   # 9 x 4-byte fields + 1 flag byte
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def oracle_seed_stream(seed: int, nsteps: int):
+    """srand(seed) + generateSeeds draws from the oracle's glibc restatement
+    (the reference arm never loads the CUDA library)."""
+    import oracle
+    v = oracle.glibc_rand(seed, 16 * (nsteps + 1))
+    return v[:16].reshape(4, 4), v[16:].reshape(nsteps, 4, 4)
+
+
+def build_workload(wl: dict, days: int, seed_fn=None):
+    from sampo_gb300 import inputs
+    from sampo_gb300.population import make_pool
+    if seed_fn is None:
+        from sampo_gb300.sim import seed_stream as seed_fn
+    w = wl["weather"]
+    if w[0] == "seasonal":
+        weather = inputs.seasonal_weather(days, w[1], w[2], w[3], w[4])
+    else:
+        weather = inputs.constant_weather(days, w[1])
+    T = np.repeat(weather.temperature_c.astype(np.float32), 24)
+    n = days * 24
+    env = np.zeros(n, dtype=inputs.ENV_DTYPE)
+    env["bloodmealSuccess"] = 0.25
+    env["carryingCapacity"] = np.float32(wl["cc"])
+    init, seeds = seed_fn(wl["seed"], n)
+    pool = None
+    if "counts" in wl:
+        pool = make_pool(wl["counts"], T[0], seed=wl["seed"])
+    return T, env, init, seeds, pool
+
+
+def start_pool(sim, wl, init, pool):
+    if pool is not None:
+        sim.load_pool(*pool)
+    else:
+        sim.init_population(wl["eggs"], init, 3, wl["seed"])
+
+
+def live_counts(rows) -> np.ndarray:
+    r = rows["ranges"].astype(np.int64)
+    return (r[:, :, 1] - r[:, :, 0])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profile():
+    """dram bytes per live agent of the update/scatter kernel from the
+    committed ncu summary (profiles/k_scatter_dram.json), or None."""
+    p = os.path.join(REPO, "profiles", "k_scatter_dram.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
+def gpu_arm(args, wl, rank, world, device):
+    from sampo_gb300.sim import PinnedArray, Simulation
+    days = max(wl["days"], args.warmup + args.steps)
+    T, env, init, seeds, pool = build_workload(wl, days)
+    if rank > 0:  # independent replicate per rank
+        from sampo_gb300.sim import seed_stream
+        init, seeds = seed_stream(wl["seed"] * 1000 + rank, days * 24)
+    nsteps = days * 24
+    sim = Simulation(capacity=wl["capacity"], carrying_capacity=wl["cc"], max_steps=nsteps + 1, device=device)
+    sim.set_inputs(T, env)
+    sim.set_seeds(0, seeds)
+
+    def fresh():
+        start_pool(sim, wl, init, pool)
+        if args.warmup:
+            sim.run(24 * args.warmup, want_rows=False)
+
+    # ---- value: device-resident inputs, day graphs, L2 flushed between days ----
+    fresh()
+    sim.flush_l2()
+    rows, ms = [], 0.0
+    sync_barrier(world)
+    t0 = time.perf_counter()
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            rows.append(sim.run(24))
+            ms += sim.last_run_ms()
+            sim.flush_l2()
+    wall = time.perf_counter() - t0
+    sync_barrier(world)
+    rows = np.concatenate(rows)
+    live = live_counts(rows)
+    agent_days = float(live.sum()) / 24.0
+    gpu_launches = 48 * args.steps
+
+    # ---- roofline: the same days again, each kernel between CUDA events ----
+    fresh()
+    sim.set_timing(True)
+    rows2 = sim.run(24 * args.steps)
+    times, launches = sim.kernel_times()
+    sim.set_timing(False)
+    live2 = live_counts(rows2)
+    if not np.array_equal(live2, live):
+        raise RuntimeError("timing-mode rerun diverged from the graph run")
+    tot = live2.sum(axis=1).astype(np.float64)
+    nxt = np.append(tot[1:], tot[-1])  # agents written = pool size at the next step's start
+    scatter_bytes = RECORD_BYTES * (tot + nxt)
+    count_bytes = (live2 * COUNT_BYTES).sum(axis=1)
+    n_launch = len(tot)
+    scatter_ms, count_ms = times[1] / n_launch, times[0] / n_launch
+    peak, peak_kind = peaks()
+    achieved = scatter_bytes.mean() / (scatter_ms * 1e-3) / 1e9
+    prof = traffic_from_profile()
+    traffic = None
+    if prof:
+        traffic = float(prof["dram_bytes_per_live_agent"] * tot.mean())
+
+    # ---- e2e: through the C ABI with page-locked host buffers, per day ----
+    from sampo_gb300._lib import ENV_DTYPE, ROW_DTYPE
+    fresh()
+    hT = PinnedArray((24,), np.float32)
+    hE = PinnedArray((24,), ENV_DTYPE)
+    hS = PinnedArray((24, 4, 4), np.uint32)
+    hR = PinnedArray((24,), ROW_DTYPE)
+    lib = sim.lib
+    first = 24 * args.warmup
+    sync_barrier(world)
+    t0 = time.perf_counter()
+    e2e_live = 0
+    for d in range(args.steps):
+        s0 = first + 24 * d
+        hT.a[:] = T[s0:s0 + 24]
+        hE.a[:] = env[s0:s0 + 24]
+        hS.a[:] = seeds[s0:s0 + 24]
+        sim._check(lib.sampo_set_inputs(sim.h, s0, hT.p, hE.p, 24))
+        sim._check(lib.sampo_set_seeds(sim.h, s0, hS.p, 24))
+        sim.run_into(24, hR.p)
+        r = hR.a["ranges"].astype(np.int64)
+        e2e_live += int((r[:, :, 1] - r[:, :, 0]).sum())
+    e2e_wall = time.perf_counter() - t0
+    sync_barrier(world)
+    for h in (hT, hE, hS, hR):
+        h.free()
+    sim.close()
+    return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(),
+                gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, achieved=achieved, peak=peak,
+                peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
+                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days)
+
+
+def cpu_reference(wl, seconds: float, first_steps: int | None = None, warmup: int = 0):
+    """The oracle port on all host threads over a bounded sample (hourly
+    steps from the workload's start, after `warmup` untimed steps) of about
+    `seconds` of CPU work, or exactly `first_steps` timed steps."""
+    from oracle import OracleSim
+    days = wl["days"]
+    T, env, init, seeds, pool = build_workload(wl, days, seed_fn=oracle_seed_stream)
+    threads = os.cpu_count() or 1
+    o = OracleSim(wl["capacity"], threads)
+    if pool is not None:
+        o.load_pool(*pool)
+    else:
+        o.init_eggs(wl["eggs"], T[0], init, 3, wl["seed"])
+    for i in range(warmup):
+        o.step(env[i], T[i], i % 24, seeds[i])
+    live_sum, steps, t0 = 0, warmup, time.perf_counter()
+    limit = warmup + first_steps if first_steps else len(T)
+    while steps < limit:
+        r = o.step(env[steps], T[steps], steps % 24, seeds[steps])
+        rr = r["ranges"].astype(np.int64)
+        live_sum += int((rr[:, 1] - rr[:, 0]).sum())
+        steps += 1
+        if first_steps is None and time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return dict(value=live_sum / 24.0 / dt, steps=steps - warmup, seconds=dt, threads=threads, agent_steps=live_sum)
+
+
+# ---------------- distributed plumbing (replicas only) ----------------
+_PG = None
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def dist_init(world):
+    global _PG
+    if world > 1 and _PG is None:
+        import torch.distributed as dist
+        dist.init_process_group(backend="gloo")
+        _PG = dist
+    return _PG
+
+
+def sync_barrier(world):
+    if world > 1:
+        _PG.barrier()
+
+
+def all_reduce(vals, op):
+    if _PG is None:
+        return vals
+    import torch
+    t = torch.tensor(vals, dtype=torch.float64)
+    _PG.all_reduce(t, op=_PG.ReduceOp.MAX if op == "max" else _PG.ReduceOp.SUM)
+    return t.tolist()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=727)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plain-large", choices=list(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    wl = WORKLOADS[args.workload]
+    rank, world, local = dist_env()
+    dist_init(world)
+    cfg = {"workload": wl["name"], "step": "one simulated day = 24 hourly steps",
+           "capacity_slots": wl["capacity"], "carrying_capacity": wl["cc"]}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # each bench step = one simulated hour of the same workload on the host cores
+        ref = cpu_reference(wl, 0, first_steps=args.steps, warmup=args.warmup)
+        line = {"impl": "reference", "metric": "agent-days/s", "value": ref["value"], "unit": "agent-days/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ref["seconds"] * 1e3 / max(ref["steps"], 1), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
+                "config": dict(cfg, step="one simulated hour (bounded sample of the same workload)"),
+                "cpu_baseline": {"value": ref["value"], "unit": "agent-days/s", "cores": ref["threads"], "kind": "port",
+                                 "sample": f"first {ref['steps']} hourly steps of the workload, all host threads (OpenMP)"},
+                "e2e": {"value": ref["value"], "unit": "agent-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    r = gpu_arm(args, wl, rank, world, local if world > 1 else 0)
+    dev_s = r["ms"] / 1e3
+    tmax, = all_reduce([dev_s], "max")
+    e2e_max, = all_reduce([r["e2e_wall"]], "max")
+    tot_days, e2e_days = all_reduce([r["agent_days"], r["e2e_agent_days"]], "sum")
+    if rank != 0:
+        return
+    cpu = cpu_reference(wl, args.cpu_seconds) if world == 1 else None
+    live_tot = r["live"].sum(axis=1)
+    pool_bytes = live_tot * RECORD_BYTES
+    cfg.update({"days_timed": args.steps, "live_agents_min": int(live_tot.min()), "live_agents_max": int(live_tot.max()),
+                "l2": "flushed between timed days (write of a buffer > 2x L2); pool bytes %.2e..%.2e" % (pool_bytes.min(), pool_bytes.max()),
+                "parallelism": f"replicas x{world}"})
+    line = {
+        "metric": "agent-days/s", "value": tot_days / tmax, "unit": "agent-days/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32 (f64 where the reference promotes)",
+        "data": "synthetic", "config": cfg,
+        "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
+                     "frac": r["achieved"] / r["peak"], "traffic": r["traffic"], "kernel": "k_scatter (update + stable scatter)",
+                     "peak_kind": r["peak_kind"], "scatter_ms_per_launch": r["scatter_ms"], "count_ms_per_launch": r["count_ms"],
+                     "count_pass_gbs": r["count_gbs"],
+                     "algorithmic_bytes": "k_scatter: 37 B read per live agent + 37 B written per agent of the next pool"},
+        "e2e": {"value": e2e_days / e2e_max, "unit": "agent-days/s", "h2d_bytes_per_step": 24 * (4 + 24 + 4 + 64),
+                "d2h_bytes_per_step": 24 * 92},
+        "gpu_launches": r["gpu_launches"] * world,
+        "clocks": r["clocks"],
+        "wall_s_timed": r["wall"],
+    }
+    if cpu:
+        line["cpu_baseline"] = {"value": cpu["value"], "unit": "agent-days/s", "cores": cpu["threads"], "kind": "port",
+                                "sample": f"first {cpu['steps']} hourly steps of the same workload ({cpu['seconds']:.1f} s), oracle port, OpenMP"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

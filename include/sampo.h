@@ -38,6 +38,7 @@ extern "C" {
 #define SAMPO_DEV_ERR_DEVRATES   0x2u
 #define SAMPO_DEV_ERR_TILECOUNT  0x4u
 #define SAMPO_DEV_ERR_LARVATABLE 0x8u
+#define SAMPO_DEV_ERR_TMA        0x10u  /* a tile's bulk copy did not land within the wait limit */
 /* warning bit: the step ran on the reference's initial layout with shared
  * empty ranges and produced agents in the ranges whose ends coincide; the
  * reference's compaction would have read one prefix-sum entry for several
@@ -103,9 +104,10 @@ int sampo_destroy(sampo_sim* s);
 const char* sampo_last_error(const sampo_sim* s);
 
 /* Per-step inputs: temperature and Environment rows for steps
- * [0, nsteps) (replaces readSingleValFile/readEnvironment, src/abms.c:94-137,
- * and the by-value kernel arguments at :319-340). */
-int sampo_set_inputs(sampo_sim* s, const float* temperature, const sampo_environment* env, uint32_t nsteps);
+ * [first, first+nsteps) (replaces readSingleValFile/readEnvironment,
+ * src/abms.c:94-137, and the by-value kernel arguments at :319-340).
+ * World time of step i is i % 24 (src/abms.c:514). */
+int sampo_set_inputs(sampo_sim* s, uint32_t first, const float* temperature, const sampo_environment* env, uint32_t nsteps);
 /* Seeds for steps [first, first+nsteps): 4 per step, in the order
  * generateSeeds draws them (src/abms.c:145-150). */
 int sampo_set_seeds(sampo_sim* s, uint32_t first, const sampo_seeds* seeds, uint32_t nsteps);
@@ -156,6 +158,16 @@ int sampo_set_timing(sampo_sim* s, int on);
 /* Sums since sampo_set_timing, in milliseconds: out[0] count pass,
  * out[1] update+scatter pass, out[2] both; *launches = kernels launched. */
 int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launches);
+/* Device time of the last sampo_run, in milliseconds, from CUDA events
+ * recorded on the simulation's stream around its launches. */
+int sampo_last_run_ms(sampo_sim* s, double* ms);
+
+/* Page-locked host memory for the per-step inputs and rows (cudaMallocHost
+ * on the handle's device), and a write of a scratch buffer larger than the
+ * L2 cache on the handle's stream (benchmarks flush L2 between iterations). */
+void* sampo_host_alloc(size_t bytes);
+void sampo_host_free(void* p);
+int sampo_flush_l2(sampo_sim* s);
 
 /* ---- host helpers ---- */
 /* glibc-compatible rand() stream (srand/rand as used by src/abms.c:611,

@@ -86,7 +86,7 @@ SIGNATURES = {
     "sampo_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
     "sampo_destroy": (C.c_int, [_P]),
     "sampo_last_error": (C.c_char_p, [_P]),
-    "sampo_set_inputs": (C.c_int, [_P, _P, _P, C.c_uint32]),
+    "sampo_set_inputs": (C.c_int, [_P, C.c_uint32, _P, _P, C.c_uint32]),
     "sampo_set_seeds": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32]),
     "sampo_init_population": (C.c_int, [_P, C.c_uint32, _P, C.c_int, C.c_uint64]),
     "sampo_load_pool": (C.c_int, [_P, C.POINTER(Population), C.POINTER(PoolView)]),
@@ -105,6 +105,10 @@ SIGNATURES = {
     "sampo_read_temperature_file": (C.c_int, [C.c_char_p, _P, C.c_uint32]),
     "sampo_read_environment_file": (C.c_int, [C.c_char_p, _P, C.c_uint32, C.c_float]),
     "sampo_eval_math": (C.c_int, [C.c_int, _P, _P, _P, C.c_uint32, C.c_int]),
+    "sampo_last_run_ms": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "sampo_host_alloc": (_P, [C.c_size_t]),
+    "sampo_host_free": (None, [_P]),
+    "sampo_flush_l2": (C.c_int, [_P]),
 }
 
 _lib = None

@@ -38,6 +38,10 @@ struct sampo_sim {
   std::vector<uint8_t> have_inputs;    // per ring slot: inputs present for absolute step
   std::vector<uint32_t> input_step;    // absolute step whose inputs occupy the slot
   std::vector<uint32_t> seed_step;     // absolute step whose seeds occupy the slot
+  std::vector<uint32_t> wt_staging;    // world times being uploaded
+  void* flush_buf = nullptr;           // L2 flush scratch (allocated on first use)
+  size_t flush_bytes = 0;
+  double last_run_ms = 0;
   SimDev host_state;                   // template for (re)initialisation
   uint32_t step = 0;                   // host mirror of the device step index
   uint32_t epoch = 1;                  // host mirror of the device epoch
@@ -115,7 +119,7 @@ extern "C" int sampo_destroy(sampo_sim* s) {
   cudaFree(s->pool_mem[0]); cudaFree(s->pool_mem[1]);
   cudaFree(s->sim_dev); cudaFree(s->tile_mem);
   cudaFree(s->T_dev); cudaFree(s->env_dev); cudaFree(s->seeds_dev); cudaFree(s->wt_dev);
-  cudaFree(s->rows_dev); cudaFree(s->init_seeds_dev); cudaFree(s->hist_dev);
+  cudaFree(s->rows_dev); cudaFree(s->init_seeds_dev); cudaFree(s->hist_dev); cudaFree(s->flush_buf);
   if (s->rows_pinned) cudaFreeHost(s->rows_pinned);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -138,7 +142,9 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     if (e != cudaSuccess) { rc = cuda_fail(s, e, "cudaSetDevice"); break; }
     if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = cuda_fail(s, e, "stream"); break; }
     const size_t C = s->capacity;
-    const size_t col4 = align256(C * 4), col1 = align256(C);
+    // 16 bytes of slack per column: tile copies are rounded up to 16 bytes
+    // and may read up to 15 bytes past the last slot.
+    const size_t col4 = align256(C * 4 + 16), col1 = align256(C + 16);
     const size_t bytes = 9 * col4 + col1;
     for (int b = 0; b < 2; b++) {
       if ((e = cudaMalloc(&s->pool_mem[b], bytes)) != cudaSuccess) { rc = cuda_fail(s, e, "pool allocation"); break; }
@@ -194,23 +200,30 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
   return SAMPO_OK;
 }
 
-extern "C" int sampo_set_inputs(sampo_sim* s, const float* temperature, const sampo_environment* env, uint32_t nsteps) {
+extern "C" int sampo_set_inputs(sampo_sim* s, uint32_t first, const float* temperature, const sampo_environment* env,
+                                uint32_t nsteps) {
   if (!s || !temperature || !env) return SAMPO_ERR_ARG;
   if (nsteps == 0 || nsteps > s->ring) return fail(s, SAMPO_ERR_ARG, "nsteps exceeds the input ring (config.max_steps)");
   for (uint32_t i = 0; i < nsteps; i++)
     if (env[i].carryingCapacity != s->cc)
       return fail(s, SAMPO_ERR_ARG, "environment carryingCapacity differs from the configured carrying capacity");
   cudaSetDevice(s->device);
-  std::vector<uint32_t> wt(nsteps);
-  for (uint32_t i = 0; i < nsteps; i++) {
-    wt[i] = i % 24u;  // (UINT)(currentStep * hoursInTimeStep) % 24u, src/abms.c:514
-    s->T_host[i] = temperature[i];
-    s->have_inputs[i] = 1;
-    s->input_step[i] = i;
+  if (s->wt_staging.size() < nsteps) s->wt_staging.resize(nsteps);
+  uint32_t done = 0;
+  while (done < nsteps) {
+    const uint32_t step = first + done, slot = step % s->ring;
+    const uint32_t n = std::min(nsteps - done, s->ring - slot);
+    for (uint32_t i = 0; i < n; i++) {
+      s->wt_staging[done + i] = (step + i) % 24u;  // (UINT)(currentStep * hoursInTimeStep) % 24u, src/abms.c:514
+      s->T_host[slot + i] = temperature[done + i];
+      s->have_inputs[slot + i] = 1;
+      s->input_step[slot + i] = step + i;
+    }
+    CK(cudaMemcpyAsync(s->T_dev + slot, temperature + done, n * sizeof(float), cudaMemcpyHostToDevice, s->stream), "inputs");
+    CK(cudaMemcpyAsync(s->env_dev + slot, env + done, n * sizeof(sampo_environment), cudaMemcpyHostToDevice, s->stream), "inputs");
+    CK(cudaMemcpyAsync(s->wt_dev + slot, s->wt_staging.data() + done, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream), "inputs");
+    done += n;
   }
-  CK(cudaMemcpyAsync(s->T_dev, temperature, nsteps * sizeof(float), cudaMemcpyHostToDevice, s->stream), "inputs");
-  CK(cudaMemcpyAsync(s->env_dev, env, nsteps * sizeof(sampo_environment), cudaMemcpyHostToDevice, s->stream), "inputs");
-  CK(cudaMemcpyAsync(s->wt_dev, wt.data(), nsteps * sizeof(uint32_t), cudaMemcpyHostToDevice, s->stream), "inputs");
   CK(cudaStreamSynchronize(s->stream), "inputs");
   return SAMPO_OK;
 }
@@ -238,7 +251,11 @@ static int reset_state(sampo_sim* s, const sampo_population& pop) {
   h.pop = pop;
   h.step = 0;
   h.cur = 0;
-  h.epoch = ++s->epoch;
+  // The look-back trusts a tile's inclusive prefix when its flag equals the
+  // running step's epoch. Epochs restart here, so flags left by an earlier
+  // run must go: clear the tile arrays before the first step.
+  h.epoch = 1;
+  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream), "tile reset");
   CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state reset");
   s->step = 0;
   return SAMPO_OK;
@@ -386,7 +403,9 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
   uint32_t done = 0;
   // rows of steps [s->step, s->step + n) are read back in chunks no longer than the ring allows
   const uint32_t chunk_max = s->ring - 1;
+  s->last_run_ms = 0;
   while (done < nsteps) {
+    CK(cudaEventRecord(s->ev[3], s->stream), "event");
     const uint32_t n = std::min(nsteps - done, chunk_max);
     const uint32_t first = s->step;
     if (s->timing) {
@@ -418,6 +437,7 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
         s->launches += 2;
       }
     }
+    CK(cudaEventRecord(s->ev[2], s->stream), "event");
     if (rows) {
       // rows[first .. first+n) live in ring slots first % ring ...
       uint32_t c = 0;
@@ -431,8 +451,40 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
     s->step += n;
     done += n;
     int rc = check_device(s);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev[3], s->ev[2]);
+    s->last_run_ms += ms;
     if (rc) return rc;
   }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_last_run_ms(sampo_sim* s, double* ms) {
+  if (!s || !ms) return SAMPO_ERR_ARG;
+  *ms = s->last_run_ms;
+  return SAMPO_OK;
+}
+
+extern "C" void* sampo_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+  return p;
+}
+
+extern "C" void sampo_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+extern "C" int sampo_flush_l2(sampo_sim* s) {
+  if (!s) return SAMPO_ERR_ARG;
+  cudaSetDevice(s->device);
+  if (!s->flush_buf) {
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->device);
+    s->flush_bytes = std::max<size_t>((size_t)l2 * 2, (size_t)256 << 20);
+    CK(cudaMalloc(&s->flush_buf, s->flush_bytes), "L2 flush buffer");
+  }
+  CK(cudaMemsetAsync(s->flush_buf, (int)(s->launches & 0xff), s->flush_bytes, s->stream), "L2 flush");
   return SAMPO_OK;
 }
 

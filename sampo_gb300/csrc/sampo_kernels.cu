@@ -18,6 +18,12 @@
 //            calcGender.cl). The last CTA to finish publishes the next
 //            population, the stats row and the larval mortality table.
 //
+// Both kernels stream tiles through shared memory with TMA bulk copies
+// (cp.async.bulk + mbarrier, double-buffered: tile j+1 is in flight while
+// tile j is processed). k_count loads only the columns the tile's ranges
+// need; k_scatter reuses the input stage as the output staging area, sorted
+// by next state, and writes each state's run with coalesced stores.
+//
 // This replaces the reference's 19 kernels per step (killAgents,
 // updateAgents, initAgents, 3 x preScan + 3 x Bolt scan-by-key,
 // oldToNewAgents, calcL1de x2, calcFemales x2) and its blocking transfers.
@@ -34,6 +40,12 @@ __device__ const float kDevRates[32] = {
     0.005532729, 0.006054144, 0.006620836, 0.007236393, 0.007904657, 0.008629745, 0.009416051, 0.010267388,
     0.011113704, 0.011960019, 0.012806335, 0.010401163, 0.007995991, 0.00033845, 0.00000533086, 0.0000000840986};
 
+constexpr uint32_t kColBytes = kTile * 4;                    // one 4-byte column of a tile
+constexpr uint32_t kCountStage = 5 * kColBytes + kTile;      // age, his, delay, uni, avail, flags
+constexpr uint32_t kScatterStage = 9 * kColBytes + kTile;    // all nine 4-byte columns, flags
+constexpr uint32_t kWaitLimit = 1u << 22;                    // bounded mbarrier waits
+
+// ---------------- memory-model and TMA helpers ----------------
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -54,6 +66,33 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
+}
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// 1-D bulk copy global -> shared, completion counted on bar (both addresses
+// 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Waits for the phase with the given parity; gives up after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
 }
 
 // Range of slot g in the current layout, -1 for gaps and the tail
@@ -132,41 +171,112 @@ __device__ void load_ctx(const KParams& p, SharedCtx& s) {
 // ------------------------------------------------------------------------
 // Count pass
 // ------------------------------------------------------------------------
+enum : uint32_t { CA_AGE = 1, CA_HIS = 2, CA_DELAY = 4, CA_UNI = 8, CA_AVAIL = 16, CA_FLAGS = 32 };
+
+// Columns the decision part of the update reads, by range (see update_agent<false>).
+__device__ __forceinline__ uint32_t count_cols(int rg, bool larvicide) {
+  switch (rg) {
+    case EGG: case PUPA: return CA_HIS | CA_DELAY;
+    case LARVA: return CA_AGE | CA_UNI | CA_DELAY | (larvicide ? CA_HIS : 0u);
+    case MATESEEKING: return CA_AGE | CA_HIS | CA_DELAY | CA_FLAGS;
+    case GRAVID: return CA_AGE | CA_AVAIL | CA_UNI;
+    default: return CA_AGE | CA_HIS | CA_DELAY;  // IMMATURE, BMS, BMD
+  }
+}
+
+__device__ void issue_count_tile(const DevPool& src, uint8_t* st, uint64_t* bar, const sampo_population& pop,
+                                 uint32_t lo, uint32_t n, bool larvicide) {
+  uint32_t m = 0;
+  for (int k = 0; k < 8; k++)
+    if (pop.r[k].end > pop.r[k].start && pop.r[k].start < lo + n && pop.r[k].end > lo) m |= count_cols(k, larvicide);
+  const uint32_t b4 = (n * 4 + 15) & ~15u, b1 = (n + 15) & ~15u;
+  uint32_t tx = __popc(m & 31u) * b4 + ((m & CA_FLAGS) ? b1 : 0u);
+  mbar_arrive_tx(bar, tx);
+  if (m & CA_AGE) bulk_load(st + 0 * kColBytes, src.age + lo, b4, bar);
+  if (m & CA_HIS) bulk_load(st + 1 * kColBytes, src.his + lo, b4, bar);
+  if (m & CA_DELAY) bulk_load(st + 2 * kColBytes, src.delay + lo, b4, bar);
+  if (m & CA_UNI) bulk_load(st + 3 * kColBytes, src.uni + lo, b4, bar);
+  if (m & CA_AVAIL) bulk_load(st + 4 * kColBytes, src.avail + lo, b4, bar);
+  if (m & CA_FLAGS) bulk_load(st + 5 * kColBytes, src.flags + lo, b1, bar);
+}
+
 __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
+  extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ SharedCtx S;
-  __shared__ uint32_t s_tile;
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t s_tick[2];
   __shared__ uint32_t s_wcnt[kWarps][8];
   load_ctx(p, S);
   const StepCtx& c = S.c;
+  SimDev* sim = p.sim;
   const DevPool src = p.pool[S.cur];
   const uint32_t end = S.pop.r[GRAVID].end;
   const uint32_t ntiles = (end + kTile - 1) / kTile;
+  const bool larvicide = c.env.larvacideValue > 0.0f;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   Acc acc = {0, 0, 0, 0, 0, 0};
   uint32_t cta_cnt = 0;  // thread b < 8: this CTA's survivors of next state b
-  uint32_t devoob = 0;
+  uint32_t devoob = 0, phase = 0, pend = 0;  // pend (thread 0): stages with a copy in flight
+  bool failed = false;
 
-  for (;;) {
-    if (tid == 0) s_tile = atomicAdd(&p.sim->ticket1, 1u);
-    __syncthreads();
-    const uint32_t t = s_tile;
+  if (tid == 0) {
+    mbar_init(&bars[0]);
+    mbar_init(&bars[1]);
+    fence_mbar_init();
+    fence_proxy_async();
+    const uint32_t t = atomicAdd(&sim->ticket1, 1u);
+    s_tick[0] = t;
+    if (t < ntiles) {
+      issue_count_tile(src, dsm, &bars[0], S.pop, t * kTile, min((uint32_t)kTile, end - t * kTile), larvicide);
+      pend |= 1u;
+    }
+  }
+  __syncthreads();
+
+  for (uint32_t it = 0;; it++) {
+    const uint32_t sidx = it & 1u;
+    const uint32_t t = s_tick[sidx];
     if (t >= ntiles) break;
+    uint8_t* st = dsm + sidx * kCountStage;
+    if (tid == 0) {  // prefetch the next tile into the other stage
+      const uint32_t t2 = atomicAdd(&sim->ticket1, 1u);
+      s_tick[sidx ^ 1u] = t2;
+      if (t2 < ntiles) {
+        fence_proxy_async();
+        issue_count_tile(src, dsm + (sidx ^ 1u) * kCountStage, &bars[sidx ^ 1u], S.pop, t2 * kTile,
+                         min((uint32_t)kTile, end - t2 * kTile), larvicide);
+        pend |= 2u >> sidx;
+      }
+    }
+    const bool ok = mbar_wait(&bars[sidx], (phase >> sidx) & 1u);
+    if (ok) {
+      phase ^= 1u << sidx;
+      pend &= ~(1u << sidx);
+    }
+    const uint32_t lo = t * kTile;
+    const float* s_age = (const float*)(st + 0 * kColBytes);
+    const float* s_his = (const float*)(st + 1 * kColBytes);
+    const float* s_delay = (const float*)(st + 2 * kColBytes);
+    const uint32_t* s_uni = (const uint32_t*)(st + 3 * kColBytes);
+    const uint32_t* s_avail = (const uint32_t*)(st + 4 * kColBytes);
+    const uint8_t* s_flags = st + 5 * kColBytes;
     uint32_t pk0 = 0, pk1 = 0;  // 8-bit survivor counters: buckets 0-3, 4-7
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
-      const uint32_t g = t * kTile + k * kBlock + tid;
-      int rg = g < end ? range_of(S.pop, g) : -1;
+      const uint32_t i = k * kBlock + tid;
+      const uint32_t g = lo + i;
+      const int rg = (ok && g < end) ? range_of(S.pop, g) : -1;
       if (rg >= 0) {
         Rec a;
-        a.age = (rg == LARVA || rg >= IMMATURE) ? src.age[g] : 0.0f;
-        a.his = rg != GRAVID ? src.his[g] : 0.0f;
-        a.delay = rg != GRAVID ? src.delay[g] : 0.0f;
-        a.uni = (rg == LARVA || rg == GRAVID) ? src.uni[g] : 0u;
-        a.avail = rg == GRAVID ? src.avail[g] : 0u;
-        a.female = rg == MATESEEKING ? (src.flags[g] >> 3) & 1u : 0u;
+        a.age = (rg == LARVA || rg >= IMMATURE) ? s_age[i] : 0.0f;
+        a.his = (rg != GRAVID && (rg != LARVA || larvicide)) ? s_his[i] : 0.0f;
+        a.delay = rg != GRAVID ? s_delay[i] : 0.0f;
+        a.uni = (rg == LARVA || rg == GRAVID) ? s_uni[i] : 0u;
+        a.avail = rg == GRAVID ? s_avail[i] : 0u;
+        a.female = rg == MATESEEKING ? (s_flags[i] >> 3) & 1u : 0u;
         a.sporo = 0.0f; a.cycle = 0u; a.hbc = 0u; a.batches = 0u;
         devoob |= (rg == LARVA) & c.devOOB;
-        int ns = update_agent<false>(c, rg, g, a, acc);
+        const int ns = update_agent<false>(c, rg, g, a, acc);
         if (ns >= 0) {
           if (ns < 4) pk0 += 1u << (8 * ns);
           else pk1 += 1u << (8 * (ns - 4));
@@ -184,13 +294,18 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
       p.tileAgg[(size_t)t * 8 + tid] = sum;
       cta_cnt += sum;
     }
-    __syncthreads();
+    if (__syncthreads_or(!ok)) { failed = true; break; }
   }
-  if (tid < 8 && cta_cnt) atomicAdd(&p.sim->cnt[tid], cta_cnt);
-  uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
-  if (lane == 0 && ne) atomicAdd(&p.sim->newEggs, ne);
-  uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
-  if (lane == 0 && bad) atomicOr(&p.sim->error, bad);
+  if (failed && tid == 0) {
+    atomicOr(&sim->error, SAMPO_DEV_ERR_TMA);
+    for (int s = 0; s < 2; s++)  // let copies still in flight land before the CTA exits
+      if ((pend >> s) & 1u) (void)mbar_wait(&bars[s], (phase >> s) & 1u);
+  }
+  if (tid < 8 && cta_cnt) atomicAdd(&sim->cnt[tid], cta_cnt);
+  const uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
+  if (lane == 0 && ne) atomicAdd(&sim->newEggs, ne);
+  const uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
+  if (lane == 0 && bad) atomicOr(&sim->error, bad);
 }
 
 // ------------------------------------------------------------------------
@@ -248,12 +363,31 @@ __device__ void publish_start(const KParams& p, const sampo_population& ranges, 
 // ------------------------------------------------------------------------
 // Update + scatter pass
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
+__device__ void issue_scatter_tile(const DevPool& src, uint8_t* st, uint64_t* bar, uint32_t lo, uint32_t n) {
+  const uint32_t b4 = (n * 4 + 15) & ~15u, b1 = (n + 15) & ~15u;
+  mbar_arrive_tx(bar, 9 * b4 + b1);
+  bulk_load(st + 0 * kColBytes, src.age + lo, b4, bar);
+  bulk_load(st + 1 * kColBytes, src.his + lo, b4, bar);
+  bulk_load(st + 2 * kColBytes, src.delay + lo, b4, bar);
+  bulk_load(st + 3 * kColBytes, src.sporo + lo, b4, bar);
+  bulk_load(st + 4 * kColBytes, src.uni + lo, b4, bar);
+  bulk_load(st + 5 * kColBytes, src.avail + lo, b4, bar);
+  bulk_load(st + 6 * kColBytes, src.cycle + lo, b4, bar);
+  bulk_load(st + 7 * kColBytes, src.hbc + lo, b4, bar);
+  bulk_load(st + 8 * kColBytes, src.batches + lo, b4, bar);
+  bulk_load(st + 9 * kColBytes, src.flags + lo, b1, bar);
+}
+
+__global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
+  extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ SharedCtx S;
+  __shared__ __align__(8) uint64_t bars[2];
   __shared__ sampo_population s_np;
-  __shared__ uint32_t s_base[8], s_prefix[8], s_newEggs, s_tile, s_ok, s_last;
+  __shared__ uint32_t s_base[8], s_prefix[8], s_btot[8], s_newEggs, s_ok, s_last, s_tick[2];
   __shared__ uint32_t s_off[kItems][kWarps][8];
   __shared__ uint32_t s_red[kWarps][8];
+  __shared__ uint32_t s_mn[kWarps], s_mx[kWarps];
+  __shared__ uint32_t s_bmq[kTile], s_bmn;  // owed Box-Muller draws: staging slot | item << 10 | kind << 20
   load_ctx(p, S);
   const StepCtx& c = S.c;
   SimDev* sim = p.sim;
@@ -277,18 +411,45 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
   const uint32_t end = S.pop.r[GRAVID].end;
   const uint32_t nold = s_ok ? (end + kTile - 1) / kTile : 0u;
   const uint32_t negg = s_ok ? (s_newEggs + kTile - 1) / kTile : 0u;
+  const uint32_t ntot = nold + negg;
   const uint32_t epoch = S.epoch;
 
   Acc acc = {0, 0, 0, 0, 0, 0};
-  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0;
+  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0, phase = 0, pend = 0;
+  bool failed = false;
 
-  for (;;) {
-    if (tid == 0) s_tile = atomicAdd(&sim->ticket2, 1u);
-    for (int q = tid; q < kItems * kWarps * 8; q += kBlock) (&s_off[0][0][0])[q] = 0u;
-    __syncthreads();
-    const uint32_t t = s_tile;
-    if (t >= nold + negg) break;
+  if (tid == 0) {
+    mbar_init(&bars[0]);
+    mbar_init(&bars[1]);
+    fence_mbar_init();
+    fence_proxy_async();
+    const uint32_t t = atomicAdd(&sim->ticket2, 1u);
+    s_tick[0] = t;
     if (t < nold) {
+      issue_scatter_tile(src, dsm, &bars[0], t * kTile, min((uint32_t)kTile, end - t * kTile));
+      pend |= 1u;
+    }
+  }
+  __syncthreads();
+
+  for (uint32_t it = 0;; it++) {
+    const uint32_t sidx = it & 1u;
+    const uint32_t t = s_tick[sidx];
+    if (t >= ntot) break;
+    uint8_t* st = dsm + sidx * kScatterStage;
+    if (tid == 0) {  // prefetch the next tile into the other stage
+      const uint32_t t2 = atomicAdd(&sim->ticket2, 1u);
+      s_tick[sidx ^ 1u] = t2;
+      if (t2 < nold) {
+        fence_proxy_async();
+        issue_scatter_tile(src, dsm + (sidx ^ 1u) * kScatterStage, &bars[sidx ^ 1u], t2 * kTile, min((uint32_t)kTile, end - t2 * kTile));
+        pend |= 2u >> sidx;
+      }
+    }
+    bool ok = true;
+    if (t < nold) {
+      for (int q = tid; q < kItems * kWarps * 8; q += kBlock) (&s_off[0][0][0])[q] = 0u;
+      if (tid == 0) s_bmn = 0;
       // ---- decoupled look-back over the count pass's tile aggregates ----
       if (warp == 0) {
         uint32_t ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -322,52 +483,95 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
           for (int b = 0; b < 8; b++) s_prefix[b] = ex[b];
         }
       }
-      // ---- recompute the step for the tile's agents ----
+      ok = mbar_wait(&bars[sidx], (phase >> sidx) & 1u);
+      if (ok) {
+        phase ^= 1u << sidx;
+        pend &= ~(1u << sidx);
+      }
+      // ---- recompute the step for the tile's agents (inputs from shared memory) ----
+      float* c_age = (float*)(st + 0 * kColBytes);
+      float* c_his = (float*)(st + 1 * kColBytes);
+      float* c_delay = (float*)(st + 2 * kColBytes);
+      float* c_sporo = (float*)(st + 3 * kColBytes);
+      uint32_t* c_uni = (uint32_t*)(st + 4 * kColBytes);
+      uint32_t* c_avail = (uint32_t*)(st + 5 * kColBytes);
+      uint32_t* c_cycle = (uint32_t*)(st + 6 * kColBytes);
+      uint32_t* c_hbc = (uint32_t*)(st + 7 * kColBytes);
+      uint32_t* c_batches = (uint32_t*)(st + 8 * kColBytes);
+      uint8_t* c_flags = st + 9 * kColBytes;
+      const uint32_t lo = t * kTile;
       Rec a[kItems];
       int nb[kItems];
       uint32_t rk[kItems];
+      __syncthreads();  // s_off cleared
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
-        const uint32_t g = t * kTile + k * kBlock + tid;
-        int rg = g < end ? range_of(S.pop, g) : -1;
+        const uint32_t i = k * kBlock + tid;
+        const uint32_t g = lo + i;
+        const int rg = (ok && g < end) ? range_of(S.pop, g) : -1;
         nb[k] = 8;
+        a[k].bm = BM_NONE;
         if (rg >= 0) {
-          a[k].age = src.age[g]; a[k].his = src.his[g]; a[k].delay = src.delay[g]; a[k].sporo = src.sporo[g];
-          a[k].uni = src.uni[g]; a[k].avail = src.avail[g]; a[k].cycle = src.cycle[g]; a[k].hbc = src.hbc[g];
-          a[k].batches = src.batches[g];
-          a[k].female = (src.flags[g] >> 3) & 1u;
-          int ns = update_agent<true>(c, rg, g, a[k], acc);
+          a[k].age = c_age[i]; a[k].his = c_his[i]; a[k].delay = c_delay[i]; a[k].sporo = c_sporo[i];
+          a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
+          a[k].batches = c_batches[i];
+          a[k].female = (c_flags[i] >> 3) & 1u;
+          const int ns = update_agent<true>(c, rg, g, a[k], acc);
           if (ns >= 0) nb[k] = ns;
         }
         const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
         rk[k] = __popc(peers & lanemask_lt());
         if (nb[k] < 8 && lane == __ffs(peers) - 1) s_off[k][warp][nb[k]] = __popc(peers);
       }
-      __syncthreads();
+      __syncthreads();  // inputs consumed (the stage becomes the output staging area), counts written
       // ---- exclusive scan of the (round, warp) counts, one warp per state ----
       if (warp < 8) {
         const int b = warp;
-        uint32_t v = (&s_off[0][0][0])[lane * 8 + b];  // entry (round, warp) = lane, kItems*kWarps == 32
+        const uint32_t v = (&s_off[0][0][0])[lane * 8 + b];  // entry (round, warp) = lane, kItems*kWarps == 32
         uint32_t incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-          uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
           if (lane >= o) incl += y;
         }
         (&s_off[0][0][0])[lane * 8 + b] = incl - v;
-        if (lane == 31 && incl != p.tileAgg[(size_t)t * 8 + b]) tilebad = 1;
+        if (lane == 31) {
+          s_btot[b] = incl;
+          if (incl != p.tileAgg[(size_t)t * 8 + b]) tilebad = 1;
+        }
       }
       __syncthreads();
-      // ---- write survivors to their new slots ----
+      // start of each state's run in the staging area (indexed with constants only)
+      uint32_t boff[9];
+      boff[0] = 0;
+#pragma unroll
+      for (int b = 0; b < 8; b++) boff[b + 1] = boff[b] + s_btot[b];
+      // ---- survivors into the staging area, sorted by next state ----
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
         const int b = nb[k];
+        uint32_t q = 0xffffffffu;
         if (b < 8) {
-          const uint32_t d = s_base[b] + s_prefix[b] + s_off[k][warp][b] + rk[k];
-          dst.age[d] = a[k].age; dst.his[d] = a[k].his; dst.delay[d] = a[k].delay; dst.sporo[d] = a[k].sporo;
-          dst.uni[d] = a[k].uni; dst.avail[d] = a[k].avail; dst.cycle[d] = a[k].cycle; dst.hbc[d] = a[k].hbc;
-          dst.batches[d] = a[k].batches;
-          dst.flags[d] = (uint8_t)(b | (a[k].female << 3));
+          uint32_t ob = 0;
+#pragma unroll
+          for (int j = 1; j < 8; j++) ob = b >= j ? boff[j] : ob;
+          q = ob + s_off[k][warp][b] + rk[k];
+          if (q >= (uint32_t)kTile) { tilebad = 1; q = 0xffffffffu; }  // never outside the stage
+        }
+        // queue the owed Box-Muller draws (warp-aggregated slot reservation)
+        const bool owe = q != 0xffffffffu && a[k].bm != BM_NONE;
+        const uint32_t om = __ballot_sync(0xffffffffu, owe);
+        if (om) {
+          uint32_t qb = 0;
+          if (lane == __ffs(om) - 1) qb = atomicAdd(&s_bmn, (uint32_t)__popc(om));
+          qb = __shfl_sync(0xffffffffu, qb, __ffs(om) - 1);
+          if (owe) s_bmq[qb + __popc(om & lanemask_lt())] = q | ((uint32_t)(k * kBlock + tid) << 10) | (a[k].bm << 20);
+        }
+        if (q != 0xffffffffu) {
+          c_age[q] = a[k].age; c_his[q] = a[k].his; c_delay[q] = a[k].delay; c_sporo[q] = a[k].sporo;
+          c_uni[q] = a[k].uni; c_avail[q] = a[k].avail; c_cycle[q] = a[k].cycle; c_hbc[q] = a[k].hbc;
+          c_batches[q] = a[k].batches;
+          c_flags[q] = (uint8_t)(b | (a[k].female << 3));
           // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
           if (b == LARVA) {
             l1 += sampo_f2u_sat(a[k].age / 24.0f);
@@ -378,6 +582,37 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
             inf += a[k].sporo >= 1.0f ? 1u : 0u;
           }
         }
+      }
+      __syncthreads();
+      // ---- the owed Box-Muller draws, in dense warps, patched into the staging area ----
+      const uint32_t nbm = s_bmn;
+      if (nbm) {
+        for (uint32_t j = tid; j < nbm; j += kBlock) {
+          const uint32_t e = s_bmq[j];
+          const uint32_t q = e & 1023u, kind = e >> 20;
+          const uint32_t v = finish_box_muller(c, lo + ((e >> 10) & 1023u), kind, c_batches[q]);
+          if (kind == BM_LARVA_DELAY) c_delay[q] = __uint_as_float(v);
+          else c_avail[q] = v;
+        }
+        __syncthreads();
+      }
+      // ---- each state's run to its slots in the next buffer, coalesced ----
+      const uint32_t nout = min(boff[8], (uint32_t)kTile);
+      for (uint32_t q = tid; q < nout; q += kBlock) {
+        int b = 0;
+        uint32_t ob = 0;
+#pragma unroll
+        for (int j = 1; j < 8; j++)
+          if (q >= boff[j]) { b = j; ob = boff[j]; }
+        const uint32_t d = s_base[b] + s_prefix[b] + (q - ob);
+        if (d >= s_np.r[b].end) {  // counts of the two passes disagree: never write out of range
+          tilebad = 1;
+          continue;
+        }
+        dst.age[d] = c_age[q]; dst.his[d] = c_his[q]; dst.delay[d] = c_delay[q]; dst.sporo[d] = c_sporo[q];
+        dst.uni[d] = c_uni[q]; dst.avail[d] = c_avail[q]; dst.cycle[d] = c_cycle[q]; dst.hbc[d] = c_hbc[q];
+        dst.batches[d] = c_batches[q];
+        dst.flags[d] = c_flags[q];
       }
     } else {
       // ---- new eggs at [0, newEggs) of the next buffer ----
@@ -395,7 +630,12 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
         }
       }
     }
-    __syncthreads();
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+  }
+  if (failed && tid == 0) {
+    atomicOr(&sim->error, SAMPO_DEV_ERR_TMA);
+    for (int s = 0; s < 2; s++)  // let copies still in flight land before the CTA exits
+      if ((pend >> s) & 1u) (void)mbar_wait(&bars[s], (phase >> s) & 1u);
   }
 
   // ---- per-CTA reduction of the accumulators, one atomic each ----
@@ -404,13 +644,13 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
                      (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u)};
 #pragma unroll
     for (int j = 0; j < 8; j++) v[j] = j == 7 ? __reduce_or_sync(0xffffffffu, v[j]) : __reduce_add_sync(0xffffffffu, v[j]);
-    uint32_t mn = __reduce_min_sync(0xffffffffu, dmin), mx = __reduce_max_sync(0xffffffffu, dmax);
+    const uint32_t mn = __reduce_min_sync(0xffffffffu, dmin), mx = __reduce_max_sync(0xffffffffu, dmax);
     if (lane == 0) {
 #pragma unroll
       for (int j = 0; j < 8; j++) s_red[warp][j] = v[j];
+      s_mn[warp] = mn;
+      s_mx[warp] = mx;
     }
-    __shared__ uint32_t s_mn[kWarps], s_mx[kWarps];
-    if (lane == 0) { s_mn[warp] = mn; s_mx[warp] = mx; }
     __syncthreads();
     if (tid == 0) {
       uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0}, rmn = 0xffffffffu, rmx = 0;
@@ -446,9 +686,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(KParams p) {
     uint32_t moved = 0;
     for (int k = 1; k < 8; k++) moved += sim->cnt[k];
     if (shared_end && moved) atomicOr(&sim->warn, SAMPO_DEV_WARN_REF_LAYOUT);
-    if (s_ok) {
-      sim->cur = S.cur ^ 1u;
-    }
+    if (s_ok) sim->cur = S.cur ^ 1u;
     sim->step = S.step + 1u;
     sim->epoch = S.epoch + 1u;
     for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
@@ -566,75 +804,6 @@ __global__ void k_histogram(KParams p, uint32_t* hist) {
     if (h[k]) atomicAdd(&hist[k], h[k]);
 }
 
-__global__ void k_pack_flags(KParams p, const uint8_t* state, const uint8_t* female, uint32_t n) {
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x)
-    p.pool[0].flags[g] = (uint8_t)((state[g] & 7u) | ((female[g] ? 1u : 0u) << 3));
-}
-__global__ void k_unpack_flags(KParams p, uint8_t* state, uint8_t* female, uint32_t n) {
-  const DevPool src = p.pool[p.sim->cur];
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
-    uint8_t f = src.flags[g];
-    state[g] = f & 7u;
-    female[g] = (f >> 3) & 1u;
-  }
-}
-
-// ------------------------------------------------------------------------
-static int g_sms = 0;
-static int sm_count() {
-  if (!g_sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sms <= 0) g_sms = 1;
-  }
-  return g_sms;
-}
-int grid_blocks_count() {
-  int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_count, kBlock, 0);
-  return sm_count() * (per > 0 ? per : 1);
-}
-int grid_blocks_scatter() {
-  int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kBlock, 0);
-  return sm_count() * (per > 0 ? per : 1);
-}
-cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
-  k_count<<<grid, kBlock, 0, st>>>(p);
-  return cudaGetLastError();
-}
-cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
-  k_scatter<<<grid, kBlock, 0, st>>>(p);
-  return cudaGetLastError();
-}
-cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev, int age_days_max,
-                             uint64_t age_seed, cudaStream_t st) {
-  int grid = sm_count() * 4;
-  k_init_eggs<<<grid, 256, 0, st>>>(p, n, T0, seeds_dev, age_days_max, age_seed);
-  return cudaGetLastError();
-}
-cudaError_t launch_publish_start(const KParams& p, cudaStream_t st) {
-  k_pool_stats<<<sm_count() * 4, 256, 0, st>>>(p);
-  k_publish_start<<<1, 128, 0, st>>>(p);
-  return cudaGetLastError();
-}
-cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st) {
-  k_histogram<<<sm_count() * 4, 256, 0, st>>>(p, hist_dev);
-  return cudaGetLastError();
-}
-cudaError_t launch_pack_pool(const KParams& p, const uint8_t* state, const uint8_t* female, uint32_t n, cudaStream_t st) {
-  k_pack_flags<<<sm_count() * 4, 256, 0, st>>>(p, state, female, n);
-  return cudaGetLastError();
-}
-cudaError_t launch_unpack_flags(const KParams& p, uint8_t* state, uint8_t* female, uint32_t n, cudaStream_t st) {
-  k_unpack_flags<<<sm_count() * 4, 256, 0, st>>>(p, state, female, n);
-  return cudaGetLastError();
-}
-
-}  // namespace sampo
-
-namespace sampo {
 // Diagnostic: the model's transcendental definitions evaluated on the device.
 __global__ void k_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -649,8 +818,67 @@ __global__ void k_eval_math(int fn, const float* x, const float* y, float* out, 
     out[i] = v;
   }
 }
+
+// ------------------------------------------------------------------------
+static int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+constexpr size_t kCountSmem = 2 * kCountStage;
+constexpr size_t kScatterSmem = 2 * kScatterStage;
+
+static void set_smem_attrs() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCountSmem);
+  cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+  done = true;
+}
+int grid_blocks_count() {
+  set_smem_attrs();
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_count, kBlock, kCountSmem);
+  return sm_count() * (per > 0 ? per : 1);
+}
+int grid_blocks_scatter() {
+  set_smem_attrs();
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kBlock, kScatterSmem);
+  return sm_count() * (per > 0 ? per : 1);
+}
+cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
+  set_smem_attrs();
+  k_count<<<grid, kBlock, kCountSmem, st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
+  set_smem_attrs();
+  k_scatter<<<grid, kBlock, kScatterSmem, st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev, int age_days_max,
+                             uint64_t age_seed, cudaStream_t st) {
+  k_init_eggs<<<sm_count() * 4, 256, 0, st>>>(p, n, T0, seeds_dev, age_days_max, age_seed);
+  return cudaGetLastError();
+}
+cudaError_t launch_publish_start(const KParams& p, cudaStream_t st) {
+  k_pool_stats<<<sm_count() * 4, 256, 0, st>>>(p);
+  k_publish_start<<<1, 128, 0, st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st) {
+  k_histogram<<<sm_count() * 4, 256, 0, st>>>(p, hist_dev);
+  return cudaGetLastError();
+}
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {
   k_eval_math<<<sm_count() * 2, 256, 0, st>>>(fn, x, y, out, n);
   return cudaGetLastError();
 }
+
 }  // namespace sampo

@@ -63,8 +63,6 @@ cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo
                              int age_days_max, uint64_t age_seed, cudaStream_t st);
 cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
-cudaError_t launch_pack_pool(const KParams& p, const uint8_t* state, const uint8_t* female, uint32_t n, cudaStream_t st);
-cudaError_t launch_unpack_flags(const KParams& p, uint8_t* state, uint8_t* female, uint32_t n, cudaStream_t st);
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
 
 }  // namespace sampo

@@ -30,7 +30,14 @@ struct Rec {
   uint32_t uni;      // cumulativeLarvalDelay (float bits) for larvae, ovipositionAttemps for gravids
   uint32_t avail, cycle, hbc, batches;
   uint32_t female;   // 0/1
+  uint32_t bm;       // Box-Muller draw still owed: 0 none, BM_LARVA_DELAY, BM_EGG_BATCH
 };
+
+// The two normal draws of the model (include/gpuRand.h:56-63) cost a binary64
+// log and sin each. They happen on rare transitions, one lane in a warp at a
+// time, so the full update leaves them owed in Rec::bm and the scatter kernel
+// evaluates them afterwards in dense warps (finish_box_muller).
+enum : uint32_t { BM_NONE = 0, BM_LARVA_DELAY = 1, BM_EGG_BATCH = 2 };
 
 // Per-step constants shared by every agent of a step (lives in shared memory).
 struct StepCtx {
@@ -122,7 +129,7 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
       if (a.his >= a.delay) {
         if (FULL) {
           a.age = 24.0f; a.his = 0.0f;
-          a.delay = box_muller(c, gid, 1.0f, 0.1f);  // larvaDelay (include/properties.h:87-91)
+          a.bm = BM_LARVA_DELAY;  // delay = larvaDelay (include/properties.h:87-91), owed
         }
         return LARVA;
       }
@@ -182,11 +189,10 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
       if (a.his >= a.delay) {
         if (FULL) {
           if (a.avail <= 0u && a.female) {
-            // generateEggs (include/properties.h:257-266)
-            uint32_t eggs = sampo_f2u_sat(box_muller(c, gid, 170.0f, 30.0f) + 0.5f);
-            eggs = sampo_f2u_sat((float)eggs * sampo_powf(0.8f, (float)a.batches) + 0.5f);
+            // generateEggs (include/properties.h:257-266): the batch size is
+            // owed; numEggBatches is incremented now, the draw uses the old value
             a.batches += 1u;
-            a.avail = eggs;
+            a.bm = BM_EGG_BATCH;
           }
           a.his = 0.0f; a.uni = 0u;
         }
@@ -224,6 +230,15 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
       return GRAVID;
     }
   }
+}
+
+// The owed draw of an agent at slot gid: larvaDelay (include/properties.h:87-91)
+// returns the new delay bits; generateEggs (:257-266) returns availableEggs,
+// given numEggBatches after its increment.
+__device__ __forceinline__ uint32_t finish_box_muller(const StepCtx& c, uint32_t gid, uint32_t kind, uint32_t batches_after) {
+  if (kind == BM_LARVA_DELAY) return __float_as_uint(box_muller(c, gid, 1.0f, 0.1f));
+  uint32_t eggs = sampo_f2u_sat(box_muller(c, gid, 170.0f, 30.0f) + 0.5f);
+  return sampo_f2u_sat((float)eggs * sampo_powf(0.8f, (float)(batches_after - 1u)) + 0.5f);
 }
 
 // initAgents (kernel/initAgents.cl:34-64) for new slot id.

@@ -65,9 +65,26 @@ DEV_RATES = np.array([0.000175044, 0.000549094, 0.00109031, 0.001494158, 0.00175
                       0.007995991, 0.00033845, 0.00000533086, 0.0000000840986]).astype(np.float32)
 
 
-def make_pool(counts_by_stage, T0: float, seed: int, female_frac: float = 0.5, larva_days: int = 10,
-              adult_days: int = 20, female_split=(0.2, 0.2, 0.2, 0.2, 0.2), male_split=(0.5, 0.5)):
-    """counts_by_stage = (eggs, larvae, pupae, adults). Returns (ranges, arrays)."""
+def larva_stage_hours(T0: float) -> int:
+    """Hours of development until a mean larva (delay 1.0) pupates at T0."""
+    Ti = int(np.clip(np.float32(T0), F(12.0), F(48.0))) - 12
+    return max(24, int(1.0 / float(DEV_RATES[min(Ti, 31)])))
+
+
+# Adult sub-state split near the end of a year-long run of the CPU-runnable
+# workload: females over IMMATURE, MATESEEKING, BMS, BMD, GRAVID; males over
+# IMMATURE, MATESEEKING.
+FEMALE_SPLIT = (0.26, 0.10, 0.04, 0.26, 0.34)
+MALE_SPLIT = (0.26, 0.74)
+
+
+def make_pool(counts_by_stage, T0: float, seed: int, female_frac: float = 0.5, larva_days: int | None = None,
+              adult_days: int = 20, female_split=FEMALE_SPLIT, male_split=MALE_SPLIT):
+    """counts_by_stage = (eggs, larvae, pupae, adults). Returns (ranges, arrays).
+    larva_days=None spreads larval development uniformly over the stage
+    length at T0 (larva_stage_hours)."""
+    if larva_days is None:
+        larva_days = max(1, larva_stage_hours(T0) // 24)
     rng = np.random.default_rng(seed)
     n_egg, n_lar, n_pup, n_ad = (int(c) for c in counts_by_stage)
     female_ad = rng.uniform(size=n_ad) < female_frac
@@ -103,7 +120,7 @@ def make_pool(counts_by_stage, T0: float, seed: int, female_frac: float = 0.5, l
     a["isFemale"][s] = rng.uniform(size=n_egg) < female_frac
     # larvae
     s = sl(1)
-    his = rng.integers(0, 24 * larva_days, n_lar).astype(np.float32)
+    his = rng.integers(0, min(24 * larva_days, larva_stage_hours(T0)), n_lar).astype(np.float32)
     a["hoursInState"][s] = his
     a["ageInHours"][s] = (his + F(24.0)).astype(np.float32)
     dl = np.maximum(rng.normal(1.0, 0.1, n_lar), 0.05).astype(np.float32)

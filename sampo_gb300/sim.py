@@ -99,11 +99,11 @@ class Simulation:
         self.close()
 
     # -- API --
-    def set_inputs(self, T: np.ndarray, env: np.ndarray):
+    def set_inputs(self, T: np.ndarray, env: np.ndarray, first: int = 0):
         T = np.ascontiguousarray(T, dtype=np.float32)
         env = np.ascontiguousarray(env).view(ENV_DTYPE)
         assert len(T) == len(env)
-        self._check(self.lib.sampo_set_inputs(self.h, ptr(T), ptr(env), len(T)))
+        self._check(self.lib.sampo_set_inputs(self.h, first, ptr(T), ptr(env), len(T)))
 
     def set_seeds(self, first: int, seeds: np.ndarray):
         seeds = np.ascontiguousarray(seeds, dtype=np.uint32).reshape(-1, 4, 4)
@@ -167,6 +167,38 @@ class Simulation:
         n = C.c_uint64()
         self._check(self.lib.sampo_kernel_times(self.h, C.byref(t), C.byref(n)))
         return list(t), n.value
+
+    def last_run_ms(self) -> float:
+        v = C.c_double()
+        self._check(self.lib.sampo_last_run_ms(self.h, C.byref(v)))
+        return v.value
+
+    def flush_l2(self):
+        self._check(self.lib.sampo_flush_l2(self.h))
+
+    def run_into(self, nsteps: int, rows_ptr: int):
+        """sampo_run writing rows into caller memory (e.g. page-locked)."""
+        self._check(self.lib.sampo_run(self.h, nsteps, rows_ptr))
+
+
+class PinnedArray:
+    """numpy array over page-locked host memory (sampo_host_alloc)."""
+
+    def __init__(self, shape, dtype):
+        self.lib = _lib.load()
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        self.p = self.lib.sampo_host_alloc(max(n, 1))
+        if not self.p:
+            raise MemoryError("cudaMallocHost failed")
+        buf = (C.c_char * max(n, 1)).from_address(self.p)
+        self.a = np.frombuffer(buf, dtype=np.uint8, count=n).view(dtype).reshape(shape)
+
+    def free(self):
+        if self.p:
+            self.a = None
+            self.lib.sampo_host_free(self.p)
+            self.p = None
 
     @property
     def step_index(self) -> int:

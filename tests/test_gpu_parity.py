@@ -155,6 +155,33 @@ def test_graph_replay_equals_single_launches(gpu_ready, oracle_mod, tmp_path):
     assert hashes[0] == hashes[1]
 
 
+def test_reinitialised_handle_repeats_exactly(gpu_ready, oracle_mod):
+    """Re-initialising one handle (new look-back epochs over tile flags left
+    by the previous run) reproduces the first run bit for bit."""
+    from sampo_gb300 import inputs
+    from sampo_gb300.population import make_pool
+    from sampo_gb300.sim import Simulation, seed_stream
+    n = 240
+    T = np.full(n, 28.0, np.float32)
+    env = np.zeros(n, dtype=inputs.ENV_DTYPE)
+    env["bloodmealSuccess"] = 0.25
+    env["carryingCapacity"] = 12000.0
+    ranges, arrays = make_pool((50000, 50000, 50000, 50000), 28.0, seed=3)
+    init, seeds = seed_stream(3, n)
+    sim = Simulation(capacity=1 << 20, carrying_capacity=12000.0, max_steps=n + 1)
+    sim.set_inputs(T, env)
+    sim.set_seeds(0, seeds)
+    results = []
+    for timing in (False, True, False):
+        sim.load_pool(ranges, arrays)
+        sim.set_timing(timing)
+        rows = sim.run(n)
+        pop, pool = sim.read_pool()
+        results.append((rows.tobytes(), oracle_mod.pool_hash(pop["ranges"], pool)))
+    assert results[0] == results[1] == results[2]
+    sim.close()
+
+
 def test_capacity_exhaustion_is_reported(gpu_ready, tmp_path):
     from sampo_gb300._lib import SampoError
     sim, *_ = _sim_for_case("small_a", tmp_path, 720, capacity=1200)
