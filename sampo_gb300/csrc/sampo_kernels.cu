@@ -42,7 +42,12 @@ __device__ const float kDevRates[32] = {
 
 constexpr uint32_t kColBytes = kTile * 4;                    // one 4-byte column of a tile
 constexpr uint32_t kCountStage = 5 * kColBytes + kTile;      // age, his, delay, uni, avail, flags
-constexpr uint32_t kScatterStage = 9 * kColBytes + kTile;    // all nine 4-byte columns, flags
+// Output staging: each next-state run starts at a staging element with the
+// same residue modulo 16 as its destination slot, so that shared and global
+// addresses of a run agree modulo 16 bytes for every column (the condition
+// for bulk stores); 8 runs add at most 8 x 30 elements of padding.
+constexpr uint32_t kStg = kTile + 256;                       // staging elements per column
+constexpr uint32_t kScatterStage = 9 * kStg * 4 + kStg;      // >= the input layout (9 x kColBytes + kTile)
 constexpr uint32_t kWaitLimit = 1u << 22;                    // bounded mbarrier waits
 
 // ---------------- memory-model and TMA helpers ----------------
@@ -94,6 +99,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// 1-D bulk copy shared -> global in the issuing thread's bulk group (both
+// addresses 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the shared-memory sources of this thread's bulk stores may be overwritten
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// this thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Range of slot g in the current layout, -1 for gaps and the tail
 // (the validity test of every reference kernel, e.g. kernel/killAgents.cl:28-35).
@@ -383,7 +399,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
   __shared__ SharedCtx S;
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ sampo_population s_np;
-  __shared__ uint32_t s_base[8], s_prefix[8], s_btot[8], s_newEggs, s_ok, s_last, s_tick[2];
+  __shared__ uint32_t s_base[8], s_newEggs, s_ok, s_last, s_tick[2];
+  __shared__ uint32_t s_d0[8], s_sb[8], s_cnt[8];  // per next state: first destination slot, staging start, survivors
   __shared__ uint32_t s_off[kItems][kWarps][8];
   __shared__ uint32_t s_red[kWarps][8];
   __shared__ uint32_t s_mn[kWarps], s_mx[kWarps];
@@ -438,6 +455,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
     if (t >= ntot) break;
     uint8_t* st = dsm + sidx * kScatterStage;
     if (tid == 0) {  // prefetch the next tile into the other stage
+      bulk_wait_read();  // ... once the previous tile's bulk stores have read it
       const uint32_t t2 = atomicAdd(&sim->ticket2, 1u);
       s_tick[sidx ^ 1u] = t2;
       if (t2 < nold) {
@@ -479,8 +497,17 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
           st_cg_v4(p.tileIncl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
           st_cg_v4(p.tileIncl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
           st_release_u32(&p.tileFlag[t], epoch);
+          const uint32_t cnt[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+          uint32_t pos = 0;
 #pragma unroll
-          for (int b = 0; b < 8; b++) s_prefix[b] = ex[b];
+          for (int b = 0; b < 8; b++) {
+            const uint32_t d0 = s_base[b] + ex[b];
+            const uint32_t sb = ((pos + 15u) & ~15u) + (d0 & 15u);
+            s_d0[b] = d0;
+            s_sb[b] = sb;
+            s_cnt[b] = cnt[b];
+            pos = sb + cnt[b];
+          }
         }
       }
       ok = mbar_wait(&bars[sidx], (phase >> sidx) & 1u);
@@ -535,28 +562,29 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
           if (lane >= o) incl += y;
         }
         (&s_off[0][0][0])[lane * 8 + b] = incl - v;
-        if (lane == 31) {
-          s_btot[b] = incl;
-          if (incl != p.tileAgg[(size_t)t * 8 + b]) tilebad = 1;
-        }
+        if (lane == 31 && incl != p.tileAgg[(size_t)t * 8 + b]) tilebad = 1;
       }
       __syncthreads();
-      // start of each state's run in the staging area (indexed with constants only)
-      uint32_t boff[9];
-      boff[0] = 0;
-#pragma unroll
-      for (int b = 0; b < 8; b++) boff[b + 1] = boff[b] + s_btot[b];
+      // staging view of the stage: columns kStg elements apart
+      float* g_age = (float*)(st + 0 * kStg * 4);
+      float* g_his = (float*)(st + 1 * kStg * 4);
+      float* g_delay = (float*)(st + 2 * kStg * 4);
+      float* g_sporo = (float*)(st + 3 * kStg * 4);
+      uint32_t* g_uni = (uint32_t*)(st + 4 * kStg * 4);
+      uint32_t* g_avail = (uint32_t*)(st + 5 * kStg * 4);
+      uint32_t* g_cycle = (uint32_t*)(st + 6 * kStg * 4);
+      uint32_t* g_hbc = (uint32_t*)(st + 7 * kStg * 4);
+      uint32_t* g_batches = (uint32_t*)(st + 8 * kStg * 4);
+      uint8_t* g_flags = st + 9 * kStg * 4;
       // ---- survivors into the staging area, sorted by next state ----
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
         const int b = nb[k];
         uint32_t q = 0xffffffffu;
         if (b < 8) {
-          uint32_t ob = 0;
-#pragma unroll
-          for (int j = 1; j < 8; j++) ob = b >= j ? boff[j] : ob;
-          q = ob + s_off[k][warp][b] + rk[k];
-          if (q >= (uint32_t)kTile) { tilebad = 1; q = 0xffffffffu; }  // never outside the stage
+          const uint32_t j = s_off[k][warp][b] + rk[k];
+          if (j < s_cnt[b]) q = s_sb[b] + j;
+          else tilebad = 1;  // the two passes disagree: stay inside this state's run
         }
         // queue the owed Box-Muller draws (warp-aggregated slot reservation)
         const bool owe = q != 0xffffffffu && a[k].bm != BM_NONE;
@@ -565,13 +593,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
           uint32_t qb = 0;
           if (lane == __ffs(om) - 1) qb = atomicAdd(&s_bmn, (uint32_t)__popc(om));
           qb = __shfl_sync(0xffffffffu, qb, __ffs(om) - 1);
-          if (owe) s_bmq[qb + __popc(om & lanemask_lt())] = q | ((uint32_t)(k * kBlock + tid) << 10) | (a[k].bm << 20);
+          if (owe) s_bmq[qb + __popc(om & lanemask_lt())] = q | ((uint32_t)(k * kBlock + tid) << 11) | (a[k].bm << 21);
         }
         if (q != 0xffffffffu) {
-          c_age[q] = a[k].age; c_his[q] = a[k].his; c_delay[q] = a[k].delay; c_sporo[q] = a[k].sporo;
-          c_uni[q] = a[k].uni; c_avail[q] = a[k].avail; c_cycle[q] = a[k].cycle; c_hbc[q] = a[k].hbc;
-          c_batches[q] = a[k].batches;
-          c_flags[q] = (uint8_t)(b | (a[k].female << 3));
+          g_age[q] = a[k].age; g_his[q] = a[k].his; g_delay[q] = a[k].delay; g_sporo[q] = a[k].sporo;
+          g_uni[q] = a[k].uni; g_avail[q] = a[k].avail; g_cycle[q] = a[k].cycle; g_hbc[q] = a[k].hbc;
+          g_batches[q] = a[k].batches;
+          g_flags[q] = (uint8_t)(b | (a[k].female << 3));
           // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
           if (b == LARVA) {
             l1 += sampo_f2u_sat(a[k].age / 24.0f);
@@ -589,30 +617,55 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
       if (nbm) {
         for (uint32_t j = tid; j < nbm; j += kBlock) {
           const uint32_t e = s_bmq[j];
-          const uint32_t q = e & 1023u, kind = e >> 20;
-          const uint32_t v = finish_box_muller(c, lo + ((e >> 10) & 1023u), kind, c_batches[q]);
-          if (kind == BM_LARVA_DELAY) c_delay[q] = __uint_as_float(v);
-          else c_avail[q] = v;
+          const uint32_t q = e & 2047u, kind = e >> 21;
+          const uint32_t v = finish_box_muller(c, lo + ((e >> 11) & 1023u), kind, g_batches[q]);
+          if (kind == BM_LARVA_DELAY) g_delay[q] = __uint_as_float(v);
+          else g_avail[q] = v;
         }
         __syncthreads();
       }
-      // ---- each state's run to its slots in the next buffer, coalesced ----
-      const uint32_t nout = min(boff[8], (uint32_t)kTile);
-      for (uint32_t q = tid; q < nout; q += kBlock) {
-        int b = 0;
-        uint32_t ob = 0;
-#pragma unroll
-        for (int j = 1; j < 8; j++)
-          if (q >= boff[j]) { b = j; ob = boff[j]; }
-        const uint32_t d = s_base[b] + s_prefix[b] + (q - ob);
-        if (d >= s_np.r[b].end) {  // counts of the two passes disagree: never write out of range
-          tilebad = 1;
-          continue;
+      // ---- each state's run to its slots in the next buffer ----
+      // Staging and destination agree modulo 16 bytes, so the aligned body
+      // of every run and column leaves with one bulk store (thread 0); the
+      // unaligned head and tail elements go with plain stores. Runs are
+      // inside the next layout by construction: d0 + count <= range end.
+      if (tid == 0) {
+        fence_proxy_async();  // staging written through the generic proxy
+#pragma unroll 1
+        for (int b = 0; b < 8; b++) {
+          const uint32_t n = s_cnt[b], d0 = s_d0[b], sb = s_sb[b];
+          if (!n) continue;
+          const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
+          if (n4) {
+            const uint32_t o = h4, by = n4 * 4;
+            bulk_store(dst.age + d0 + o, g_age + sb + o, by); bulk_store(dst.his + d0 + o, g_his + sb + o, by);
+            bulk_store(dst.delay + d0 + o, g_delay + sb + o, by); bulk_store(dst.sporo + d0 + o, g_sporo + sb + o, by);
+            bulk_store(dst.uni + d0 + o, g_uni + sb + o, by); bulk_store(dst.avail + d0 + o, g_avail + sb + o, by);
+            bulk_store(dst.cycle + d0 + o, g_cycle + sb + o, by); bulk_store(dst.hbc + d0 + o, g_hbc + sb + o, by);
+            bulk_store(dst.batches + d0 + o, g_batches + sb + o, by);
+          }
+          const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
+          if (n1) bulk_store(dst.flags + d0 + h1, g_flags + sb + h1, n1);
         }
-        dst.age[d] = c_age[q]; dst.his[d] = c_his[q]; dst.delay[d] = c_delay[q]; dst.sporo[d] = c_sporo[q];
-        dst.uni[d] = c_uni[q]; dst.avail[d] = c_avail[q]; dst.cycle[d] = c_cycle[q]; dst.hbc[d] = c_hbc[q];
-        dst.batches[d] = c_batches[q];
-        dst.flags[d] = c_flags[q];
+        bulk_commit();
+      }
+      // heads and tails: per state at most 15 + 15 flag elements, of which the
+      // four-byte columns need at most 3 + 3
+      {
+        const int b = tid >> 5, e = tid & 31;
+        const uint32_t n = s_cnt[b], d0 = s_d0[b], sb = s_sb[b];
+        const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
+        const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
+        const uint32_t j = (uint32_t)e < h1 ? (uint32_t)e : h1 + n1 + ((uint32_t)e - h1);
+        if (e < 30 && j < n) {
+          const uint32_t q = sb + j, d = d0 + j;
+          dst.flags[d] = g_flags[q];
+          if (j < h4 || j >= h4 + n4) {
+            dst.age[d] = g_age[q]; dst.his[d] = g_his[q]; dst.delay[d] = g_delay[q]; dst.sporo[d] = g_sporo[q];
+            dst.uni[d] = g_uni[q]; dst.avail[d] = g_avail[q]; dst.cycle[d] = g_cycle[q]; dst.hbc[d] = g_hbc[q];
+            dst.batches[d] = g_batches[q];
+          }
+        }
       }
     } else {
       // ---- new eggs at [0, newEggs) of the next buffer ----
@@ -637,6 +690,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
     for (int s = 0; s < 2; s++)  // let copies still in flight land before the CTA exits
       if ((pend >> s) & 1u) (void)mbar_wait(&bars[s], (phase >> s) & 1u);
   }
+  if (tid == 0) bulk_wait_all();  // this CTA's bulk stores are complete
 
   // ---- per-CTA reduction of the accumulators, one atomic each ----
   {
