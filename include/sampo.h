@@ -183,6 +183,40 @@ void sampo_rand_seeds(sampo_rand_state* st, sampo_seeds* out, uint32_t nsteps);
 int sampo_read_temperature_file(const char* path, float* out, uint32_t nsteps);
 int sampo_read_environment_file(const char* path, sampo_environment* out, uint32_t nsteps, float carrying_capacity);
 
+/* ---- one step without any device allocation ----
+ * No counterpart in the reference. For callers that cannot call cudaMalloc:
+ * code running where allocation is forbidden or unsafe (inside another
+ * framework's memory pool or arena, a host that must not grow device memory
+ * after start-up, a memory-capped sandbox). They bring their own pool
+ * buffers; the step's scratch (step state, look-back tile counts, one step
+ * of inputs and stats) lives in a fixed array inside the library, sized for
+ * pools of up to SAMPO_NOALLOC_MAX_SLOTS slots (about 1.1 MB, held by every
+ * GPU that loads the library until the process exits).
+ *
+ * in/out: device columns of two pool buffers; each column 16-byte aligned
+ * with 16 bytes of slack after capacity elements; flags = state |
+ * isFemale << 3. pop_in: ranges of `in` (stats are recomputed). Writes the
+ * next pool into `out`; *row = stats at the start of the step (bnc zero),
+ * *pop_out = ranges and stats of `out`, *bnc_out = this step's counters.
+ * Capacities above SAMPO_NOALLOC_MAX_SLOTS return SAMPO_ERR_ARG.
+ * The first call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array and it keeps the last call's contents:
+ * calls that overlap on the GPU (other threads, other streams) race. The
+ * call is synchronous on `stream` (NULL = the default stream). */
+#define SAMPO_NOALLOC_MAX_SLOTS (1u << 24)
+typedef struct {
+  float* ageInHours; float* hoursInState; float* delay; float* cumulativeSporogonicDevelopment;
+  uint32_t* larvalDelayOrOviAttempts; uint32_t* availableEggs; uint32_t* cycleLength;
+  uint32_t* humanBloodmealCount; uint32_t* numEggBatches;
+  uint8_t* flags;
+} sampo_device_pool;
+int sampo_step_noalloc(const sampo_device_pool* in, uint32_t in_capacity, const sampo_device_pool* out,
+                       uint32_t out_capacity, const sampo_population* pop_in, const sampo_environment* env,
+                       float temperature, uint32_t world_time, const sampo_seeds seeds[4], float carrying_capacity,
+                       sampo_stats_row* row, sampo_population* pop_out, sampo_bites_cycles* bnc_out, int device,
+                       void* stream);
+
 /* Diagnostic: evaluates the model's deterministic transcendentals on the
  * device (fn 0 exp(x), 1 log(x), 2 sin(x), 3 pow(x, y)); they must equal the
  * host definitions bit for bit. No counterpart in the reference, whose

@@ -65,6 +65,14 @@ class RandState(C.Structure):
     _fields_ = [("r", C.c_uint32 * 31), ("i", C.c_uint32)]
 
 
+class DevicePool(C.Structure):
+    """sampo_device_pool: device addresses of one caller-owned pool buffer."""
+    _fields_ = [("ageInHours", C.c_void_p), ("hoursInState", C.c_void_p), ("delay", C.c_void_p),
+                ("cumulativeSporogonicDevelopment", C.c_void_p), ("larvalDelayOrOviAttempts", C.c_void_p),
+                ("availableEggs", C.c_void_p), ("cycleLength", C.c_void_p), ("humanBloodmealCount", C.c_void_p),
+                ("numEggBatches", C.c_void_p), ("flags", C.c_void_p)]
+
+
 # numpy views of the same layouts
 ROW_DTYPE = np.dtype([("ranges", "<u4", (8, 2)), ("L1de", "<u4"), ("numFemale", "<u4"), ("numPotInf", "<u4"),
                       ("numCycles", "<u4"), ("sumCycles", "<u4"), ("numBites", "<u4"), ("numInfectBites", "<u4")])
@@ -109,6 +117,10 @@ SIGNATURES = {
     "sampo_host_alloc": (_P, [C.c_size_t]),
     "sampo_host_free": (None, [_P]),
     "sampo_flush_l2": (C.c_int, [_P]),
+    "sampo_step_noalloc": (C.c_int, [C.POINTER(DevicePool), C.c_uint32, C.POINTER(DevicePool), C.c_uint32,
+                                     C.POINTER(Population), C.POINTER(Environment), C.c_float, C.c_uint32, _P,
+                                     C.c_float, C.POINTER(StatsRow), C.POINTER(Population), C.POINTER(BitesCycles),
+                                     C.c_int, _P]),
 }
 
 _lib = None

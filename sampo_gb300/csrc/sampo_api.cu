@@ -88,24 +88,6 @@ static KParams make_params(sampo_sim* s) {
   return p;
 }
 
-// Hourly mortality tables that do not change during a run
-// (kernel/killAgents.cl:84-115,135-147), computed on the host with the same
-// deterministic functions the device uses.
-static void fill_constant_tables(SimDev& h) {
-  for (int d = 0; d < 100; d++) {
-    const float a = 0.1f, B = 25.0f, sg = 0.1f;
-    float e = sampo_expf((float)(uint32_t)d / B);
-    float dmr = (a * e) / (1.0f + (a * B * sg * (e - 1.0f)));
-    float dsr = 1.0f - dmr;
-    float hsr = sampo_powf(dsr, 1.0f / 24.0f);
-    h.adultHMR[d] = 1.0f - hsr;
-    h.larvaHMR[d] = SAMPO_NAN_F;
-  }
-  float dmr = 0.1f;
-  float dsr = 1.0f - dmr;
-  h.aquaticHMR = 1.0f - sampo_powf(dsr, 1.0f / 24.0f);
-}
-
 extern "C" int sampo_abi_version(void) { return SAMPO_ABI_VERSION; }
 
 extern "C" const char* sampo_last_error(const sampo_sim* s) { return s ? s->err.c_str() : "null handle"; }

@@ -2,6 +2,7 @@
 #pragma once
 #include <stdint.h>
 #include "../../include/sampo.h"
+#include "sampo_math.h"
 
 namespace sampo {
 
@@ -53,6 +54,24 @@ struct KParams {
   uint32_t ring;
   uint32_t maxTiles;
 };
+
+// Hourly mortality tables that do not change during a run
+// (kernel/killAgents.cl:84-115,135-147), computed on the host with the same
+// deterministic functions the device uses.
+inline void fill_constant_tables(SimDev& h) {
+  for (int d = 0; d < 100; d++) {
+    const float a = 0.1f, B = 25.0f, sg = 0.1f;
+    float e = sampo_expf((float)(uint32_t)d / B);
+    float dmr = (a * e) / (1.0f + (a * B * sg * (e - 1.0f)));
+    float dsr = 1.0f - dmr;
+    float hsr = sampo_powf(dsr, 1.0f / 24.0f);
+    h.adultHMR[d] = 1.0f - hsr;
+    h.larvaHMR[d] = SAMPO_NAN_F;
+  }
+  float dmr = 0.1f;
+  float dsr = 1.0f - dmr;
+  h.aquaticHMR = 1.0f - sampo_powf(dsr, 1.0f / 24.0f);
+}
 
 // Launch helpers (sampo_kernels.cu).
 int grid_blocks_count();

@@ -1,0 +1,166 @@
+// sampo_noalloc.cu - one hourly step for callers that cannot allocate device
+// memory (see sampo_step_noalloc in include/sampo.h).
+//
+// The caller owns both pool buffers. Everything else the step needs - the
+// device step state, the per-tile survivor counts and look-back prefixes,
+// one step of inputs and two stats rows - lives in g_noalloc_scratch, a
+// fixed file-scope device array sized for pools of up to
+// SAMPO_NOALLOC_MAX_SLOTS slots. The kernels are the ones sampo_step runs;
+// only where their scratch lives differs. Nothing here calls cudaMalloc,
+// cudaFree or any routine that allocates device memory.
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <string.h>
+#include <mutex>
+#include "sampo_model.cuh"
+#include "sampo_kernels.cuh"
+
+using namespace sampo;
+
+namespace {
+
+constexpr uint32_t kMaxTiles = SAMPO_NOALLOC_MAX_SLOTS / kTile;
+
+// One step of inputs (ring of two, as the kernels index step % ring).
+struct InputBlock {
+  float T[2];
+  uint32_t wt[2];
+  sampo_environment env[2];
+  sampo_seeds seeds[8];
+};
+
+struct Scratch {
+  uint32_t tiles[kMaxTiles * 17];  // survivor counts [8] | inclusive prefixes [8] | epoch flag, per tile
+  SimDev sim;
+  sampo_stats_row rows[2];
+  InputBlock in;
+};
+
+}  // namespace
+
+// Held by every GPU that loads the library, until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(Scratch)];
+
+// The array's device address, resolved once per device with that device
+// current. In host code g_noalloc_scratch names a host-side stand-in, never
+// a device address, so kernels only ever receive the resolved pointer.
+static std::mutex g_scratch_mutex;
+static unsigned char* g_scratch_addr[64];
+
+static cudaError_t scratch_address(int device, unsigned char** out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+  if (!g_scratch_addr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_addr[device] = (unsigned char*)p;
+  }
+  *out = g_scratch_addr[device];
+  return cudaSuccess;
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+static bool pool_ok(const sampo_device_pool* d) {
+  return aligned16(d->ageInHours) && aligned16(d->hoursInState) && aligned16(d->delay) &&
+         aligned16(d->cumulativeSporogonicDevelopment) && aligned16(d->larvalDelayOrOviAttempts) &&
+         aligned16(d->availableEggs) && aligned16(d->cycleLength) && aligned16(d->humanBloodmealCount) &&
+         aligned16(d->numEggBatches) && aligned16(d->flags) && d->ageInHours && d->flags;
+}
+
+static DevPool to_dev(const sampo_device_pool* d) {
+  DevPool p;
+  p.age = d->ageInHours; p.his = d->hoursInState; p.delay = d->delay; p.sporo = d->cumulativeSporogonicDevelopment;
+  p.uni = d->larvalDelayOrOviAttempts; p.avail = d->availableEggs; p.cycle = d->cycleLength;
+  p.hbc = d->humanBloodmealCount; p.batches = d->numEggBatches; p.flags = d->flags;
+  return p;
+}
+
+static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sampo_device_pool* out, uint32_t out_capacity,
+                    const sampo_population* pop_in, const sampo_environment* env, float temperature, uint32_t world_time,
+                    const sampo_seeds seeds[4], float cc, sampo_stats_row* row, sampo_population* pop_out,
+                    sampo_bites_cycles* bnc_out, int device, cudaStream_t st) {
+  unsigned char* base = nullptr;
+  if (scratch_address(device, &base) != cudaSuccess) return SAMPO_ERR_CUDA;
+  Scratch* sc = (Scratch*)base;
+
+  SimDev h;
+  memset(&h, 0, sizeof(h));
+  fill_constant_tables(h);
+  h.pop = *pop_in;
+  h.pop.numLarvae1DayEquiv = h.pop.numFemale = h.pop.numPotentiallyInfective = 0;
+  h.capacity = out_capacity;
+  h.cc = cc;
+  h.acc_dmin = 0xffffffffu;
+  h.epoch = 1;
+  InputBlock ib;
+  memset(&ib, 0, sizeof(ib));
+  ib.T[0] = temperature;
+  ib.wt[0] = world_time;
+  ib.env[0] = *env;
+  for (int k = 0; k < 4; k++) ib.seeds[k] = seeds[k];
+
+  // The array keeps the previous call's contents: reset the state, and clear
+  // the epoch flags of the tiles this step uses (a stale flag equal to this
+  // step's epoch would be taken for a published prefix).
+  const uint32_t ntiles = (pop_in->r[7].end + kTile - 1) / kTile;
+  if (cudaMemcpyAsync(&sc->sim, &h, sizeof(h), cudaMemcpyHostToDevice, st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (cudaMemcpyAsync(&sc->in, &ib, sizeof(ib), cudaMemcpyHostToDevice, st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (ntiles && cudaMemsetAsync(sc->tiles + (size_t)kMaxTiles * 16, 0, (size_t)ntiles * 4, st) != cudaSuccess)
+    return SAMPO_ERR_CUDA;
+
+  KParams p;
+  p.sim = &sc->sim;
+  p.pool[0] = to_dev(in);
+  p.pool[1] = to_dev(out);
+  p.tileAgg = sc->tiles;
+  p.tileIncl = sc->tiles + (size_t)kMaxTiles * 8;
+  p.tileFlag = sc->tiles + (size_t)kMaxTiles * 16;
+  p.T = sc->in.T;
+  p.env = sc->in.env;
+  p.seeds = sc->in.seeds;
+  p.wt = sc->in.wt;
+  p.rows = sc->rows;
+  p.ring = 2;
+  p.maxTiles = kMaxTiles;
+  if (launch_publish_start(p, st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (launch_count(p, grid_blocks_count(), st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (launch_scatter(p, grid_blocks_scatter(), st) != cudaSuccess) return SAMPO_ERR_CUDA;
+
+  uint32_t err = 0;
+  if (cudaMemcpyAsync(row, &sc->rows[0], sizeof(*row), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(pop_out, &sc->sim.pop, sizeof(*pop_out), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(bnc_out, &sc->sim.bnc, sizeof(*bnc_out), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&err, &sc->sim.error, sizeof(err), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return SAMPO_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (err & SAMPO_DEV_ERR_CAPACITY) return SAMPO_ERR_CAPACITY;
+  if (err & SAMPO_DEV_ERR_DEVRATES) return SAMPO_ERR_TEMPERATURE;
+  if (err) return SAMPO_ERR_INTERNAL;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_step_noalloc(const sampo_device_pool* in, uint32_t in_capacity, const sampo_device_pool* out,
+                                  uint32_t out_capacity, const sampo_population* pop_in, const sampo_environment* env,
+                                  float temperature, uint32_t world_time, const sampo_seeds seeds[4], float carrying_capacity,
+                                  sampo_stats_row* row, sampo_population* pop_out, sampo_bites_cycles* bnc_out, int device,
+                                  void* stream) {
+  if (!in || !out || !pop_in || !env || !seeds || !row || !pop_out || !bnc_out) return SAMPO_ERR_ARG;
+  if (in_capacity > SAMPO_NOALLOC_MAX_SLOTS || out_capacity > SAMPO_NOALLOC_MAX_SLOTS || out_capacity < 128)
+    return SAMPO_ERR_ARG;  // the fixed scratch covers pools of up to SAMPO_NOALLOC_MAX_SLOTS slots
+  if (!(carrying_capacity > 0.0f) || env->carryingCapacity != carrying_capacity) return SAMPO_ERR_ARG;
+  if (pop_in->r[0].start != 0 || pop_in->r[7].end > in_capacity) return SAMPO_ERR_ARG;
+  for (int k = 0; k < 8; k++) {
+    if (pop_in->r[k].end < pop_in->r[k].start) return SAMPO_ERR_ARG;
+    if (k > 0 && pop_in->r[k].start <= pop_in->r[k - 1].end) return SAMPO_ERR_ARG;
+  }
+  if (!pool_ok(in) || !pool_ok(out)) return SAMPO_ERR_ARG;
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return SAMPO_ERR_CUDA;
+  const int rc = run_step(in, in_capacity, out, out_capacity, pop_in, env, temperature, world_time, seeds,
+                          carrying_capacity, row, pop_out, bnc_out, device, (cudaStream_t)stream);
+  cudaSetDevice(prev);
+  return rc;
+}
