@@ -394,17 +394,72 @@ __device__ void issue_scatter_tile(const DevPool& src, uint8_t* st, uint64_t* ba
   bulk_load(st + 9 * kColBytes, src.flags + lo, b1, bar);
 }
 
-__global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
+// Decoupled look-back for tile t by one warp over the count pass's tile
+// aggregates: sums earlier tiles' aggregates back to the nearest published
+// inclusive prefix (no waiting). Lane 0 publishes t's inclusive prefix.
+// Every lane returns the exclusive prefix ex[] and t's counts cnt[].
+__device__ void tile_lookback(const KParams& p, uint32_t t, uint32_t epoch, int lane, uint32_t ex[8], uint32_t cnt[8]) {
+#pragma unroll
+  for (int b = 0; b < 8; b++) ex[b] = 0;
+  int64_t pos = (int64_t)t - 1;
+  while (pos >= 0) {
+    const int64_t idx = pos - lane;
+    const bool valid = idx >= 0;
+    const uint32_t f = valid ? ld_acquire_u32(&p.tileFlag[idx]) : 0u;
+    const uint32_t m = __ballot_sync(0xffffffffu, !valid || f == epoch);
+    const int stop = m ? __ffs(m) - 1 : 32;
+    uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
+    if (valid && lane <= stop) {
+      const uint32_t* q = (lane == stop ? p.tileIncl : p.tileAgg) + (size_t)idx * 8;
+      v0 = ld_cg_v4(q);
+      v1 = ld_cg_v4(q + 4);
+    }
+    ex[0] += __reduce_add_sync(0xffffffffu, v0.x); ex[1] += __reduce_add_sync(0xffffffffu, v0.y);
+    ex[2] += __reduce_add_sync(0xffffffffu, v0.z); ex[3] += __reduce_add_sync(0xffffffffu, v0.w);
+    ex[4] += __reduce_add_sync(0xffffffffu, v1.x); ex[5] += __reduce_add_sync(0xffffffffu, v1.y);
+    ex[6] += __reduce_add_sync(0xffffffffu, v1.z); ex[7] += __reduce_add_sync(0xffffffffu, v1.w);
+    if (m) break;
+    pos -= 32;
+  }
+  const uint32_t* ag = p.tileAgg + (size_t)t * 8;
+  const uint4 a0 = ld_cg_v4(ag), a1 = ld_cg_v4(ag + 4);
+  cnt[0] = a0.x; cnt[1] = a0.y; cnt[2] = a0.z; cnt[3] = a0.w; cnt[4] = a1.x; cnt[5] = a1.y; cnt[6] = a1.z; cnt[7] = a1.w;
+  if (lane == 0) {
+    st_cg_v4(p.tileIncl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
+    st_cg_v4(p.tileIncl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
+    st_release_u32(&p.tileFlag[t], epoch);
+  }
+}
+
+// Named barrier of the eight consumer warps (the producer warp is not in it).
+__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ void mbar_init_count(uint64_t* bar, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one producer warp
+static_assert(kBlock == 256, "consumer_sync() names 256 threads");
+enum : uint32_t { TK_OLD = 0, TK_EGG = 1, TK_END = 2 };
+
+// The producer warp keeps two tiles in flight ahead of the consumers: it
+// takes tickets, issues the TMA loads, runs the look-back and lays out the
+// staging runs (full[s]: its expect-tx arrival + one arrival once the layout
+// is written); after the consumers have staged a tile (empty[s]: 256
+// arrivals) it sends the runs with bulk stores and refills the stage.
+__global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ SharedCtx S;
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) uint64_t full[2], empty[2];
   __shared__ sampo_population s_np;
-  __shared__ uint32_t s_base[8], s_newEggs, s_ok, s_last, s_tick[2];
-  __shared__ uint32_t s_d0[8], s_sb[8], s_cnt[8];  // per next state: first destination slot, staging start, survivors
+  __shared__ uint32_t s_base[8], s_newEggs, s_ok, s_last, s_tick[2], s_fullok[2];
+  __shared__ uint32_t s_d0[2][8], s_sb[2][8], s_cnt[2][8];  // per stage and next state: first slot, staging start, survivors
   __shared__ uint32_t s_off[kItems][kWarps][8];
   __shared__ uint32_t s_red[kWarps][8];
   __shared__ uint32_t s_mn[kWarps], s_mx[kWarps];
-  __shared__ uint32_t s_bmq[kTile], s_bmn;  // owed Box-Muller draws: staging slot | item << 10 | kind << 20
+  __shared__ uint32_t s_bmq[kTile], s_bmn;  // owed Box-Muller draws: staging slot | item << 11 | kind << 21
   load_ctx(p, S);
   const StepCtx& c = S.c;
   SimDev* sim = p.sim;
@@ -421,6 +476,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
     ok = ok && e <= (uint64_t)sim->capacity;
     s_ok = ok;
     if (!ok && blockIdx.x == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
+    mbar_init_count(&full[0], 2);
+    mbar_init_count(&full[1], 2);
+    mbar_init_count(&empty[0], kBlock);
+    mbar_init_count(&empty[1], kBlock);
+    fence_mbar_init();
   }
   __syncthreads();
   const DevPool src = p.pool[S.cur];
@@ -432,265 +492,257 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
   const uint32_t epoch = S.epoch;
 
   Acc acc = {0, 0, 0, 0, 0, 0};
-  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0, phase = 0, pend = 0;
-  bool failed = false;
+  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0, fail = 0;
 
-  if (tid == 0) {
-    mbar_init(&bars[0]);
-    mbar_init(&bars[1]);
-    fence_mbar_init();
-    fence_proxy_async();
-    const uint32_t t = atomicAdd(&sim->ticket2, 1u);
-    s_tick[0] = t;
-    if (t < nold) {
-      issue_scatter_tile(src, dsm, &bars[0], t * kTile, min((uint32_t)kTile, end - t * kTile));
-      pend |= 1u;
-    }
-  }
-  __syncthreads();
-
-  for (uint32_t it = 0;; it++) {
-    const uint32_t sidx = it & 1u;
-    const uint32_t t = s_tick[sidx];
-    if (t >= ntot) break;
-    uint8_t* st = dsm + sidx * kScatterStage;
-    if (tid == 0) {  // prefetch the next tile into the other stage
-      bulk_wait_read();  // ... once the previous tile's bulk stores have read it
-      const uint32_t t2 = atomicAdd(&sim->ticket2, 1u);
-      s_tick[sidx ^ 1u] = t2;
-      if (t2 < nold) {
-        fence_proxy_async();
-        issue_scatter_tile(src, dsm + (sidx ^ 1u) * kScatterStage, &bars[sidx ^ 1u], t2 * kTile, min((uint32_t)kTile, end - t2 * kTile));
-        pend |= 2u >> sidx;
+  if (warp == kWarps) {
+    // ================= producer warp =================
+    // fill stage s with the next ticket's tile; returns its kind
+    auto fill = [&](uint32_t s) -> uint32_t {
+      uint32_t t = 0;
+      if (lane == 0) {
+        t = atomicAdd(&sim->ticket2, 1u);
+        s_tick[s] = t;
       }
-    }
-    bool ok = true;
-    if (t < nold) {
-      for (int q = tid; q < kItems * kWarps * 8; q += kBlock) (&s_off[0][0][0])[q] = 0u;
-      if (tid == 0) s_bmn = 0;
-      // ---- decoupled look-back over the count pass's tile aggregates ----
-      if (warp == 0) {
-        uint32_t ex[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        int64_t pos = (int64_t)t - 1;
-        while (pos >= 0) {
-          const int64_t idx = pos - lane;
-          const bool valid = idx >= 0;
-          const uint32_t f = valid ? ld_acquire_u32(&p.tileFlag[idx]) : 0u;
-          const uint32_t m = __ballot_sync(0xffffffffu, !valid || f == epoch);
-          const int stop = m ? __ffs(m) - 1 : 32;
-          uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
-          if (valid && lane <= stop) {
-            const uint32_t* q = (lane == stop ? p.tileIncl : p.tileAgg) + (size_t)idx * 8;
-            v0 = ld_cg_v4(q);
-            v1 = ld_cg_v4(q + 4);
-          }
-          ex[0] += __reduce_add_sync(0xffffffffu, v0.x); ex[1] += __reduce_add_sync(0xffffffffu, v0.y);
-          ex[2] += __reduce_add_sync(0xffffffffu, v0.z); ex[3] += __reduce_add_sync(0xffffffffu, v0.w);
-          ex[4] += __reduce_add_sync(0xffffffffu, v1.x); ex[5] += __reduce_add_sync(0xffffffffu, v1.y);
-          ex[6] += __reduce_add_sync(0xffffffffu, v1.z); ex[7] += __reduce_add_sync(0xffffffffu, v1.w);
-          if (m) break;
-          pos -= 32;
-        }
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if (t < nold) {
         if (lane == 0) {
-          const uint32_t* ag = p.tileAgg + (size_t)t * 8;
-          uint4 a0 = ld_cg_v4(ag), a1 = ld_cg_v4(ag + 4);
-          st_cg_v4(p.tileIncl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
-          st_cg_v4(p.tileIncl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
-          st_release_u32(&p.tileFlag[t], epoch);
-          const uint32_t cnt[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+          fence_proxy_async();  // the stage was last written through the generic proxy
+          issue_scatter_tile(src, dsm + s * kScatterStage, &full[s], t * kTile, min((uint32_t)kTile, end - t * kTile));
+        }
+        uint32_t ex[8], cnt[8];
+        tile_lookback(p, t, epoch, lane, ex, cnt);
+        if (lane == 0) {
           uint32_t pos = 0;
 #pragma unroll
           for (int b = 0; b < 8; b++) {
             const uint32_t d0 = s_base[b] + ex[b];
             const uint32_t sb = ((pos + 15u) & ~15u) + (d0 & 15u);
-            s_d0[b] = d0;
-            s_sb[b] = sb;
-            s_cnt[b] = cnt[b];
+            s_d0[s][b] = d0;
+            s_sb[s][b] = sb;
+            s_cnt[s][b] = cnt[b];
             pos = sb + cnt[b];
           }
+          mbar_arrive(&full[s]);  // layout written (release)
         }
+        return TK_OLD;
       }
-      ok = mbar_wait(&bars[sidx], (phase >> sidx) & 1u);
-      if (ok) {
-        phase ^= 1u << sidx;
-        pend &= ~(1u << sidx);
+      if (lane == 0) {
+        mbar_arrive(&full[s]);
+        mbar_arrive(&full[s]);
       }
-      // ---- recompute the step for the tile's agents (inputs from shared memory) ----
-      float* c_age = (float*)(st + 0 * kColBytes);
-      float* c_his = (float*)(st + 1 * kColBytes);
-      float* c_delay = (float*)(st + 2 * kColBytes);
-      float* c_sporo = (float*)(st + 3 * kColBytes);
-      uint32_t* c_uni = (uint32_t*)(st + 4 * kColBytes);
-      uint32_t* c_avail = (uint32_t*)(st + 5 * kColBytes);
-      uint32_t* c_cycle = (uint32_t*)(st + 6 * kColBytes);
-      uint32_t* c_hbc = (uint32_t*)(st + 7 * kColBytes);
-      uint32_t* c_batches = (uint32_t*)(st + 8 * kColBytes);
-      uint8_t* c_flags = st + 9 * kColBytes;
-      const uint32_t lo = t * kTile;
-      Rec a[kItems];
-      int nb[kItems];
-      uint32_t rk[kItems];
-      __syncthreads();  // s_off cleared
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        const uint32_t i = k * kBlock + tid;
-        const uint32_t g = lo + i;
-        const int rg = (ok && g < end) ? range_of(S.pop, g) : -1;
-        nb[k] = 8;
-        a[k].bm = BM_NONE;
-        if (rg >= 0) {
-          a[k].age = c_age[i]; a[k].his = c_his[i]; a[k].delay = c_delay[i]; a[k].sporo = c_sporo[i];
-          a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
-          a[k].batches = c_batches[i];
-          a[k].female = (c_flags[i] >> 3) & 1u;
-          const int ns = update_agent<true>(c, rg, g, a[k], acc);
-          if (ns >= 0) nb[k] = ns;
-        }
-        const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
-        rk[k] = __popc(peers & lanemask_lt());
-        if (nb[k] < 8 && lane == __ffs(peers) - 1) s_off[k][warp][nb[k]] = __popc(peers);
-      }
-      __syncthreads();  // inputs consumed (the stage becomes the output staging area), counts written
-      // ---- exclusive scan of the (round, warp) counts, one warp per state ----
-      if (warp < 8) {
-        const int b = warp;
-        const uint32_t v = (&s_off[0][0][0])[lane * 8 + b];  // entry (round, warp) = lane, kItems*kWarps == 32
-        uint32_t incl = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        (&s_off[0][0][0])[lane * 8 + b] = incl - v;
-        if (lane == 31 && incl != p.tileAgg[(size_t)t * 8 + b]) tilebad = 1;
-      }
-      __syncthreads();
-      // staging view of the stage: columns kStg elements apart
-      float* g_age = (float*)(st + 0 * kStg * 4);
-      float* g_his = (float*)(st + 1 * kStg * 4);
-      float* g_delay = (float*)(st + 2 * kStg * 4);
-      float* g_sporo = (float*)(st + 3 * kStg * 4);
-      uint32_t* g_uni = (uint32_t*)(st + 4 * kStg * 4);
-      uint32_t* g_avail = (uint32_t*)(st + 5 * kStg * 4);
-      uint32_t* g_cycle = (uint32_t*)(st + 6 * kStg * 4);
-      uint32_t* g_hbc = (uint32_t*)(st + 7 * kStg * 4);
-      uint32_t* g_batches = (uint32_t*)(st + 8 * kStg * 4);
-      uint8_t* g_flags = st + 9 * kStg * 4;
-      // ---- survivors into the staging area, sorted by next state ----
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        const int b = nb[k];
-        uint32_t q = 0xffffffffu;
-        if (b < 8) {
-          const uint32_t j = s_off[k][warp][b] + rk[k];
-          if (j < s_cnt[b]) q = s_sb[b] + j;
-          else tilebad = 1;  // the two passes disagree: stay inside this state's run
-        }
-        // queue the owed Box-Muller draws (warp-aggregated slot reservation)
-        const bool owe = q != 0xffffffffu && a[k].bm != BM_NONE;
-        const uint32_t om = __ballot_sync(0xffffffffu, owe);
-        if (om) {
-          uint32_t qb = 0;
-          if (lane == __ffs(om) - 1) qb = atomicAdd(&s_bmn, (uint32_t)__popc(om));
-          qb = __shfl_sync(0xffffffffu, qb, __ffs(om) - 1);
-          if (owe) s_bmq[qb + __popc(om & lanemask_lt())] = q | ((uint32_t)(k * kBlock + tid) << 11) | (a[k].bm << 21);
-        }
-        if (q != 0xffffffffu) {
-          g_age[q] = a[k].age; g_his[q] = a[k].his; g_delay[q] = a[k].delay; g_sporo[q] = a[k].sporo;
-          g_uni[q] = a[k].uni; g_avail[q] = a[k].avail; g_cycle[q] = a[k].cycle; g_hbc[q] = a[k].hbc;
-          g_batches[q] = a[k].batches;
-          g_flags[q] = (uint8_t)(b | (a[k].female << 3));
-          // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
-          if (b == LARVA) {
-            l1 += sampo_f2u_sat(a[k].age / 24.0f);
-            const uint32_t dd = age_days(a[k].age);
-            dmin = min(dmin, dd); dmax = max(dmax, dd);
-          } else if (b >= IMMATURE && a[k].female) {
-            fem += 1u;
-            inf += a[k].sporo >= 1.0f ? 1u : 0u;
-          }
-        }
-      }
-      __syncthreads();
-      // ---- the owed Box-Muller draws, in dense warps, patched into the staging area ----
-      const uint32_t nbm = s_bmn;
-      if (nbm) {
-        for (uint32_t j = tid; j < nbm; j += kBlock) {
-          const uint32_t e = s_bmq[j];
-          const uint32_t q = e & 2047u, kind = e >> 21;
-          const uint32_t v = finish_box_muller(c, lo + ((e >> 11) & 1023u), kind, g_batches[q]);
-          if (kind == BM_LARVA_DELAY) g_delay[q] = __uint_as_float(v);
-          else g_avail[q] = v;
-        }
-        __syncthreads();
-      }
-      // ---- each state's run to its slots in the next buffer ----
-      // Staging and destination agree modulo 16 bytes, so the aligned body
-      // of every run and column leaves with one bulk store (thread 0); the
-      // unaligned head and tail elements go with plain stores. Runs are
-      // inside the next layout by construction: d0 + count <= range end.
-      if (tid == 0) {
+      return t < ntot ? TK_EGG : TK_END;
+    };
+    uint32_t kind0 = fill(0), kind1 = fill(1), ph = 0;
+    for (uint32_t it = 0;; it++) {
+      const uint32_t s = it & 1u;
+      const uint32_t k = s ? kind1 : kind0;
+      if (k == TK_END) break;
+      uint32_t ok = 1;
+      if (lane == 0) ok = mbar_wait(&empty[s], (ph >> s) & 1u) ? 1u : 0u;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) { fail = 1; break; }
+      ph ^= 1u << s;
+      if (k == TK_OLD && lane == 0) {
+        // ---- each state's run to its slots in the next buffer ----
+        // staging and destination agree modulo 16 bytes: the aligned body of
+        // every run and column leaves with one bulk store; the consumers
+        // wrote the unaligned heads and tails. Runs lie inside the next
+        // layout by construction (d0 + count <= range end).
+        uint8_t* st = dsm + s * kScatterStage;
         fence_proxy_async();  // staging written through the generic proxy
 #pragma unroll 1
         for (int b = 0; b < 8; b++) {
-          const uint32_t n = s_cnt[b], d0 = s_d0[b], sb = s_sb[b];
+          const uint32_t n = s_cnt[s][b], d0 = s_d0[s][b], sb = s_sb[s][b];
           if (!n) continue;
           const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
           if (n4) {
-            const uint32_t o = h4, by = n4 * 4;
-            bulk_store(dst.age + d0 + o, g_age + sb + o, by); bulk_store(dst.his + d0 + o, g_his + sb + o, by);
-            bulk_store(dst.delay + d0 + o, g_delay + sb + o, by); bulk_store(dst.sporo + d0 + o, g_sporo + sb + o, by);
-            bulk_store(dst.uni + d0 + o, g_uni + sb + o, by); bulk_store(dst.avail + d0 + o, g_avail + sb + o, by);
-            bulk_store(dst.cycle + d0 + o, g_cycle + sb + o, by); bulk_store(dst.hbc + d0 + o, g_hbc + sb + o, by);
-            bulk_store(dst.batches + d0 + o, g_batches + sb + o, by);
+            const uint32_t o = h4, by = n4 * 4, so = (sb + o) * 4;
+            bulk_store(dst.age + d0 + o, st + 0 * kStg * 4 + so, by);
+            bulk_store(dst.his + d0 + o, st + 1 * kStg * 4 + so, by);
+            bulk_store(dst.delay + d0 + o, st + 2 * kStg * 4 + so, by);
+            bulk_store(dst.sporo + d0 + o, st + 3 * kStg * 4 + so, by);
+            bulk_store(dst.uni + d0 + o, st + 4 * kStg * 4 + so, by);
+            bulk_store(dst.avail + d0 + o, st + 5 * kStg * 4 + so, by);
+            bulk_store(dst.cycle + d0 + o, st + 6 * kStg * 4 + so, by);
+            bulk_store(dst.hbc + d0 + o, st + 7 * kStg * 4 + so, by);
+            bulk_store(dst.batches + d0 + o, st + 8 * kStg * 4 + so, by);
           }
           const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
-          if (n1) bulk_store(dst.flags + d0 + h1, g_flags + sb + h1, n1);
+          if (n1) bulk_store(dst.flags + d0 + h1, st + 9 * kStg * 4 + sb + h1, n1);
         }
         bulk_commit();
       }
-      // heads and tails: per state at most 15 + 15 flag elements, of which the
-      // four-byte columns need at most 3 + 3
-      {
-        const int b = tid >> 5, e = tid & 31;
-        const uint32_t n = s_cnt[b], d0 = s_d0[b], sb = s_sb[b];
-        const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
-        const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
-        const uint32_t j = (uint32_t)e < h1 ? (uint32_t)e : h1 + n1 + ((uint32_t)e - h1);
-        if (e < 30 && j < n) {
-          const uint32_t q = sb + j, d = d0 + j;
-          dst.flags[d] = g_flags[q];
-          if (j < h4 || j >= h4 + n4) {
-            dst.age[d] = g_age[q]; dst.his[d] = g_his[q]; dst.delay[d] = g_delay[q]; dst.sporo[d] = g_sporo[q];
-            dst.uni[d] = g_uni[q]; dst.avail[d] = g_avail[q]; dst.cycle[d] = g_cycle[q]; dst.hbc[d] = g_hbc[q];
-            dst.batches[d] = g_batches[q];
+      if (lane == 0) bulk_wait_read();  // the stage's sources are read: it may be refilled
+      __syncwarp();
+      const uint32_t nk = fill(s);
+      if (s) kind1 = nk;
+      else kind0 = nk;
+    }
+    if (lane == 0) bulk_wait_all();  // this CTA's bulk stores are complete
+  } else {
+    // ================= consumer warps =================
+    uint32_t ph = 0;
+    for (uint32_t it = 0;; it++) {
+      const uint32_t s = it & 1u;
+      uint8_t* st = dsm + s * kScatterStage;
+      for (int q = tid; q < kItems * kWarps * 8; q += kBlock) (&s_off[0][0][0])[q] = 0u;
+      if (tid == 0) {
+        s_bmn = 0;
+        s_fullok[s] = mbar_wait(&full[s], (ph >> s) & 1u) ? 1u : 0u;
+      }
+      consumer_sync();
+      if (!s_fullok[s]) { fail = 1; break; }
+      (void)mbar_try_wait(&full[s], (ph >> s) & 1u);  // the completed phase, observed by this thread
+      ph ^= 1u << s;
+      const uint32_t t = s_tick[s];
+      if (t >= ntot) break;
+      if (t < nold) {
+        // ---- recompute the step for the tile's agents (inputs from shared memory) ----
+        const float* c_age = (const float*)(st + 0 * kColBytes);
+        const float* c_his = (const float*)(st + 1 * kColBytes);
+        const float* c_delay = (const float*)(st + 2 * kColBytes);
+        const float* c_sporo = (const float*)(st + 3 * kColBytes);
+        const uint32_t* c_uni = (const uint32_t*)(st + 4 * kColBytes);
+        const uint32_t* c_avail = (const uint32_t*)(st + 5 * kColBytes);
+        const uint32_t* c_cycle = (const uint32_t*)(st + 6 * kColBytes);
+        const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
+        const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
+        const uint8_t* c_flags = st + 9 * kColBytes;
+        const uint32_t lo = t * kTile;
+        Rec a[kItems];
+        int nb[kItems];
+        uint32_t rk[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+          const uint32_t i = k * kBlock + tid;
+          const uint32_t g = lo + i;
+          const int rg = g < end ? range_of(S.pop, g) : -1;
+          nb[k] = 8;
+          a[k].bm = BM_NONE;
+          if (rg >= 0) {
+            a[k].age = c_age[i]; a[k].his = c_his[i]; a[k].delay = c_delay[i]; a[k].sporo = c_sporo[i];
+            a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
+            a[k].batches = c_batches[i];
+            a[k].female = (c_flags[i] >> 3) & 1u;
+            const int ns = update_agent<true>(c, rg, g, a[k], acc);
+            if (ns >= 0) nb[k] = ns;
+          }
+          const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
+          rk[k] = __popc(peers & lanemask_lt());
+          if (nb[k] < 8 && lane == __ffs(peers) - 1) s_off[k][warp][nb[k]] = __popc(peers);
+        }
+        consumer_sync();  // inputs consumed (the stage becomes the output staging area), counts written
+        // ---- exclusive scan of the (round, warp) counts, one warp per state ----
+        {
+          const int b = warp;
+          const uint32_t v = (&s_off[0][0][0])[lane * 8 + b];  // entry (round, warp) = lane, kItems*kWarps == 32
+          uint32_t incl = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          (&s_off[0][0][0])[lane * 8 + b] = incl - v;
+          if (lane == 31 && incl != s_cnt[s][b]) tilebad = 1;
+        }
+        consumer_sync();
+        float* g_age = (float*)(st + 0 * kStg * 4);
+        float* g_his = (float*)(st + 1 * kStg * 4);
+        float* g_delay = (float*)(st + 2 * kStg * 4);
+        float* g_sporo = (float*)(st + 3 * kStg * 4);
+        uint32_t* g_uni = (uint32_t*)(st + 4 * kStg * 4);
+        uint32_t* g_avail = (uint32_t*)(st + 5 * kStg * 4);
+        uint32_t* g_cycle = (uint32_t*)(st + 6 * kStg * 4);
+        uint32_t* g_hbc = (uint32_t*)(st + 7 * kStg * 4);
+        uint32_t* g_batches = (uint32_t*)(st + 8 * kStg * 4);
+        uint8_t* g_flags = st + 9 * kStg * 4;
+        // ---- survivors into the staging area, sorted by next state ----
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+          const int b = nb[k];
+          uint32_t q = 0xffffffffu;
+          if (b < 8) {
+            const uint32_t j = s_off[k][warp][b] + rk[k];
+            if (j < s_cnt[s][b]) q = s_sb[s][b] + j;
+            else tilebad = 1;  // the two passes disagree: stay inside this state's run
+          }
+          // queue the owed Box-Muller draws (warp-aggregated slot reservation)
+          const bool owe = q != 0xffffffffu && a[k].bm != BM_NONE;
+          const uint32_t om = __ballot_sync(0xffffffffu, owe);
+          if (om) {
+            uint32_t qb = 0;
+            if (lane == __ffs(om) - 1) qb = atomicAdd(&s_bmn, (uint32_t)__popc(om));
+            qb = __shfl_sync(0xffffffffu, qb, __ffs(om) - 1);
+            if (owe) s_bmq[qb + __popc(om & lanemask_lt())] = q | ((uint32_t)(k * kBlock + tid) << 11) | (a[k].bm << 21);
+          }
+          if (q != 0xffffffffu) {
+            g_age[q] = a[k].age; g_his[q] = a[k].his; g_delay[q] = a[k].delay; g_sporo[q] = a[k].sporo;
+            g_uni[q] = a[k].uni; g_avail[q] = a[k].avail; g_cycle[q] = a[k].cycle; g_hbc[q] = a[k].hbc;
+            g_batches[q] = a[k].batches;
+            g_flags[q] = (uint8_t)(b | (a[k].female << 3));
+            // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
+            if (b == LARVA) {
+              l1 += sampo_f2u_sat(a[k].age / 24.0f);
+              const uint32_t dd = age_days(a[k].age);
+              dmin = min(dmin, dd); dmax = max(dmax, dd);
+            } else if (b >= IMMATURE && a[k].female) {
+              fem += 1u;
+              inf += a[k].sporo >= 1.0f ? 1u : 0u;
+            }
+          }
+        }
+        consumer_sync();
+        // ---- the owed Box-Muller draws, in dense warps, patched into the staging area ----
+        const uint32_t nbm = s_bmn;
+        if (nbm) {
+          for (uint32_t j = tid; j < nbm; j += kBlock) {
+            const uint32_t e = s_bmq[j];
+            const uint32_t q = e & 2047u, kind = e >> 21;
+            const uint32_t v = finish_box_muller(c, lo + ((e >> 11) & 1023u), kind, g_batches[q]);
+            if (kind == BM_LARVA_DELAY) g_delay[q] = __uint_as_float(v);
+            else g_avail[q] = v;
+          }
+          consumer_sync();
+        }
+        // ---- heads and tails of the runs: per state at most 15 + 15 flag
+        //      elements, of which the four-byte columns need at most 3 + 3 ----
+        {
+          const int b = warp, e = lane;
+          const uint32_t n = s_cnt[s][b], d0 = s_d0[s][b], sb = s_sb[s][b];
+          const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
+          const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
+          const uint32_t j = (uint32_t)e < h1 ? (uint32_t)e : h1 + n1 + ((uint32_t)e - h1);
+          if (e < 30 && j < n) {
+            const uint32_t q = sb + j, d = d0 + j;
+            dst.flags[d] = g_flags[q];
+            if (j < h4 || j >= h4 + n4) {
+              dst.age[d] = g_age[q]; dst.his[d] = g_his[q]; dst.delay[d] = g_delay[q]; dst.sporo[d] = g_sporo[q];
+              dst.uni[d] = g_uni[q]; dst.avail[d] = g_avail[q]; dst.cycle[d] = g_cycle[q]; dst.hbc[d] = g_hbc[q];
+              dst.batches[d] = g_batches[q];
+            }
+          }
+        }
+      } else {
+        // ---- new eggs at [0, newEggs) of the next buffer ----
+        const uint32_t e0 = (t - nold) * kTile;
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+          const uint32_t id = e0 + k * kBlock + tid;
+          if (id < s_newEggs) {
+            Rec a;
+            new_egg(c, id, a);
+            dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
+            dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
+            dst.batches[id] = a.batches;
+            dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
           }
         }
       }
-    } else {
-      // ---- new eggs at [0, newEggs) of the next buffer ----
-      const uint32_t e0 = (t - nold) * kTile;
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        const uint32_t id = e0 + k * kBlock + tid;
-        if (id < s_newEggs) {
-          Rec a;
-          new_egg(c, id, a);
-          dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
-          dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
-          dst.batches[id] = a.batches;
-          dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
-        }
-      }
+      mbar_arrive(&empty[s]);  // staged (release): the producer may send and refill the stage
     }
-    if (__syncthreads_or(!ok)) { failed = true; break; }
   }
-  if (failed && tid == 0) {
-    atomicOr(&sim->error, SAMPO_DEV_ERR_TMA);
-    for (int s = 0; s < 2; s++)  // let copies still in flight land before the CTA exits
-      if ((pend >> s) & 1u) (void)mbar_wait(&bars[s], (phase >> s) & 1u);
-  }
-  if (tid == 0) bulk_wait_all();  // this CTA's bulk stores are complete
+  if (fail) atomicOr(&sim->error, SAMPO_DEV_ERR_TMA);
+  __syncthreads();
 
   // ---- per-CTA reduction of the accumulators, one atomic each ----
   {
@@ -699,7 +751,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_scatter(KParams p) {
 #pragma unroll
     for (int j = 0; j < 8; j++) v[j] = j == 7 ? __reduce_or_sync(0xffffffffu, v[j]) : __reduce_add_sync(0xffffffffu, v[j]);
     const uint32_t mn = __reduce_min_sync(0xffffffffu, dmin), mx = __reduce_max_sync(0xffffffffu, dmax);
-    if (lane == 0) {
+    if (lane == 0 && warp < kWarps) {
 #pragma unroll
       for (int j = 0; j < 8; j++) s_red[warp][j] = v[j];
       s_mn[warp] = mn;
@@ -903,7 +955,7 @@ int grid_blocks_count() {
 int grid_blocks_scatter() {
   set_smem_attrs();
   int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kBlock, kScatterSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kScatterThreads, kScatterSmem);
   return sm_count() * (per > 0 ? per : 1);
 }
 cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
@@ -913,7 +965,7 @@ cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
 }
 cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
   set_smem_attrs();
-  k_scatter<<<grid, kBlock, kScatterSmem, st>>>(p);
+  k_scatter<<<grid, kScatterThreads, kScatterSmem, st>>>(p);
   return cudaGetLastError();
 }
 cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev, int age_days_max,
