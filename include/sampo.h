@@ -218,8 +218,9 @@ int sampo_step_noalloc(const sampo_device_pool* in, uint32_t in_capacity, const 
                        void* stream);
 
 /* Diagnostic: evaluates the model's deterministic transcendentals on the
- * device (fn 0 exp(x), 1 log(x), 2 sin(x), 3 pow(x, y)); they must equal the
- * host definitions bit for bit. No counterpart in the reference, whose
+ * device (fn 0 exp(x), 1 log(x), 2 sin(x), 3 pow(x, y), and the binary32
+ * evaluations the normal draw uses: 4 log(x), 5 sin(x)); they must equal the
+ * host definitions of 0-3 bit for bit. No counterpart in the reference, whose
  * OpenCL built-ins are implementation-defined. */
 int sampo_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, int device);
 

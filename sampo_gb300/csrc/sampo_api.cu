@@ -551,7 +551,7 @@ extern "C" int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launche
 }
 
 extern "C" int sampo_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, int device) {
-  if (!x || !out || fn < 0 || fn > 3 || (fn == 3 && !y)) return SAMPO_ERR_ARG;
+  if (!x || !out || fn < 0 || fn > 5 || (fn == 3 && !y)) return SAMPO_ERR_ARG;
   if (n == 0) return SAMPO_OK;
   sampo_sim* s = nullptr;  // CK() reports through a null handle
   CK(cudaSetDevice(device), "device");

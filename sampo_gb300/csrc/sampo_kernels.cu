@@ -173,6 +173,7 @@ __device__ void load_ctx(const KParams& p, SharedCtx& s) {
     c.bmdDelay = -1.231f * T + 77.231f;                                // :239-241
     c.sporoOn = T > 16.0f;                                             // kernel/updateAgents.cl:69-70
     c.sporoInc = __ddiv_rn(1.0, __dmul_rn((double)(111.0f / (T - 16.0f)), 14.0));
+    sampo_split_double(c.sporoInc, &c.sporoH, &c.sporoM, &c.sporoL);
     s.cur = sim->cur;
     s.epoch = sim->epoch;
     s.step = step;
@@ -180,6 +181,7 @@ __device__ void load_ctx(const KParams& p, SharedCtx& s) {
   for (int k = threadIdx.x; k < 100; k += blockDim.x) {
     s.c.adultHMR[k] = sim->adultHMR[k];
     s.c.larvaHMR[k] = sim->larvaHMR[k];
+    if (k < kEggBatchTable) s.c.eggBatchScale[k] = sim->eggBatchScale[k];
   }
   __syncthreads();
 }
@@ -682,7 +684,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
             g_flags[q] = (uint8_t)(b | (a[k].female << 3));
             // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
             if (b == LARVA) {
-              l1 += sampo_f2u_sat(a[k].age / 24.0f);
+              l1 += age_days_uncapped(a[k].age);
               const uint32_t dd = age_days(a[k].age);
               dmin = min(dmin, dd); dmax = max(dmax, dd);
             } else if (b >= IMMATURE && a[k].female) {
@@ -855,7 +857,7 @@ __global__ void k_pool_stats(KParams p) {
     int rg = range_of(pop, g);
     if (rg == LARVA) {
       float age = src.age[g];
-      l1 += sampo_f2u_sat(age / 24.0f);
+      l1 += age_days_uncapped(age);
       uint32_t dd = age_days(age);
       dmin = min(dmin, dd); dmax = max(dmax, dd);
     } else if (rg >= IMMATURE) {
@@ -899,7 +901,7 @@ __global__ void k_histogram(KParams p, uint32_t* hist) {
     int rg = (base + threadIdx.x < span) ? range_of(pop, g) : -1;
     uint32_t bin = 0xffffffffu;
     if (rg >= IMMATURE) {
-      bin = sampo_f2u_sat(src.age[g] / 24.0f);
+      bin = age_days_uncapped(src.age[g]);
       bin = bin < 99u ? bin : 99u;
     }
     const uint32_t peers = __match_any_sync(0xffffffffu, bin);
@@ -919,6 +921,8 @@ __global__ void k_eval_math(int fn, const float* x, const float* y, float* out, 
       case 1: v = sampo_logf(x[i]); break;
       case 2: v = sampo_sinf(x[i]); break;
       case 3: v = sampo_powf(x[i], y[i]); break;
+      case 4: v = sampo_logf_bm(x[i]); break;
+      case 5: v = sampo_sinf_bm(x[i]); break;
       default: break;
     }
     out[i] = v;

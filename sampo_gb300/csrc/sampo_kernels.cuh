@@ -3,6 +3,7 @@
 #include <stdint.h>
 #include "../../include/sampo.h"
 #include "sampo_math.h"
+#include "sampo_model.cuh"
 
 namespace sampo {
 
@@ -38,6 +39,7 @@ struct SimDev {
   float aquaticHMR;
   float adultHMR[100];
   float larvaHMR[100];        // for the current step; NaN outside the larvae's age range
+  float eggBatchScale[kEggBatchTable];
 };
 
 struct KParams {
@@ -71,6 +73,7 @@ inline void fill_constant_tables(SimDev& h) {
   float dmr = 0.1f;
   float dsr = 1.0f - dmr;
   h.aquaticHMR = 1.0f - sampo_powf(dsr, 1.0f / 24.0f);
+  for (uint32_t k = 0; k < kEggBatchTable; k++) h.eggBatchScale[k] = egg_batch_scale(k);
 }
 
 // Launch helpers (sampo_kernels.cu).

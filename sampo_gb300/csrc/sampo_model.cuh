@@ -17,12 +17,18 @@
 #pragma once
 #include <stdint.h>
 #include "sampo_math.h"
+#include "sampo_math_fast.h"
 #include "../../include/sampo.h"
 
 namespace sampo {
 
 enum : int { EGG = 0, LARVA, PUPA, IMMATURE, MATESEEKING, BMS, BMD, GRAVID, NSTATE };
 constexpr uint32_t kLayoutAlign = 64;  // LOCAL_SIZE (include/agent.h:9-17): a layout constant
+constexpr uint32_t kEggBatchTable = 64;  // batches with a tabulated 0.8^(n-1)
+
+// The egg-batch factor pow(0.8f, n) (include/properties.h:262), tabulated on
+// the host for n < kEggBatchTable with the same definition.
+__host__ __device__ __forceinline__ float egg_batch_scale(uint32_t n) { return sampo_powf(0.8f, (float)n); }
 
 // One agent record in registers (the SoA columns of the pool).
 struct Rec {
@@ -53,10 +59,12 @@ struct StepCtx {
   float larvaDev;              // larvaDevelopment(T)
   float pupaDelay, immatureDelay, bmdDelay;
   double sporoInc;             // 1/((111/(T-16))*14) in double, used when T > 16 and bitten
+  float sporoH, sporoM, sporoL;  // sporoInc = sporoH + sporoM + sporoL exactly
   uint32_t sporoOn;            // T > 16
   uint32_t devOOB;             // T >= 44: the reference reads past devRates
   float adultHMR[100];
   float larvaHMR[100];
+  float eggBatchScale[kEggBatchTable];  // egg_batch_scale(n)
 };
 
 // Counters an agent update contributes to (BitesNcycles, EggsNbiomass).
@@ -70,35 +78,69 @@ __host__ __device__ __forceinline__ uint32_t taus_step(uint32_t z, int S1, int S
   return (((z & M) << S3) ^ b);
 }
 
+// Exact int <-> float conversions from FP32 adds and integer ops only: the
+// hardware conversion instructions issue at a fraction of the FP32 rate.
+// (float)v rounded to nearest: both 16-bit halves are exact as 2^23-biased
+// floats, hi * 2^16 is exact, so the one rounding of the final add is the
+// correct rounding of v.
+__device__ __forceinline__ float u32_to_f32_rn(uint32_t v) {
+  const float hi = __uint_as_float(0x4B000000u | (v >> 16)) - 8388608.0f;
+  const float lo = __uint_as_float(0x4B000000u | (v & 0xFFFFu)) - 8388608.0f;
+  return __fadd_rn(__fmul_rn(hi, 65536.0f), lo);
+}
+// (uint32_t)x truncated toward zero for 0 <= x < 2^22 (x + 2^23 rounds to
+// the nearest integer; step back when that rounded up); NaN and x <= 0 give 0.
+__device__ __forceinline__ uint32_t f32_to_u32_small(float x) {
+  if (!(x > 0.0f)) return 0u;
+  const float r = __fadd_rn(x, 8388608.0f);
+  const uint32_t n = __float_as_uint(r) - 0x4B000000u;
+  return __fadd_rn(r, -8388608.0f) > x ? n - 1u : n;
+}
+// sampo_f2u_sat(x) for every x, through FP32 adds below 2^22.
+__device__ __forceinline__ uint32_t f2u_sat_fast(float x) {
+  return x < 4194304.0f ? f32_to_u32_small(x) : sampo_f2u_sat(x);
+}
+// (float)sampo_f2u_sat(x) for every x, through FP32 adds below 2^22.
+__device__ __forceinline__ float trunc_sat_fast(float x) {
+  if (!(x > 0.0f)) return 0.0f;
+  if (!(x < 4194304.0f)) return (float)sampo_f2u_sat(x);
+  const float r = __fadd_rn(__fadd_rn(x, 8388608.0f), -8388608.0f);  // x rounded to an integer
+  return r > x ? __fadd_rn(r, -1.0f) : r;
+}
+
 __device__ __forceinline__ float rng(const StepCtx& c, int slot, uint32_t gid) {
   uint32_t v = c.rng_c13[slot] ^ taus_step(c.rng_z2[slot] + gid, 2, 25, 4, 4294967288u) ^
                (1664525u * (c.rng_z4[slot] * gid) + 1013904223u);
-  return 2.3283064365387e-10f * __uint2float_rn(v);
+  return 2.3283064365387e-10f * u32_to_f32_rn(v);  // (float)v * 2^-32
 }
 
 // BoxMuller(seeds+1, ...) (include/gpuRand.h:56-63): u0 from slot 1, u1 from slot 2.
 __device__ __forceinline__ float box_muller(const StepCtx& c, uint32_t gid, float mean, float sd) {
   float u0 = rng(c, 1, gid), u1 = rng(c, 2, gid);
-  float r = __fsqrt_rn(-2.0f * sampo_logf(u0));
+  float r = __fsqrt_rn(-2.0f * sampo_logf_bm(u0));
   float theta = (2.0f * 3.14159274101257f) * u1;
-  return (r * sampo_sinf(theta)) * sd + mean;
+  return (r * sampo_sinf_bm(theta)) * sd + mean;
 }
 
 // eggsHatching (include/properties.h:39-60)
-__host__ __device__ __forceinline__ float eggs_hatching(float p) {
+__device__ __forceinline__ float eggs_hatching(float p) {
   float m, b;
   if (p < 0.5f) { m = 48.0f; b = 0.0f; }
   else if (p < 0.85f) { m = 68.5714f; b = -10.2857f; }
   else if (p < 0.90f) { m = 480.0f; b = -360.0f; }
   else if (p < 0.94f) { m = 600.00f; b = -468.0f; }
   else { m = 2400.0f; b = -2160.0f; }
-  return (float)sampo_f2u_sat(m * p + b + 0.5f);
+  return trunc_sat_fast(m * p + b + 0.5f);
 }
 
 __host__ __device__ __forceinline__ bool night(uint32_t wt) { return wt <= 6u || wt >= 18u; }
 
 __device__ __forceinline__ uint32_t age_days(float age) {
-  return sampo_f2u_sat(sampo_fminf(age / 24.0f, 99.0f));  // kernel/killAgents.cl:55
+  return f32_to_u32_small(sampo_fminf(age / 24.0f, 99.0f));  // kernel/killAgents.cl:55
+}
+// (UINT)(age / 24.0f) without the 99-day cap (kernel/calcL1de.cl:30)
+__device__ __forceinline__ uint32_t age_days_uncapped(float age) {
+  return f2u_sat_fast(age / 24.0f);
 }
 
 // Kill then update one valid agent of range rg at slot gid.
@@ -123,7 +165,7 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
   a.age = a.age + 1.0f;
   a.his = a.his + 1.0f;
   if (FULL && c.sporoOn && a.hbc > 0u)  // kernel/updateAgents.cl:69-70, in double
-    a.sporo = __double2float_rn(__dadd_rn((double)a.sporo, c.sporoInc));
+    a.sporo = sampo_sporo_add(a.sporo, c.sporoH, c.sporoM, c.sporoL, c.sporoInc);
   switch (rg) {
     case EGG:
       if (a.his >= a.delay) {
@@ -210,9 +252,9 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
           }
           if (!trapped) {
             // layEggs (include/properties.h:296-307)
-            float nbm = (float)c.totalBiomass / (((float)a.uni + 1.0f) * c.env.carryingCapacity);
+            float nbm = u32_to_f32_rn(c.totalBiomass) / ((u32_to_f32_rn(a.uni) + 1.0f) * c.env.carryingCapacity);
             float pbm = sampo_fmaxf(0.0f, 1.0f - nbm);
-            uint32_t pe = sampo_f2u_sat(ceilf((float)avail * pbm));
+            uint32_t pe = f2u_sat_fast(ceilf(u32_to_f32_rn(avail) * pbm));
             if (!FULL) acc.newEggs += pe;
             avail = avail - pe;
           }
@@ -237,8 +279,10 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
 // given numEggBatches after its increment.
 __device__ __forceinline__ uint32_t finish_box_muller(const StepCtx& c, uint32_t gid, uint32_t kind, uint32_t batches_after) {
   if (kind == BM_LARVA_DELAY) return __float_as_uint(box_muller(c, gid, 1.0f, 0.1f));
-  uint32_t eggs = sampo_f2u_sat(box_muller(c, gid, 170.0f, 30.0f) + 0.5f);
-  return sampo_f2u_sat((float)eggs * sampo_powf(0.8f, (float)(batches_after - 1u)) + 0.5f);
+  uint32_t eggs = f2u_sat_fast(box_muller(c, gid, 170.0f, 30.0f) + 0.5f);
+  const uint32_t n = batches_after - 1u;
+  const float scale = n < kEggBatchTable ? c.eggBatchScale[n] : egg_batch_scale(n);
+  return f2u_sat_fast(u32_to_f32_rn(eggs) * scale + 0.5f);
 }
 
 // initAgents (kernel/initAgents.cl:34-64) for new slot id.

@@ -47,6 +47,35 @@ def test_device_math_matches_host(gpu_ready, oracle_mod):
         assert np.array_equal(host.view(np.uint32), dev.view(np.uint32)), f"fn {fn}"
 
 
+def test_device_fast_paths_match_definitions(gpu_ready, oracle_mod):
+    """The normal draw's binary32 log and sin (fn 4, 5) equal the binary64
+    definitions (fn 1, 2) on the device for every input of their domains, and
+    the host definitions on a sample."""
+    import ctypes
+    lib = oracle_mod.load()
+    lib.orc_eval_math.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
+    lo = int(np.float32(2.0 ** -32).view(np.uint32))
+    hi = int(np.float32(1.0).view(np.uint32))
+    u_all = np.arange(lo, hi + 1, dtype=np.uint32).view(np.float32)
+    u_all = np.concatenate([np.zeros(1, np.float32), u_all])
+    chunk = 1 << 26
+    for fast, ref in ((4, 1), (5, 2)):
+        for s in range(0, u_all.size, chunk):
+            u = u_all[s:s + chunk]
+            x = u if fast == 4 else (np.float32(6.2831855) * u).astype(np.float32)
+            a = np.empty_like(x)
+            b = np.empty_like(x)
+            assert gpu_ready.sampo_eval_math(fast, x.ctypes.data, None, a.ctypes.data, x.size, 0) == 0
+            assert gpu_ready.sampo_eval_math(ref, x.ctypes.data, None, b.ctypes.data, x.size, 0) == 0
+            bad = np.nonzero(a.view(np.uint32) != b.view(np.uint32))[0]
+            assert bad.size == 0, f"fn {fast}: x={x[bad[0]]!r} fast {a[bad[0]]!r} definition {b[bad[0]]!r}"
+            if s == 0:
+                xs = np.ascontiguousarray(x[::61])
+                h = np.empty_like(xs)
+                lib.orc_eval_math(ref, xs.ctypes.data, xs.ctypes.data, h.ctypes.data, xs.size)
+                assert np.array_equal(h.view(np.uint32), a[::61].view(np.uint32)), f"fn {fast} vs host"
+
+
 def _compare_pools(ra, aa, rb, ab, where):
     assert np.array_equal(np.asarray(ra, np.int64), np.asarray(rb, np.int64)), f"{where}: ranges differ"
     for k in range(8):
