@@ -203,7 +203,7 @@ def gpu_arm(args, wl, rank, world, device):
     rows = np.concatenate(rows)
     live = live_counts(rows)
     agent_days = float(live.sum()) / 24.0
-    gpu_launches = 48 * args.steps
+    gpu_launches = 73 * args.steps  # per day: one constants refresh + 24 x (count, scatter, publish)
 
     # ---- roofline: the same days again, each kernel between CUDA events ----
     fresh()

@@ -156,7 +156,8 @@ int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear);
  * Turning it on or off clears the sums. */
 int sampo_set_timing(sampo_sim* s, int on);
 /* Sums since sampo_set_timing, in milliseconds: out[0] count pass,
- * out[1] update+scatter pass, out[2] both; *launches = kernels launched. */
+ * out[1] update+scatter pass, out[2] the whole step (both + the per-step
+ * publish kernel); *launches = kernels launched. */
 int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launches);
 /* Device time of the last sampo_run, in milliseconds, from CUDA events
  * recorded on the simulation's stream around its launches. */
@@ -223,6 +224,62 @@ int sampo_step_noalloc(const sampo_device_pool* in, uint32_t in_capacity, const 
  * host definitions of 0-3 bit for bit. No counterpart in the reference, whose
  * OpenCL built-ins are implementation-defined. */
 int sampo_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, int device);
+
+/* ---- batches: many independent simulations stepped together ----
+ * No counterpart in the reference, which runs one simulation per process.
+ * A batch owns up to max_replicates slots on one GPU; every slot holds one
+ * simulation (a "replicate": its own pool, carrying capacity, seeds, inputs
+ * and step counter). sampo_batch_run advances every active replicate by the
+ * same number of steps in one pass of the step kernels per hour (tiles of all
+ * replicates share the persistent CTAs), replayed as a CUDA graph per day.
+ * Each replicate's results are bit-identical to the same simulation run
+ * alone through sampo_step / sampo_run. Slots can be filled and emptied
+ * between runs (continuous batching); pools are allocated stream-ordered
+ * from the batch's memory pool. */
+#define SAMPO_BATCH_MAX_REPLICATES 1024u
+typedef struct sampo_batch sampo_batch;
+typedef struct {
+  uint32_t max_replicates;   /* slots (<= SAMPO_BATCH_MAX_REPLICATES) */
+  uint32_t ring_steps;       /* per-replicate ring of inputs and stats rows, in steps (>= 2) */
+  int device;
+} sampo_batch_config;
+typedef struct {
+  uint64_t capacity;         /* slots per pool buffer */
+  float carrying_capacity;   /* constant per run (src/abms.c:19,132) */
+  uint32_t stop_step;        /* the replicate stops once it has run this many steps; 0xffffffff: never */
+} sampo_replicate_config;
+
+int sampo_batch_create(const sampo_batch_config* cfg, sampo_batch** out);
+int sampo_batch_destroy(sampo_batch* b);
+const char* sampo_batch_last_error(const sampo_batch* b);
+/* Device bytes one replicate of this capacity holds in a batch of this ring. */
+uint64_t sampo_batch_replicate_bytes(uint64_t capacity, uint32_t ring_steps);
+/* Takes a free slot and allocates its buffers; the replicate is inactive
+ * until sampo_batch_init_population. */
+int sampo_batch_add(sampo_batch* b, const sampo_replicate_config* rc, uint32_t* slot);
+/* Frees the slot and its buffers (stream-ordered after the work queued so far). */
+int sampo_batch_remove(sampo_batch* b, uint32_t slot);
+/* As sampo_set_inputs / sampo_set_seeds, for one replicate. */
+int sampo_batch_set_inputs(sampo_batch* b, uint32_t slot, uint32_t first, const float* temperature,
+                           const sampo_environment* env, uint32_t nsteps);
+int sampo_batch_set_seeds(sampo_batch* b, uint32_t slot, uint32_t first, const sampo_seeds* seeds, uint32_t nsteps);
+/* As sampo_init_population; activates the replicate at step 0. */
+int sampo_batch_init_population(sampo_batch* b, uint32_t slot, uint32_t n, const sampo_seeds init_seeds[4],
+                                int age_days_max, uint64_t age_seed);
+/* Advances every active replicate by nsteps (a replicate stops at its
+ * stop_step). Asynchronous unless wait != 0; status of the replicates is
+ * read with sampo_batch_state after sampo_batch_sync. */
+int sampo_batch_run(sampo_batch* b, uint32_t nsteps, int wait);
+int sampo_batch_sync(sampo_batch* b);
+/* Rows of steps [first, first + n) of one replicate (row k = stats at the
+ * start of step k, as sampo_run returns them); the ring must still hold them. */
+int sampo_batch_rows(sampo_batch* b, uint32_t slot, uint32_t first, uint32_t n, sampo_stats_row* out);
+/* Step reached, whether still active, and device error/warning bits. */
+int sampo_batch_state(sampo_batch* b, uint32_t slot, uint32_t* step, uint32_t* active, uint32_t* status_bits);
+int sampo_batch_histogram(sampo_batch* b, uint32_t slot, uint32_t out[100]);
+int sampo_batch_read_pool(sampo_batch* b, uint32_t slot, sampo_population* pop, sampo_pool_view* v);
+/* Device time of the last sampo_batch_run, in milliseconds (after sync). */
+int sampo_batch_last_run_ms(sampo_batch* b, double* ms);
 
 /* Library version and build information. */
 int sampo_abi_version(void);

@@ -89,6 +89,14 @@ POOL_COLUMNS = (("ageInHours", np.float32), ("hoursInState", np.float32), ("dela
 
 # every function the header declares, with its ctypes signature
 _P = C.c_void_p
+class BatchConfig(C.Structure):
+    _fields_ = [("max_replicates", C.c_uint32), ("ring_steps", C.c_uint32), ("device", C.c_int)]
+
+
+class ReplicateConfig(C.Structure):
+    _fields_ = [("capacity", C.c_uint64), ("carrying_capacity", C.c_float), ("stop_step", C.c_uint32)]
+
+
 SIGNATURES = {
     "sampo_abi_version": (C.c_int, []),
     "sampo_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
@@ -121,6 +129,22 @@ SIGNATURES = {
                                      C.POINTER(Population), C.POINTER(Environment), C.c_float, C.c_uint32, _P,
                                      C.c_float, C.POINTER(StatsRow), C.POINTER(Population), C.POINTER(BitesCycles),
                                      C.c_int, _P]),
+    "sampo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),
+    "sampo_batch_destroy": (C.c_int, [_P]),
+    "sampo_batch_last_error": (C.c_char_p, [_P]),
+    "sampo_batch_replicate_bytes": (C.c_uint64, [C.c_uint64, C.c_uint32]),
+    "sampo_batch_add": (C.c_int, [_P, C.POINTER(ReplicateConfig), C.POINTER(C.c_uint32)]),
+    "sampo_batch_remove": (C.c_int, [_P, C.c_uint32]),
+    "sampo_batch_set_inputs": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint32]),
+    "sampo_batch_set_seeds": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32]),
+    "sampo_batch_init_population": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_int, C.c_uint64]),
+    "sampo_batch_run": (C.c_int, [_P, C.c_uint32, C.c_int]),
+    "sampo_batch_sync": (C.c_int, [_P]),
+    "sampo_batch_rows": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
+    "sampo_batch_state": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "sampo_batch_histogram": (C.c_int, [_P, C.c_uint32, _P]),
+    "sampo_batch_read_pool": (C.c_int, [_P, C.c_uint32, C.POINTER(Population), C.POINTER(PoolView)]),
+    "sampo_batch_last_run_ms": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
 _lib = None

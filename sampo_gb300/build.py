@@ -23,7 +23,7 @@ CLI = os.path.join(OUT, "sampo")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-lineinfo", "-std=c++17",
                   "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", f"-I{os.path.join(REPO, 'include')}"]
-SOURCES = ["sampo_kernels.cu", "sampo_api.cu", "sampo_host.cpp", "sampo_noalloc.cu"]
+SOURCES = ["sampo_kernels.cu", "sampo_api.cu", "sampo_batch.cu", "sampo_host.cpp", "sampo_noalloc.cu"]
 
 
 def nvcc() -> str:

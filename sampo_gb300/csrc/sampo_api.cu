@@ -2,8 +2,9 @@
 //
 // One handle owns one simulation on one GPU: two pool buffers, the device
 // step state, the per-tile look-back arrays and rings of per-step inputs and
-// stats rows. No call exits the process; errors come back as status codes
-// with a message in sampo_last_error.
+// stats rows; the kernels see it as a batch of one replicate. No call exits
+// the process; errors come back as status codes with a message in
+// sampo_last_error.
 #include <cuda_runtime.h>
 #include <string.h>
 #include <stdio.h>
@@ -24,6 +25,9 @@ struct sampo_sim {
   void* pool_mem[2] = {nullptr, nullptr};
   DevPool pool[2];
   SimDev* sim_dev = nullptr;
+  RepParams* rep_dev = nullptr;        // this simulation as a batch of one
+  BatchDev* bat_dev = nullptr;
+  ModelConst* mc_dev = nullptr;
   uint32_t* tile_mem = nullptr;
   uint32_t max_tiles = 0;
   float* T_dev = nullptr;
@@ -49,7 +53,7 @@ struct sampo_sim {
   int grid_count = 0, grid_scatter = 0;
   cudaGraphExec_t day_graph = nullptr;
   bool timing = false;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   double t_count = 0, t_scatter = 0, t_total = 0;
   uint64_t launches = 0;
   std::string err;
@@ -70,21 +74,30 @@ static int cuda_fail(sampo_sim* s, cudaError_t e, const char* what) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+static RepParams make_rep(sampo_sim* s) {
+  RepParams r;
+  r.sim = s->sim_dev;
+  r.pool[0] = s->pool[0];
+  r.pool[1] = s->pool[1];
+  r.tileAgg = s->tile_mem;
+  r.tileIncl = s->tile_mem + (size_t)s->max_tiles * 8;
+  r.tileFlag = s->tile_mem + (size_t)s->max_tiles * 16;
+  r.T = s->T_dev;
+  r.env = s->env_dev;
+  r.seeds = s->seeds_dev;
+  r.wt = s->wt_dev;
+  r.rows = s->rows_dev;
+  r.ring = s->ring;
+  r.maxTiles = s->max_tiles;
+  return r;
+}
+
 static KParams make_params(sampo_sim* s) {
   KParams p;
-  p.sim = s->sim_dev;
-  p.pool[0] = s->pool[0];
-  p.pool[1] = s->pool[1];
-  p.tileAgg = s->tile_mem;
-  p.tileIncl = s->tile_mem + (size_t)s->max_tiles * 8;
-  p.tileFlag = s->tile_mem + (size_t)s->max_tiles * 16;
-  p.T = s->T_dev;
-  p.env = s->env_dev;
-  p.seeds = s->seeds_dev;
-  p.wt = s->wt_dev;
-  p.rows = s->rows_dev;
-  p.ring = s->ring;
-  p.maxTiles = s->max_tiles;
+  p.reps = s->rep_dev;
+  p.nrep = 1;
+  p.bat = s->bat_dev;
+  p.mc = s->mc_dev;
   return p;
 }
 
@@ -100,6 +113,7 @@ extern "C" int sampo_destroy(sampo_sim* s) {
   for (auto& e : s->ev) if (e) cudaEventDestroy(e);
   cudaFree(s->pool_mem[0]); cudaFree(s->pool_mem[1]);
   cudaFree(s->sim_dev); cudaFree(s->tile_mem);
+  cudaFree(s->rep_dev); cudaFree(s->bat_dev); cudaFree(s->mc_dev);
   cudaFree(s->T_dev); cudaFree(s->env_dev); cudaFree(s->seeds_dev); cudaFree(s->wt_dev);
   cudaFree(s->rows_dev); cudaFree(s->init_seeds_dev); cudaFree(s->hist_dev); cudaFree(s->flush_buf);
   if (s->rows_pinned) cudaFreeHost(s->rows_pinned);
@@ -141,7 +155,13 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     s->max_tiles = (uint32_t)((C + kTile - 1) / kTile);
     if ((e = cudaMalloc(&s->tile_mem, (size_t)s->max_tiles * 17 * 4)) != cudaSuccess) { rc = cuda_fail(s, e, "tile arrays"); break; }
     cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream);
-    if ((e = cudaMalloc(&s->sim_dev, sizeof(SimDev))) != cudaSuccess) { rc = cuda_fail(s, e, "state"); break; }
+    if ((e = cudaMalloc(&s->sim_dev, sizeof(SimDev))) != cudaSuccess ||
+        (e = cudaMalloc(&s->rep_dev, sizeof(RepParams))) != cudaSuccess ||
+        (e = cudaMalloc(&s->bat_dev, sizeof(BatchDev))) != cudaSuccess ||
+        (e = cudaMalloc(&s->mc_dev, sizeof(ModelConst))) != cudaSuccess) {
+      rc = cuda_fail(s, e, "state");
+      break;
+    }
     const size_t R = s->ring;
     if ((e = cudaMalloc(&s->T_dev, R * sizeof(float))) != cudaSuccess ||
         (e = cudaMalloc(&s->env_dev, R * sizeof(sampo_environment))) != cudaSuccess ||
@@ -158,18 +178,20 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     s->have_inputs.assign(R, 0);
     s->input_step.assign(R, 0xffffffffu);
     s->seed_step.assign(R, 0xffffffffu);
-    memset(&s->host_state, 0, sizeof(SimDev));
-    s->host_state.capacity = (uint32_t)C;
-    s->host_state.cc = s->cc;
-    s->host_state.acc_dmin = 0xffffffffu;
-    s->host_state.epoch = 1;
-    fill_constant_tables(s->host_state);
-    if ((e = cudaMemcpyAsync(s->sim_dev, &s->host_state, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess) {
+    s->host_state = initial_sim_state((uint32_t)C, s->cc);
+    s->host_state.active = 1;
+    ModelConst mc;
+    fill_constant_tables(mc);
+    const RepParams rep = make_rep(s);
+    if ((e = cudaMemcpyAsync(s->sim_dev, &s->host_state, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->rep_dev, &rep, sizeof(RepParams), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->mc_dev, &mc, sizeof(ModelConst), cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(s->bat_dev, 0, sizeof(BatchDev), s->stream)) != cudaSuccess) {
       rc = cuda_fail(s, e, "state upload");
       break;
     }
-    s->grid_count = grid_blocks_count();
-    s->grid_scatter = grid_blocks_scatter();
+    s->grid_count = grid_blocks_count(1);
+    s->grid_scatter = grid_blocks_scatter(1);
     for (auto& ev : s->ev) cudaEventCreate(&ev);
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_fail(s, e, "create"); break; }
   } while (0);
@@ -231,6 +253,7 @@ extern "C" int sampo_set_seeds(sampo_sim* s, uint32_t first, const sampo_seeds* 
 static int reset_state(sampo_sim* s, const sampo_population& pop) {
   SimDev h = s->host_state;
   h.pop = pop;
+  h.active = 1;
   h.step = 0;
   h.cur = 0;
   // The look-back trusts a tile's inclusive prefix when its flag equals the
@@ -321,7 +344,8 @@ static int check_device(sampo_sim* s) {
 static cudaError_t launch_step(sampo_sim* s, const KParams& p) {
   cudaError_t e = launch_count(p, s->grid_count, s->stream);
   if (e != cudaSuccess) return e;
-  return launch_scatter(p, s->grid_scatter, s->stream);
+  if ((e = launch_scatter(p, s->grid_scatter, s->stream)) != cudaSuccess) return e;
+  return launch_publish(p, PUB_AFTER_STEP, s->stream);
 }
 
 extern "C" int sampo_step(sampo_sim* s, const sampo_environment* env, float temperature, uint32_t world_time,
@@ -341,8 +365,9 @@ extern "C" int sampo_step(sampo_sim* s, const sampo_environment* env, float temp
   s->seed_step[slot] = s->step;
   if (row) CK(cudaMemcpyAsync(row, s->rows_dev + slot, sizeof(sampo_stats_row), cudaMemcpyDeviceToHost, s->stream), "row");
   KParams p = make_params(s);
+  CK(launch_publish(p, PUB_REFRESH, s->stream), "step constants");  // this step's inputs were just written
   CK(launch_step(s, p), "step kernels");
-  s->launches += 2;
+  s->launches += 4;
   s->step++;
   return check_device(s);
 }
@@ -382,6 +407,8 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
     if (s->seed_step[slot] != st) return fail(s, SAMPO_ERR_STATE, "no seeds for step " + std::to_string(st));
   }
   KParams p = make_params(s);
+  CK(launch_publish(p, PUB_REFRESH, s->stream), "step constants");  // inputs may postdate the last publish
+  s->launches += 1;
   uint32_t done = 0;
   // rows of steps [s->step, s->step + n) are read back in chunks no longer than the ring allows
   const uint32_t chunk_max = s->ring - 1;
@@ -397,12 +424,15 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
         CK(cudaEventRecord(s->ev[1], s->stream), "event");
         CK(launch_scatter(p, s->grid_scatter, s->stream), "scatter kernel");
         CK(cudaEventRecord(s->ev[2], s->stream), "event");
-        CK(cudaEventSynchronize(s->ev[2]), "event");
-        float a = 0, b = 0;
+        CK(launch_publish(p, PUB_AFTER_STEP, s->stream), "publish kernel");
+        CK(cudaEventRecord(s->ev[4], s->stream), "event");
+        CK(cudaEventSynchronize(s->ev[4]), "event");
+        float a = 0, b = 0, c = 0;
         cudaEventElapsedTime(&a, s->ev[0], s->ev[1]);
         cudaEventElapsedTime(&b, s->ev[1], s->ev[2]);
-        s->t_count += a; s->t_scatter += b; s->t_total += a + b;
-        s->launches += 2;
+        cudaEventElapsedTime(&c, s->ev[2], s->ev[4]);
+        s->t_count += a; s->t_scatter += b; s->t_total += a + b + c;
+        s->launches += 3;
       }
     } else {
       uint32_t i = 0;
@@ -411,12 +441,12 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
         if (rc) return rc;
         for (; i + 24 <= n; i += 24) {
           CK(cudaGraphLaunch(s->day_graph, s->stream), "day graph");
-          s->launches += 48;
+          s->launches += 72;
         }
       }
       for (; i < n; i++) {
         CK(launch_step(s, p), "step kernels");
-        s->launches += 2;
+        s->launches += 3;
       }
     }
     CK(cudaEventRecord(s->ev[2], s->stream), "event");

@@ -1,22 +1,25 @@
 // sampo_kernels.cu - the SAMPO hourly step on GB300 (sm_103a).
 //
-// A step is two persistent-CTA kernels over the current pool buffer:
+// A step of a batch of simulations is two persistent-CTA kernels over every
+// active replicate's current pool buffer, whose 1024-slot tiles they take
+// from one ticket counter, and a small one with a CTA per replicate:
 //
 //  k_count   reads the ~12 bytes per agent that decide survival, the next
 //            state and the eggs laid (killAgents + the decision part of
-//            updateAgents), and publishes per 1024-slot tile the number of
-//            survivors per next state plus the step's newEggs total.
+//            updateAgents), and publishes per tile the number of survivors
+//            per next state plus the replicate's newEggs total.
 //  k_scatter recomputes the same decisions with the complete record,
 //            obtains each survivor's stable rank within its next state
 //            (warp match/popc + a block scan + a decoupled look-back over
-//            the tile counts that k_count already published, so no CTA ever
-//            waits on another), writes the updated record to its slot in the
-//            other buffer (the reference's oldToNewAgents layout,
-//            kernel/oldToNewAgents.cl:57-95,126-226), writes the new eggs at
-//            [0, newEggs) (initAgents, kernel/initAgents.cl:26-65), and
-//            accumulates the next step's statistics (calcL1de.cl,
-//            calcGender.cl). The last CTA to finish publishes the next
-//            population, the stats row and the larval mortality table.
+//            the tile counts that k_count already published, within the
+//            replicate, so no CTA ever waits on another), writes the updated
+//            record to its slot in the other buffer (the reference's
+//            oldToNewAgents layout, kernel/oldToNewAgents.cl:57-95,126-226),
+//            writes the new eggs at [0, newEggs) (initAgents,
+//            kernel/initAgents.cl:26-65), and accumulates the next step's
+//            statistics (calcL1de.cl, calcGender.cl).
+//  k_publish turns each replicate's counts into its next population, stats
+//            row, step constants and larval mortality table.
 //
 // Both kernels stream tiles through shared memory with TMA bulk copies
 // (cp.async.bulk + mbarrier, double-buffered: tile j+1 is in flight while
@@ -137,54 +140,134 @@ __device__ __forceinline__ void next_layout(const uint32_t cnt[8], uint32_t newE
   np.numLarvae1DayEquiv = 0; np.numFemale = 0; np.numPotentiallyInfective = 0;
 }
 
-struct alignas(16) SharedCtx {
-  StepCtx c;
-  sampo_population pop;
-  uint32_t cur, epoch, step;
-};
-
-__device__ void load_ctx(const KParams& p, SharedCtx& s) {
-  SimDev* sim = p.sim;
-  if (threadIdx.x == 0) {
-    StepCtx& c = s.c;
-    uint32_t step = sim->step;
-    uint32_t i = step % p.ring;
-    const sampo_seeds* sd = p.seeds + (size_t)i * 4;
+// Whether the next layout (kernel/oldToNewAgents.cl:57-95) fits in one buffer.
+__device__ __forceinline__ bool layout_fits(const uint32_t cnt[8], uint32_t newEggs, uint32_t capacity) {
+  const uint64_t tot = (uint64_t)newEggs + cnt[0];
+  uint64_t e = tot;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      c.rng_c13[k] = taus_step(sd[k].z1 + 128u, 13, 19, 12, 4294967294u) ^ taus_step(sd[k].z3 + 128u, 3, 11, 17, 4294967280u);
-      c.rng_z2[k] = sd[k].z2 + 128u;
-      c.rng_z4[k] = sd[k].z4;
-    }
-    c.env = p.env[i];
-    float T = p.T[i];
-    c.T = T;
-    c.wt = p.wt[i];
-    s.pop = sim->pop;
-    c.totalBiomass = s.pop.numLarvae1DayEquiv + s.pop.r[EGG].end + (s.pop.r[PUPA].end - s.pop.r[PUPA].start);
-    c.aquaticHMR = sim->aquaticHMR;
-    c.eggIncubation = -0.923f * T + 60.923f;                           // include/properties.h:29-31
-    float cl = sampo_fminf(sampo_fmaxf(T, 12.0f), 48.0f);               // :105-109
-    int di = (int)cl - 12;
-    c.devOOB = di > 31;
-    c.larvaDev = di > 31 ? 0.0f : kDevRates[di];
-    c.pupaDelay = __double2float_rn(__dadd_rn(__dmul_rn(-0.923, (double)T), 60.923));  // :133-135
-    c.immatureDelay = -2.667f * T + 120.0f;                            // :159-161
-    c.bmdDelay = -1.231f * T + 77.231f;                                // :239-241
-    c.sporoOn = T > 16.0f;                                             // kernel/updateAgents.cl:69-70
-    c.sporoInc = __ddiv_rn(1.0, __dmul_rn((double)(111.0f / (T - 16.0f)), 14.0));
-    sampo_split_double(c.sporoInc, &c.sporoH, &c.sporoM, &c.sporoL);
-    s.cur = sim->cur;
-    s.epoch = sim->epoch;
-    s.step = step;
+  for (int k = 1; k < 8; k++) e = ((e + kLayoutAlign) / kLayoutAlign) * kLayoutAlign + cnt[k];
+  return tot <= 0xffffffffull && e <= (uint64_t)capacity;
+}
+
+// The constants of step `step` of one simulation starting from `pop`:
+// HybridTaus with z1 and z3 folded per seed slot (include/gpuRand.h:33-50),
+// the species functions of the step's temperature (include/properties.h) and
+// the biomass of the pool (kernel/killAgents.cl:42-43). The larval mortality
+// table is filled separately (k_publish).
+__device__ void compute_ctx(const RepParams& rp, const sampo_population& pop, uint32_t step, StepCtx& c) {
+  c.larvaHMR = rp.sim->larvaHMR;
+  const uint32_t i = step % rp.ring;
+  const sampo_seeds* sd = rp.seeds + (size_t)i * 4;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    c.rng_c13[k] = taus_step(sd[k].z1 + 128u, 13, 19, 12, 4294967294u) ^ taus_step(sd[k].z3 + 128u, 3, 11, 17, 4294967280u);
+    c.rng_z2[k] = sd[k].z2 + 128u;
+    c.rng_z4[k] = sd[k].z4;
   }
-  for (int k = threadIdx.x; k < 100; k += blockDim.x) {
-    s.c.adultHMR[k] = sim->adultHMR[k];
-    s.c.larvaHMR[k] = sim->larvaHMR[k];
-    if (k < kEggBatchTable) s.c.eggBatchScale[k] = sim->eggBatchScale[k];
+  c.env = rp.env[i];
+  const float T = rp.T[i];
+  c.T = T;
+  c.wt = rp.wt[i];
+  c.totalBiomass = pop.numLarvae1DayEquiv + pop.r[EGG].end + (pop.r[PUPA].end - pop.r[PUPA].start);
+  c.eggIncubation = -0.923f * T + 60.923f;                           // include/properties.h:29-31
+  const float cl = sampo_fminf(sampo_fmaxf(T, 12.0f), 48.0f);         // :105-109
+  const int di = (int)cl - 12;
+  c.devOOB = di > 31;
+  c.larvaDev = di > 31 ? 0.0f : kDevRates[di];
+  c.pupaDelay = __double2float_rn(__dadd_rn(__dmul_rn(-0.923, (double)T), 60.923));  // :133-135
+  c.immatureDelay = -2.667f * T + 120.0f;                            // :159-161
+  c.bmdDelay = -1.231f * T + 77.231f;                                // :239-241
+  c.sporoOn = T > 16.0f;                                             // kernel/updateAgents.cl:69-70
+  c.sporoInc = __ddiv_rn(1.0, __dmul_rn((double)(111.0f / (T - 16.0f)), 14.0));
+  sampo_split_double(c.sporoInc, &c.sporoH, &c.sporoM, &c.sporoL);
+}
+
+template <class T>
+__device__ void load_model_const(const T* g, T& s) {
+  const float* src = reinterpret_cast<const float*>(g);
+  float* dst = reinterpret_cast<float*>(&s);
+  for (int k = threadIdx.x; k < (int)(sizeof(T) / 4); k += blockDim.x) dst[k] = src[k];
+}
+
+// Exclusive scan of one value per thread over the CTA (blockDim.x a multiple
+// of 32); s_w holds 33 words. Ends with all threads synchronised.
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_w, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < nw ? s_w[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    s_w[lane] = wi - w;
+    if (lane == 31) s_w[32] = wi;
   }
   __syncthreads();
+  const uint32_t r = s_w[warp] + incl - v;
+  *total = s_w[32];
+  __syncthreads();
+  return r;
 }
+
+// Ticket ranges of a pass over the batch: replicate r owns tickets
+// [s_pre[r], s_pre[r+1]); s_pre[nrep] is the number of tickets. tiles(r) is
+// r's tile count in this pass. All threads; ends synchronised.
+template <class F>
+__device__ void plan_tickets(uint32_t nrep, uint32_t* s_pre, uint32_t* s_w, F tiles) {
+  if (nrep == 1) {  // a single simulation
+    if (threadIdx.x == 0) {
+      s_pre[0] = 0;
+      s_pre[1] = tiles(0u);
+    }
+    __syncthreads();
+    return;
+  }
+  const uint32_t per = (nrep + blockDim.x - 1) / blockDim.x;  // <= 4: nrep <= kMaxRep, blockDim.x >= 256
+  const uint32_t r0 = min(threadIdx.x * per, nrep), r1 = min(r0 + per, nrep);
+  uint32_t loc[4], sum = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    loc[k] = r0 + k < r1 ? tiles(r0 + k) : 0u;
+    sum += loc[k];
+  }
+  uint32_t total;
+  uint32_t run = block_exclusive_scan(sum, s_w, &total);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if (r0 + k < r1) s_pre[r0 + k] = run;
+    run += loc[k];
+  }
+  if (threadIdx.x == 0) s_pre[nrep] = total;
+  __syncthreads();
+}
+
+// The replicate owning ticket t < s_pre[nrep].
+__device__ __forceinline__ uint32_t find_rep(const uint32_t* s_pre, uint32_t nrep, uint32_t t) {
+  uint32_t lo = 0, hi = nrep;  // s_pre[lo] <= t < s_pre[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (s_pre[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void copy16(void* dst, const void* src, int bytes, int i, int n) {
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int k = i; k < bytes / 16; k += n) d[k] = s[k];
+}
+static_assert(sizeof(StepCtx) % 16 == 0, "StepCtx is copied in 16-byte words");
 
 // ------------------------------------------------------------------------
 // Count pass
@@ -218,60 +301,117 @@ __device__ void issue_count_tile(const DevPool& src, uint8_t* st, uint64_t* bar,
   if (m & CA_FLAGS) bulk_load(st + 5 * kColBytes, src.flags + lo, b1, bar);
 }
 
+// One tile in flight or in work in a count stage. Everything but lt is the
+// replicate's and stays valid while the stage keeps serving that replicate.
+struct alignas(16) CountStage {
+  StepCtx c;
+  sampo_population pop;
+  DevPool src;
+  uint32_t* tileAgg;
+  uint32_t rep, lt, end, larv;    // replicate, its tile index, its pool end, larvicide on
+  uint32_t loaded;                // replicate whose c is loaded
+};
+
+// Dynamic shared memory of the persistent kernels: the two stages, then the
+// batch's ticket prefix (nrep + 1 words), sized at launch so that a single
+// simulation pays 8 bytes for it.
+constexpr size_t kCountSmem = 2 * kCountStage;
+constexpr size_t kScatterSmem = 2 * kScatterStage;
+__host__ __device__ constexpr size_t plan_bytes(uint32_t nrep) { return ((size_t)(nrep + 1) * 4 + 15) & ~(size_t)15; }
+
 __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
-  __shared__ SharedCtx S;
+  __shared__ CountStage s_cs[2];
+  __shared__ KillConst s_mc;
+  __shared__ uint32_t s_w[33];
+  uint32_t* s_pre = reinterpret_cast<uint32_t*>(dsm + kCountSmem);
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ uint32_t s_tick[2];
   __shared__ uint32_t s_wcnt[kWarps][8];
-  load_ctx(p, S);
-  const StepCtx& c = S.c;
-  SimDev* sim = p.sim;
-  const DevPool src = p.pool[S.cur];
-  const uint32_t end = S.pop.r[GRAVID].end;
-  const uint32_t ntiles = (end + kTile - 1) / kTile;
-  const bool larvicide = c.env.larvacideValue > 0.0f;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  load_model_const(&p.mc->kill, s_mc);
+  plan_tickets(p.nrep, s_pre, s_w, [&](uint32_t r) -> uint32_t {
+    const SimDev* sim = p.reps[r].sim;
+    return sim->active ? (sim->pop.r[GRAVID].end + kTile - 1) / kTile : 0u;
+  });
+  const uint32_t total = s_pre[p.nrep];
   Acc acc = {0, 0, 0, 0, 0, 0};
-  uint32_t cta_cnt = 0;  // thread b < 8: this CTA's survivors of next state b
+  uint32_t cta_cnt = 0;  // thread b < 8: this CTA's survivors of next state b in the current replicate
   uint32_t devoob = 0, phase = 0, pend = 0;  // pend (thread 0): stages with a copy in flight
+  uint32_t fail_rep = 0;
   bool failed = false;
+
+  // thread 0: take the next ticket into stage sidx and start its copies
+  auto claim = [&](uint32_t sidx) {
+    const uint32_t t = atomicAdd(&p.bat->ticket1, 1u);
+    s_tick[sidx] = t;
+    if (t >= total) return;
+    const uint32_t r = find_rep(s_pre, p.nrep, t);
+    CountStage& cs = s_cs[sidx];
+    if (cs.rep != r) {
+      const RepParams& rp = p.reps[r];
+      const SimDev* sim = rp.sim;
+      cs.rep = r;
+      cs.pop = sim->pop;
+      cs.end = cs.pop.r[GRAVID].end;
+      cs.src = rp.pool[sim->cur];
+      cs.tileAgg = rp.tileAgg;
+      cs.larv = sim->ctx.env.larvacideValue > 0.0f;
+    }
+    cs.lt = t - s_pre[r];
+    const uint32_t lo = cs.lt * kTile;
+    fence_proxy_async();  // the stage was last read through the generic proxy
+    issue_count_tile(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, min((uint32_t)kTile, cs.end - lo), cs.larv != 0);
+    pend |= 1u << sidx;
+  };
+  // all threads: the stage's step constants when its replicate changed (a
+  // uniform test); then synchronised
+  auto stage_ctx = [&](CountStage& cs) {
+    const uint32_t r = cs.rep;
+    if (cs.loaded == r) return;
+    copy16(&cs.c, &p.reps[r].sim->ctx, (int)sizeof(StepCtx), tid, kBlock);
+    __syncthreads();
+    if (tid == 0) cs.loaded = r;
+  };
+  // all threads: add this CTA's counts of replicate r to its totals
+  auto flush = [&](uint32_t r) {
+    SimDev* sim = p.reps[r].sim;
+    if (tid < 8 && cta_cnt) atomicAdd(&sim->cnt[tid], cta_cnt);
+    cta_cnt = 0;
+    const uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
+    if (lane == 0 && ne) atomicAdd(&sim->newEggs, ne);
+    const uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
+    if (lane == 0 && bad) atomicOr(&sim->error, bad);
+    acc.newEggs = 0; acc.bad = 0; devoob = 0;
+  };
 
   if (tid == 0) {
     mbar_init(&bars[0]);
     mbar_init(&bars[1]);
     fence_mbar_init();
-    fence_proxy_async();
-    const uint32_t t = atomicAdd(&sim->ticket1, 1u);
-    s_tick[0] = t;
-    if (t < ntiles) {
-      issue_count_tile(src, dsm, &bars[0], S.pop, t * kTile, min((uint32_t)kTile, end - t * kTile), larvicide);
-      pend |= 1u;
-    }
+    s_cs[0].loaded = s_cs[1].loaded = 0xffffffffu;
+    s_cs[0].rep = s_cs[1].rep = 0xffffffffu;
+    claim(0);
   }
+  __syncthreads();
+  if (s_tick[0] < total) stage_ctx(s_cs[0]);
   __syncthreads();
 
   for (uint32_t it = 0;; it++) {
     const uint32_t sidx = it & 1u;
     const uint32_t t = s_tick[sidx];
-    if (t >= ntiles) break;
+    if (t >= total) break;
+    const CountStage& cs = s_cs[sidx];
     uint8_t* st = dsm + sidx * kCountStage;
-    if (tid == 0) {  // prefetch the next tile into the other stage
-      const uint32_t t2 = atomicAdd(&sim->ticket1, 1u);
-      s_tick[sidx ^ 1u] = t2;
-      if (t2 < ntiles) {
-        fence_proxy_async();
-        issue_count_tile(src, dsm + (sidx ^ 1u) * kCountStage, &bars[sidx ^ 1u], S.pop, t2 * kTile,
-                         min((uint32_t)kTile, end - t2 * kTile), larvicide);
-        pend |= 2u >> sidx;
-      }
-    }
+    if (tid == 0) claim(sidx ^ 1u);  // prefetch the next tile into the other stage
     const bool ok = mbar_wait(&bars[sidx], (phase >> sidx) & 1u);
     if (ok) {
       phase ^= 1u << sidx;
       pend &= ~(1u << sidx);
     }
-    const uint32_t lo = t * kTile;
+    const StepCtx& c = cs.c;
+    const uint32_t end = cs.end, lo = cs.lt * kTile;
+    const bool larvicide = c.env.larvacideValue > 0.0f;
     const float* s_age = (const float*)(st + 0 * kColBytes);
     const float* s_his = (const float*)(st + 1 * kColBytes);
     const float* s_delay = (const float*)(st + 2 * kColBytes);
@@ -283,7 +423,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     for (int k = 0; k < kItems; k++) {
       const uint32_t i = k * kBlock + tid;
       const uint32_t g = lo + i;
-      const int rg = (ok && g < end) ? range_of(S.pop, g) : -1;
+      const int rg = (ok && g < end) ? range_of(cs.pop, g) : -1;
       if (rg >= 0) {
         Rec a;
         a.age = (rg == LARVA || rg >= IMMATURE) ? s_age[i] : 0.0f;
@@ -294,7 +434,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
         a.female = rg == MATESEEKING ? (s_flags[i] >> 3) & 1u : 0u;
         a.sporo = 0.0f; a.cycle = 0u; a.hbc = 0u; a.batches = 0u;
         devoob |= (rg == LARVA) & c.devOOB;
-        const int ns = update_agent<false>(c, rg, g, a, acc);
+        const int ns = update_agent<false>(c, s_mc, rg, g, a, acc);
         if (ns >= 0) {
           if (ns < 4) pk0 += 1u << (8 * ns);
           else pk1 += 1u << (8 * (ns - 4));
@@ -305,65 +445,111 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     pk1 = __reduce_add_sync(0xffffffffu, pk1);
     if (lane < 8) s_wcnt[warp][lane] = ((lane < 4 ? pk0 : pk1) >> (8 * (lane & 3))) & 0xffu;
     __syncthreads();
+    const uint32_t rep = cs.rep;
     if (tid < 8) {
       uint32_t sum = 0;
 #pragma unroll
       for (int w = 0; w < kWarps; w++) sum += s_wcnt[w][tid];
-      p.tileAgg[(size_t)t * 8 + tid] = sum;
+      cs.tileAgg[(size_t)cs.lt * 8 + tid] = sum;
       cta_cnt += sum;
     }
-    if (__syncthreads_or(!ok)) { failed = true; break; }
+    if (!ok) fail_rep = rep;
+    // the next tile was claimed above and is visible after the barrier
+    const bool more = s_tick[sidx ^ 1u] < total;
+    const bool sw = !more || s_cs[sidx ^ 1u].rep != rep;
+    if (sw) flush(rep);
+    if (more) stage_ctx(s_cs[sidx ^ 1u]);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      if (!sw) flush(rep);
+      break;
+    }
   }
   if (failed && tid == 0) {
-    atomicOr(&sim->error, SAMPO_DEV_ERR_TMA);
+    atomicOr(&p.reps[fail_rep].sim->error, SAMPO_DEV_ERR_TMA);
     for (int s = 0; s < 2; s++)  // let copies still in flight land before the CTA exits
       if ((pend >> s) & 1u) (void)mbar_wait(&bars[s], (phase >> s) & 1u);
   }
-  if (tid < 8 && cta_cnt) atomicAdd(&sim->cnt[tid], cta_cnt);
-  const uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
-  if (lane == 0 && ne) atomicAdd(&sim->newEggs, ne);
-  const uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
-  if (lane == 0 && bad) atomicOr(&sim->error, bad);
 }
 
 // ------------------------------------------------------------------------
-// Publishing the statistics of the pool a step starts from: L1de, female and
-// infective counts (calcStats, src/abms.c:230-310), the stats row, and the
-// larval hourly mortality for every larva age present this step
-// (kernel/killAgents.cl:117-133 depends on the age and L1de only). Run by one
-// CTA, all threads. Reads and clears the acc_* accumulators.
+// Publishing the start of a step for every replicate of p (one CTA each):
+// after a step, the next layout from the survivor counts
+// (kernel/oldToNewAgents.cl:57-95); then the pool's L1de, female and
+// infective counts (calcStats, src/abms.c:230-310), the stats row, the next
+// step's constants and the larval hourly mortality for every larva age
+// present (kernel/killAgents.cl:117-133 depends on the age and L1de only).
+// Reads and clears the acc_* accumulators; block 0 rearms the tickets.
+// mode PUB_REFRESH only recomputes the input-dependent step constants (the
+// inputs of the coming step may have been written after its publish).
 // ------------------------------------------------------------------------
-__device__ void publish_start(const KParams& p, const sampo_population& ranges, bool count_bnc) {
-  SimDev* sim = p.sim;
-  __shared__ uint32_t s_l1, s_dmin, s_dmax;
+__global__ void k_publish(KParams p, int mode) {
+  __shared__ uint32_t s_go, s_l1, s_dmin, s_dmax;
   __shared__ float s_cc;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.bat->ticket1 = 0u;
+    p.bat->ticket2 = 0u;
+  }
+  const RepParams& rp = p.reps[blockIdx.x];
+  SimDev* sim = rp.sim;
+  if (mode == PUB_REFRESH) {
+    if (threadIdx.x == 0 && sim->active) compute_ctx(rp, sim->pop, sim->step, sim->ctx);
+    return;
+  }
+  const bool after_step = mode == PUB_AFTER_STEP;
   if (threadIdx.x == 0) {
-    volatile SimDev* vs = sim;
-    sampo_population np = ranges;
-    uint32_t l1 = vs->acc_L1de;
-    np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? l1 : 0u;  // kernel/calcL1de.cl:259-280
-    np.numFemale = vs->acc_fem;
-    np.numPotentiallyInfective = vs->acc_inf;
-    sim->pop = np;
-    if (count_bnc) {
-      sim->bnc.numCyclesReported = vs->acc_bnc[0];
-      sim->bnc.sumCyclesReported = vs->acc_bnc[1];
-      sim->bnc.numBitesReported = vs->acc_bnc[2];
-      sim->bnc.numInfectBitesReported = vs->acc_bnc[3];
+    s_go = sim->active;
+    if (s_go) {
+      sampo_population np = sim->pop;
+      if (after_step) {
+        uint32_t cnt[8];
+        for (int k = 0; k < 8; k++) cnt[k] = sim->cnt[k];
+        const uint32_t ne = sim->newEggs;
+        // the reference's shared empty initial ranges (src/abms.c:204-219) make
+        // oldToNewAgents read one prefix-sum entry for several range ends
+        bool shared_end = false;
+        uint32_t moved = 0;
+        for (int k = 1; k < 8; k++) {
+          shared_end |= np.r[k].end == np.r[k - 1].end;
+          moved += cnt[k];
+        }
+        if (shared_end && moved) sim->warn |= SAMPO_DEV_WARN_REF_LAYOUT;
+        if (layout_fits(cnt, ne, sim->capacity)) {  // else the scatter pass flagged the capacity error
+          uint32_t base[8];
+          next_layout(cnt, ne, np, base);
+          sim->cur ^= 1u;
+        }
+        sim->step += 1u;
+        sim->epoch += 1u;
+        for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
+        sim->newEggs = 0;
+        sim->bnc.numCyclesReported = sim->acc_bnc[0];
+        sim->bnc.sumCyclesReported = sim->acc_bnc[1];
+        sim->bnc.numBitesReported = sim->acc_bnc[2];
+        sim->bnc.numInfectBitesReported = sim->acc_bnc[3];
+      }
+      np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? sim->acc_L1de : 0u;  // kernel/calcL1de.cl:259-280
+      np.numFemale = sim->acc_fem;
+      np.numPotentiallyInfective = sim->acc_inf;
+      sim->pop = np;
+      const uint32_t step = sim->step;
+      sampo_stats_row row;
+      row.pop = np;
+      row.bnc = sim->bnc;
+      rp.rows[step % rp.ring] = row;
+      s_l1 = np.numLarvae1DayEquiv;
+      s_dmin = sim->acc_dmin;
+      s_dmax = sim->acc_dmax;
+      s_cc = sim->cc;
+      sim->acc_L1de = 0; sim->acc_fem = 0; sim->acc_inf = 0;
+      sim->acc_dmin = 0xffffffffu; sim->acc_dmax = 0;
+      sim->acc_bnc[0] = sim->acc_bnc[1] = sim->acc_bnc[2] = sim->acc_bnc[3] = 0;
+      compute_ctx(rp, np, step, sim->ctx);
+      if (step >= sim->stop_step) sim->active = 0;
     }
-    sampo_stats_row row;
-    row.pop = np;
-    row.bnc = sim->bnc;
-    p.rows[sim->step % p.ring] = row;
-    s_l1 = np.numLarvae1DayEquiv;
-    s_dmin = vs->acc_dmin;
-    s_dmax = vs->acc_dmax;
-    s_cc = sim->cc;
-    sim->acc_L1de = 0; sim->acc_fem = 0; sim->acc_inf = 0;
-    sim->acc_dmin = 0xffffffffu; sim->acc_dmax = 0;
-    sim->acc_bnc[0] = sim->acc_bnc[1] = sim->acc_bnc[2] = sim->acc_bnc[3] = 0;
   }
   __syncthreads();
+  if (!s_go) return;
   for (int d = threadIdx.x; d < 100; d += blockDim.x) {
     float hmr = SAMPO_NAN_F;
     if ((uint32_t)d >= s_dmin && (uint32_t)d <= s_dmax) {
@@ -396,23 +582,29 @@ __device__ void issue_scatter_tile(const DevPool& src, uint8_t* st, uint64_t* ba
   bulk_load(st + 9 * kColBytes, src.flags + lo, b1, bar);
 }
 
-// Decoupled look-back for tile t by one warp over the count pass's tile
-// aggregates: sums earlier tiles' aggregates back to the nearest published
-// inclusive prefix (no waiting). Lane 0 publishes t's inclusive prefix.
-// Every lane returns the exclusive prefix ex[] and t's counts cnt[].
-__device__ void tile_lookback(const KParams& p, uint32_t t, uint32_t epoch, int lane, uint32_t ex[8], uint32_t cnt[8]) {
+// Decoupled look-back for tile t of one replicate by one warp over the count
+// pass's tile aggregates: sums earlier tiles' aggregates back to the nearest
+// published inclusive prefix (no waiting). Lane 0 publishes t's inclusive
+// prefix. Every lane returns the exclusive prefix ex[] and t's counts cnt[].
+struct LookbackArrays {
+  uint32_t* agg;   // count pass tile aggregates
+  uint32_t* incl;  // inclusive prefixes
+  uint32_t* flag;  // epoch flags
+};
+
+__device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epoch, int lane, uint32_t ex[8], uint32_t cnt[8]) {
 #pragma unroll
   for (int b = 0; b < 8; b++) ex[b] = 0;
   int64_t pos = (int64_t)t - 1;
   while (pos >= 0) {
     const int64_t idx = pos - lane;
     const bool valid = idx >= 0;
-    const uint32_t f = valid ? ld_acquire_u32(&p.tileFlag[idx]) : 0u;
+    const uint32_t f = valid ? ld_acquire_u32(&rp.flag[idx]) : 0u;
     const uint32_t m = __ballot_sync(0xffffffffu, !valid || f == epoch);
     const int stop = m ? __ffs(m) - 1 : 32;
     uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
     if (valid && lane <= stop) {
-      const uint32_t* q = (lane == stop ? p.tileIncl : p.tileAgg) + (size_t)idx * 8;
+      const uint32_t* q = (lane == stop ? rp.incl : rp.agg) + (size_t)idx * 8;
       v0 = ld_cg_v4(q);
       v1 = ld_cg_v4(q + 4);
     }
@@ -423,13 +615,13 @@ __device__ void tile_lookback(const KParams& p, uint32_t t, uint32_t epoch, int 
     if (m) break;
     pos -= 32;
   }
-  const uint32_t* ag = p.tileAgg + (size_t)t * 8;
+  const uint32_t* ag = rp.agg + (size_t)t * 8;
   const uint4 a0 = ld_cg_v4(ag), a1 = ld_cg_v4(ag + 4);
   cnt[0] = a0.x; cnt[1] = a0.y; cnt[2] = a0.z; cnt[3] = a0.w; cnt[4] = a1.x; cnt[5] = a1.y; cnt[6] = a1.z; cnt[7] = a1.w;
   if (lane == 0) {
-    st_cg_v4(p.tileIncl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
-    st_cg_v4(p.tileIncl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
-    st_release_u32(&p.tileFlag[t], epoch);
+    st_cg_v4(rp.incl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
+    st_cg_v4(rp.incl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
+    st_release_u32(&rp.flag[t], epoch);
   }
 }
 
@@ -446,93 +638,140 @@ constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one pr
 static_assert(kBlock == 256, "consumer_sync() names 256 threads");
 enum : uint32_t { TK_OLD = 0, TK_EGG = 1, TK_END = 2 };
 
+// What the producer warp hands the consumers with a stage. The replicate's
+// part (c .. base) is reloaded only when the stage changes replicate.
+struct alignas(16) ScatterStage {
+  StepCtx c;                 // the replicate's step constants
+  sampo_population pop;      // its current ranges
+  DevPool dst, src;          // its next and current buffers
+  LookbackArrays lb;         // its look-back arrays
+  uint32_t rep, end, newEggs, nold, epoch;  // replicate, pool end, eggs laid, old tiles, look-back epoch
+  uint32_t base[8];          // first slot of each next-state range
+  uint32_t kind, lo;         // TK_*, first slot (old tile) or first egg id (egg tile)
+  uint32_t d0[8], sb[8], cnt[8];  // per next state: first slot, staging start, survivors
+};
+
 // The producer warp keeps two tiles in flight ahead of the consumers: it
 // takes tickets, issues the TMA loads, runs the look-back and lays out the
-// staging runs (full[s]: its expect-tx arrival + one arrival once the layout
-// is written); after the consumers have staged a tile (empty[s]: 256
-// arrivals) it sends the runs with bulk stores and refills the stage.
+// staging runs (full[s]: its expect-tx arrival + one arrival once the stage
+// description is written); after the consumers have staged a tile (empty[s]:
+// 256 arrivals) it sends the runs with bulk stores and refills the stage.
 __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
-  __shared__ SharedCtx S;
+  __shared__ ScatterStage s_si[2];
+  __shared__ ModelConst s_mc;
+  __shared__ uint32_t s_w[33];
+  uint32_t* s_pre = reinterpret_cast<uint32_t*>(dsm + kScatterSmem);
   __shared__ __align__(8) uint64_t full[2], empty[2];
-  __shared__ sampo_population s_np;
-  __shared__ uint32_t s_base[8], s_newEggs, s_ok, s_last, s_tick[2], s_fullok[2];
-  __shared__ uint32_t s_d0[2][8], s_sb[2][8], s_cnt[2][8];  // per stage and next state: first slot, staging start, survivors
+  __shared__ uint32_t s_fullok[2];
   __shared__ uint32_t s_off[kItems][kWarps][8];
-  __shared__ uint32_t s_red[kWarps][8];
-  __shared__ uint32_t s_mn[kWarps], s_mx[kWarps];
   __shared__ uint32_t s_bmq[kTile], s_bmn;  // owed Box-Muller draws: staging slot | item << 11 | kind << 21
-  load_ctx(p, S);
-  const StepCtx& c = S.c;
-  SimDev* sim = p.sim;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
+  load_model_const(p.mc, s_mc);
+  plan_tickets(p.nrep, s_pre, s_w, [&](uint32_t r) -> uint32_t {
+    SimDev* sim = p.reps[r].sim;
+    if (!sim->active) return 0u;
     uint32_t cnt[8];
     for (int k = 0; k < 8; k++) cnt[k] = sim->cnt[k];
-    s_newEggs = sim->newEggs;
-    next_layout(cnt, s_newEggs, s_np, s_base);
-    uint64_t tot = (uint64_t)s_newEggs + cnt[0];
-    bool ok = tot <= 0xffffffffull;
-    uint64_t e = tot;
-    for (int k = 1; k < 8; k++) e = ((e + kLayoutAlign) / kLayoutAlign) * kLayoutAlign + cnt[k];
-    ok = ok && e <= (uint64_t)sim->capacity;
-    s_ok = ok;
-    if (!ok && blockIdx.x == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
+    const uint32_t ne = sim->newEggs;
+    if (!layout_fits(cnt, ne, sim->capacity)) {
+      if (blockIdx.x == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
+      return 0u;
+    }
+    return (sim->pop.r[GRAVID].end + kTile - 1) / kTile + (ne + kTile - 1) / kTile;
+  });
+  const uint32_t total = s_pre[p.nrep];
+  if (tid == 0) {
     mbar_init_count(&full[0], 2);
     mbar_init_count(&full[1], 2);
     mbar_init_count(&empty[0], kBlock);
     mbar_init_count(&empty[1], kBlock);
     fence_mbar_init();
+    s_si[0].rep = s_si[1].rep = 0xffffffffu;
   }
   __syncthreads();
-  const DevPool src = p.pool[S.cur];
-  const DevPool dst = p.pool[S.cur ^ 1];
-  const uint32_t end = S.pop.r[GRAVID].end;
-  const uint32_t nold = s_ok ? (end + kTile - 1) / kTile : 0u;
-  const uint32_t negg = s_ok ? (s_newEggs + kTile - 1) / kTile : 0u;
-  const uint32_t ntot = nold + negg;
-  const uint32_t epoch = S.epoch;
 
-  Acc acc = {0, 0, 0, 0, 0, 0};
-  uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0, fail = 0;
-
+  uint32_t fail = 0, fail_rep = 0;
   if (warp == kWarps) {
     // ================= producer warp =================
     // fill stage s with the next ticket's tile; returns its kind
     auto fill = [&](uint32_t s) -> uint32_t {
       uint32_t t = 0;
-      if (lane == 0) {
-        t = atomicAdd(&sim->ticket2, 1u);
-        s_tick[s] = t;
-      }
+      if (lane == 0) t = atomicAdd(&p.bat->ticket2, 1u);
       t = __shfl_sync(0xffffffffu, t, 0);
-      if (t < nold) {
+      ScatterStage& si = s_si[s];
+      if (t >= total) {
+        if (lane == 0) {
+          si.kind = TK_END;
+          mbar_arrive(&full[s]);
+          mbar_arrive(&full[s]);
+        }
+        return TK_END;
+      }
+      const uint32_t r = find_rep(s_pre, p.nrep, t);
+      const uint32_t j = t - s_pre[r];
+      if (si.rep != r) {  // uniform: the stage's replicate data, once per replicate
+        const RepParams& rp = p.reps[r];
+        SimDev* sim = rp.sim;
+        copy16(&si.c, &sim->ctx, (int)sizeof(StepCtx), lane, 32);
+        if (lane == 0) {
+          const uint32_t cur = sim->cur, ne = sim->newEggs;
+          si.pop = sim->pop;
+          si.end = si.pop.r[GRAVID].end;
+          si.nold = (si.end + kTile - 1) / kTile;
+          si.newEggs = ne;
+          si.epoch = sim->epoch;
+          si.src = rp.pool[cur];
+          si.dst = rp.pool[cur ^ 1u];
+          si.lb.agg = rp.tileAgg;
+          si.lb.incl = rp.tileIncl;
+          si.lb.flag = rp.tileFlag;
+          uint32_t tc[8], base[8];
+          for (int k = 0; k < 8; k++) tc[k] = sim->cnt[k];
+          sampo_population np;
+          next_layout(tc, ne, np, base);
+          for (int k = 0; k < 8; k++) si.base[k] = base[k];
+        }
+        __syncwarp();
+        if (lane == 0) si.rep = r;
+        __syncwarp();
+      }
+      const uint32_t end = si.end, nold = si.nold;
+      if (j < nold) {
         if (lane == 0) {
           fence_proxy_async();  // the stage was last written through the generic proxy
-          issue_scatter_tile(src, dsm + s * kScatterStage, &full[s], t * kTile, min((uint32_t)kTile, end - t * kTile));
+          issue_scatter_tile(si.src, dsm + s * kScatterStage, &full[s], j * kTile, min((uint32_t)kTile, end - j * kTile));
         }
         uint32_t ex[8], cnt[8];
-        tile_lookback(p, t, epoch, lane, ex, cnt);
+        tile_lookback(si.lb, j, si.epoch, lane, ex, cnt);
         if (lane == 0) {
           uint32_t pos = 0;
 #pragma unroll
           for (int b = 0; b < 8; b++) {
-            const uint32_t d0 = s_base[b] + ex[b];
+            const uint32_t d0 = si.base[b] + ex[b];
             const uint32_t sb = ((pos + 15u) & ~15u) + (d0 & 15u);
-            s_d0[s][b] = d0;
-            s_sb[s][b] = sb;
-            s_cnt[s][b] = cnt[b];
+            si.d0[b] = d0;
+            si.sb[b] = sb;
+            si.cnt[b] = cnt[b];
             pos = sb + cnt[b];
           }
-          mbar_arrive(&full[s]);  // layout written (release)
+          si.kind = TK_OLD;
+          si.lo = j * kTile;
         }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&full[s]);  // stage described (release)
         return TK_OLD;
       }
+      if (lane == 0) {
+        si.kind = TK_EGG;
+        si.lo = (j - nold) * kTile;
+      }
+      __syncwarp();
       if (lane == 0) {
         mbar_arrive(&full[s]);
         mbar_arrive(&full[s]);
       }
-      return t < ntot ? TK_EGG : TK_END;
+      return TK_EGG;
     };
     uint32_t kind0 = fill(0), kind1 = fill(1), ph = 0;
     for (uint32_t it = 0;; it++) {
@@ -542,7 +781,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
       uint32_t ok = 1;
       if (lane == 0) ok = mbar_wait(&empty[s], (ph >> s) & 1u) ? 1u : 0u;
       ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) { fail = 1; break; }
+      if (!ok) { fail = 1; fail_rep = s_si[s].rep; break; }
       ph ^= 1u << s;
       if (k == TK_OLD && lane == 0) {
         // ---- each state's run to its slots in the next buffer ----
@@ -550,11 +789,13 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         // every run and column leaves with one bulk store; the consumers
         // wrote the unaligned heads and tails. Runs lie inside the next
         // layout by construction (d0 + count <= range end).
+        const ScatterStage& si = s_si[s];
+        const DevPool& dst = si.dst;
         uint8_t* st = dsm + s * kScatterStage;
         fence_proxy_async();  // staging written through the generic proxy
 #pragma unroll 1
         for (int b = 0; b < 8; b++) {
-          const uint32_t n = s_cnt[s][b], d0 = s_d0[s][b], sb = s_sb[s][b];
+          const uint32_t n = si.cnt[b], d0 = si.d0[b], sb = si.sb[b];
           if (!n) continue;
           const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
           if (n4) {
@@ -583,6 +824,33 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     if (lane == 0) bulk_wait_all();  // this CTA's bulk stores are complete
   } else {
     // ================= consumer warps =================
+    const ModelConst& mc = s_mc;
+    Acc acc = {0, 0, 0, 0, 0, 0};
+    uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0;
+    uint32_t cur_rep = 0xffffffffu;
+    // this warp's statistics of replicate r into its totals
+    auto flush = [&](uint32_t r) {
+      SimDev* sim = p.reps[r].sim;
+      uint32_t v[8] = {l1, fem, inf, acc.cycles, acc.sumCycles, acc.bites, acc.infectBites,
+                       (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u)};
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = j == 7 ? __reduce_or_sync(0xffffffffu, v[j]) : __reduce_add_sync(0xffffffffu, v[j]);
+      const uint32_t mn = __reduce_min_sync(0xffffffffu, dmin), mx = __reduce_max_sync(0xffffffffu, dmax);
+      if (lane == 0) {
+        if (v[0]) atomicAdd(&sim->acc_L1de, v[0]);
+        if (v[1]) atomicAdd(&sim->acc_fem, v[1]);
+        if (v[2]) atomicAdd(&sim->acc_inf, v[2]);
+        if (v[3]) atomicAdd(&sim->acc_bnc[0], v[3]);
+        if (v[4]) atomicAdd(&sim->acc_bnc[1], v[4]);
+        if (v[5]) atomicAdd(&sim->acc_bnc[2], v[5]);
+        if (v[6]) atomicAdd(&sim->acc_bnc[3], v[6]);
+        if (v[7]) atomicOr(&sim->error, v[7]);
+        if (mn != 0xffffffffu) { atomicMin(&sim->acc_dmin, mn); atomicMax(&sim->acc_dmax, mx); }
+      }
+      acc = Acc{0, 0, 0, 0, 0, 0};
+      l1 = fem = inf = dmax = tilebad = 0;
+      dmin = 0xffffffffu;
+    };
     uint32_t ph = 0;
     for (uint32_t it = 0;; it++) {
       const uint32_t s = it & 1u;
@@ -593,12 +861,19 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         s_fullok[s] = mbar_wait(&full[s], (ph >> s) & 1u) ? 1u : 0u;
       }
       consumer_sync();
-      if (!s_fullok[s]) { fail = 1; break; }
+      if (!s_fullok[s]) { fail = 1; fail_rep = cur_rep == 0xffffffffu ? 0u : cur_rep; break; }
       (void)mbar_try_wait(&full[s], (ph >> s) & 1u);  // the completed phase, observed by this thread
       ph ^= 1u << s;
-      const uint32_t t = s_tick[s];
-      if (t >= ntot) break;
-      if (t < nold) {
+      const ScatterStage& si = s_si[s];
+      const uint32_t kind = si.kind;
+      if (kind == TK_END) break;
+      if (si.rep != cur_rep) {
+        if (cur_rep != 0xffffffffu) flush(cur_rep);
+        cur_rep = si.rep;
+      }
+      const StepCtx& c = si.c;
+      const DevPool& dst = si.dst;
+      if (kind == TK_OLD) {
         // ---- recompute the step for the tile's agents (inputs from shared memory) ----
         const float* c_age = (const float*)(st + 0 * kColBytes);
         const float* c_his = (const float*)(st + 1 * kColBytes);
@@ -610,7 +885,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
         const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
         const uint8_t* c_flags = st + 9 * kColBytes;
-        const uint32_t lo = t * kTile;
+        const uint32_t lo = si.lo, end = si.end;
         Rec a[kItems];
         int nb[kItems];
         uint32_t rk[kItems];
@@ -618,7 +893,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         for (int k = 0; k < kItems; k++) {
           const uint32_t i = k * kBlock + tid;
           const uint32_t g = lo + i;
-          const int rg = g < end ? range_of(S.pop, g) : -1;
+          const int rg = g < end ? range_of(si.pop, g) : -1;
           nb[k] = 8;
           a[k].bm = BM_NONE;
           if (rg >= 0) {
@@ -626,7 +901,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
             a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
             a[k].batches = c_batches[i];
             a[k].female = (c_flags[i] >> 3) & 1u;
-            const int ns = update_agent<true>(c, rg, g, a[k], acc);
+            const int ns = update_agent<true>(c, mc.kill, rg, g, a[k], acc);
             if (ns >= 0) nb[k] = ns;
           }
           const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
@@ -645,7 +920,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
             if (lane >= o) incl += y;
           }
           (&s_off[0][0][0])[lane * 8 + b] = incl - v;
-          if (lane == 31 && incl != s_cnt[s][b]) tilebad = 1;
+          if (lane == 31 && incl != si.cnt[b]) tilebad = 1;
         }
         consumer_sync();
         float* g_age = (float*)(st + 0 * kStg * 4);
@@ -665,7 +940,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           uint32_t q = 0xffffffffu;
           if (b < 8) {
             const uint32_t j = s_off[k][warp][b] + rk[k];
-            if (j < s_cnt[s][b]) q = s_sb[s][b] + j;
+            if (j < si.cnt[b]) q = si.sb[b] + j;
             else tilebad = 1;  // the two passes disagree: stay inside this state's run
           }
           // queue the owed Box-Muller draws (warp-aggregated slot reservation)
@@ -699,9 +974,9 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         if (nbm) {
           for (uint32_t j = tid; j < nbm; j += kBlock) {
             const uint32_t e = s_bmq[j];
-            const uint32_t q = e & 2047u, kind = e >> 21;
-            const uint32_t v = finish_box_muller(c, lo + ((e >> 11) & 1023u), kind, g_batches[q]);
-            if (kind == BM_LARVA_DELAY) g_delay[q] = __uint_as_float(v);
+            const uint32_t q = e & 2047u, kind_bm = e >> 21;
+            const uint32_t v = finish_box_muller(c, mc, lo + ((e >> 11) & 1023u), kind_bm, g_batches[q]);
+            if (kind_bm == BM_LARVA_DELAY) g_delay[q] = __uint_as_float(v);
             else g_avail[q] = v;
           }
           consumer_sync();
@@ -710,7 +985,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         //      elements, of which the four-byte columns need at most 3 + 3 ----
         {
           const int b = warp, e = lane;
-          const uint32_t n = s_cnt[s][b], d0 = s_d0[s][b], sb = s_sb[s][b];
+          const uint32_t n = si.cnt[b], d0 = si.d0[b], sb = si.sb[b];
           const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
           const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
           const uint32_t j = (uint32_t)e < h1 ? (uint32_t)e : h1 + n1 + ((uint32_t)e - h1);
@@ -726,11 +1001,11 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         }
       } else {
         // ---- new eggs at [0, newEggs) of the next buffer ----
-        const uint32_t e0 = (t - nold) * kTile;
+        const uint32_t e0 = si.lo, ne = si.newEggs;
 #pragma unroll
         for (int k = 0; k < kItems; k++) {
           const uint32_t id = e0 + k * kBlock + tid;
-          if (id < s_newEggs) {
+          if (id < ne) {
             Rec a;
             new_egg(c, id, a);
             dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
@@ -742,75 +1017,19 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
       }
       mbar_arrive(&empty[s]);  // staged (release): the producer may send and refill the stage
     }
-  }
-  if (fail) atomicOr(&sim->error, SAMPO_DEV_ERR_TMA);
-  __syncthreads();
-
-  // ---- per-CTA reduction of the accumulators, one atomic each ----
-  {
-    uint32_t v[8] = {l1, fem, inf, acc.cycles, acc.sumCycles, acc.bites, acc.infectBites,
-                     (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u)};
-#pragma unroll
-    for (int j = 0; j < 8; j++) v[j] = j == 7 ? __reduce_or_sync(0xffffffffu, v[j]) : __reduce_add_sync(0xffffffffu, v[j]);
-    const uint32_t mn = __reduce_min_sync(0xffffffffu, dmin), mx = __reduce_max_sync(0xffffffffu, dmax);
-    if (lane == 0 && warp < kWarps) {
-#pragma unroll
-      for (int j = 0; j < 8; j++) s_red[warp][j] = v[j];
-      s_mn[warp] = mn;
-      s_mx[warp] = mx;
+    if (cur_rep != 0xffffffffu) flush(cur_rep);
+    if (fail && tid == 0) {
+      // let loads still in flight land before the CTA exits (bounded waits)
+      for (int s = 0; s < 2; s++) (void)mbar_wait(&full[s], (ph >> s) & 1u);
     }
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0}, rmn = 0xffffffffu, rmx = 0;
-      for (int w = 0; w < kWarps; w++) {
-        for (int j = 0; j < 7; j++) r[j] += s_red[w][j];
-        r[7] |= s_red[w][7];
-        rmn = min(rmn, s_mn[w]); rmx = max(rmx, s_mx[w]);
-      }
-      if (r[0]) atomicAdd(&sim->acc_L1de, r[0]);
-      if (r[1]) atomicAdd(&sim->acc_fem, r[1]);
-      if (r[2]) atomicAdd(&sim->acc_inf, r[2]);
-      if (r[3]) atomicAdd(&sim->acc_bnc[0], r[3]);
-      if (r[4]) atomicAdd(&sim->acc_bnc[1], r[4]);
-      if (r[5]) atomicAdd(&sim->acc_bnc[2], r[5]);
-      if (r[6]) atomicAdd(&sim->acc_bnc[3], r[6]);
-      if (r[7]) atomicOr(&sim->error, r[7]);
-      if (rmn != 0xffffffffu) { atomicMin(&sim->acc_dmin, rmn); atomicMax(&sim->acc_dmax, rmx); }
-      __threadfence();
-      s_last = atomicAdd(&sim->done2, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
   }
-  if (!s_last) return;
-
-  // ---- epilogue: the last CTA publishes the next step's start ----
-  __threadfence();
-  if (tid == 0) {
-    // the reference's shared empty initial ranges (src/abms.c:204-219) make
-    // oldToNewAgents read one prefix-sum entry for several range ends
-    const sampo_population& op = S.pop;
-    bool shared_end = false;
-    for (int k = 1; k < 8; k++) shared_end |= op.r[k].end == op.r[k - 1].end;
-    uint32_t moved = 0;
-    for (int k = 1; k < 8; k++) moved += sim->cnt[k];
-    if (shared_end && moved) atomicOr(&sim->warn, SAMPO_DEV_WARN_REF_LAYOUT);
-    if (s_ok) sim->cur = S.cur ^ 1u;
-    sim->step = S.step + 1u;
-    sim->epoch = S.epoch + 1u;
-    for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
-    sim->newEggs = 0;
-    sim->ticket1 = 0;
-    sim->ticket2 = 0;
-    sim->done2 = 0;
-  }
-  __syncthreads();
-  if (s_ok) publish_start(p, s_np, true);
-  else publish_start(p, S.pop, true);
+  if (fail && (lane == 0)) atomicOr(&p.reps[fail_rep].sim->error, SAMPO_DEV_ERR_TMA);
 }
 
 // ------------------------------------------------------------------------
-// Initial population: initAgents over [0, n) (kernel/initAgents.cl:26-65),
-// optionally with ages 24*U{0..age_days_max} from splitmix64 (an extension).
+// Initial population of p.reps[0]: initAgents over [0, n)
+// (kernel/initAgents.cl:26-65), optionally with ages 24*U{0..age_days_max}
+// from splitmix64 (an extension).
 // ------------------------------------------------------------------------
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   z += 0x9E3779B97F4A7C15ULL;
@@ -830,7 +1049,7 @@ __global__ void k_init_eggs(KParams p, uint32_t n, float T0, const sampo_seeds* 
     c.eggIncubation = -0.923f * T0 + 60.923f;
   }
   __syncthreads();
-  const DevPool dst = p.pool[0];
+  const DevPool dst = p.reps[0].pool[0];
   for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
     Rec a;
     new_egg(c, id, a);
@@ -846,11 +1065,11 @@ __global__ void k_init_eggs(KParams p, uint32_t n, float T0, const sampo_seeds* 
   }
 }
 
-// Statistics of the current pool (grid-stride), accumulated into acc_*.
+// Statistics of p.reps[0]'s current pool (grid-stride), accumulated into acc_*.
 __global__ void k_pool_stats(KParams p) {
-  SimDev* sim = p.sim;
+  SimDev* sim = p.reps[0].sim;
   const sampo_population pop = sim->pop;
-  const DevPool src = p.pool[sim->cur];
+  const DevPool src = p.reps[0].pool[sim->cur];
   uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0;
   const uint32_t end = pop.r[GRAVID].end;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < end; g += gridDim.x * blockDim.x) {
@@ -877,22 +1096,15 @@ __global__ void k_pool_stats(KParams p) {
   }
 }
 
-__global__ void k_publish_start(KParams p) {
-  __shared__ sampo_population ranges;
-  if (threadIdx.x == 0) ranges = p.sim->pop;
-  __syncthreads();
-  publish_start(p, ranges, false);
-}
-
-// ageHistogram (kernel/ageHistogram.cl:13-35) with warp-aggregated shared
-// atomics: lanes that fall in the same bin add once.
+// ageHistogram (kernel/ageHistogram.cl:13-35) of p.reps[0] with
+// warp-aggregated shared atomics: lanes that fall in the same bin add once.
 __global__ void k_histogram(KParams p, uint32_t* hist) {
   __shared__ uint32_t h[100];
   for (int k = threadIdx.x; k < 100; k += blockDim.x) h[k] = 0;
   __syncthreads();
-  SimDev* sim = p.sim;
+  SimDev* sim = p.reps[0].sim;
   const sampo_population pop = sim->pop;
-  const DevPool src = p.pool[sim->cur];
+  const DevPool src = p.reps[0].pool[sim->cur];
   const uint32_t lo = pop.r[IMMATURE].start, hi = pop.r[GRAVID].end;
   const uint32_t span = hi > lo ? hi - lo : 0u;
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -940,36 +1152,37 @@ static int sm_count() {
   }
   return sms;
 }
-constexpr size_t kCountSmem = 2 * kCountStage;
-constexpr size_t kScatterSmem = 2 * kScatterStage;
-
 static void set_smem_attrs() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCountSmem);
-  cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+  cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kCountSmem + plan_bytes(kMaxRep)));
+  cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kScatterSmem + plan_bytes(kMaxRep)));
   done = true;
 }
-int grid_blocks_count() {
+int grid_blocks_count(uint32_t nrep) {
   set_smem_attrs();
   int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_count, kBlock, kCountSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_count, kBlock, kCountSmem + plan_bytes(nrep));
   return sm_count() * (per > 0 ? per : 1);
 }
-int grid_blocks_scatter() {
+int grid_blocks_scatter(uint32_t nrep) {
   set_smem_attrs();
   int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kScatterThreads, kScatterSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, kScatterThreads, kScatterSmem + plan_bytes(nrep));
   return sm_count() * (per > 0 ? per : 1);
 }
 cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
   set_smem_attrs();
-  k_count<<<grid, kBlock, kCountSmem, st>>>(p);
+  k_count<<<grid, kBlock, kCountSmem + plan_bytes(p.nrep), st>>>(p);
   return cudaGetLastError();
 }
 cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
   set_smem_attrs();
-  k_scatter<<<grid, kScatterThreads, kScatterSmem, st>>>(p);
+  k_scatter<<<grid, kScatterThreads, kScatterSmem + plan_bytes(p.nrep), st>>>(p);
+  return cudaGetLastError();
+}
+cudaError_t launch_publish(const KParams& p, int mode, cudaStream_t st) {
+  k_publish<<<p.nrep, mode == PUB_REFRESH ? 32 : 128, 0, st>>>(p, mode);
   return cudaGetLastError();
 }
 cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev, int age_days_max,
@@ -979,7 +1192,7 @@ cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo
 }
 cudaError_t launch_publish_start(const KParams& p, cudaStream_t st) {
   k_pool_stats<<<sm_count() * 4, 256, 0, st>>>(p);
-  k_publish_start<<<1, 128, 0, st>>>(p);
+  k_publish<<<1, 128, 0, st>>>(p, PUB_INITIAL);
   return cudaGetLastError();
 }
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st) {

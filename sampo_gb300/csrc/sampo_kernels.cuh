@@ -1,6 +1,13 @@
 // sampo_kernels.cuh - device state shared by the kernels and the host API.
+//
+// The kernels step a batch of independent simulations ("replicates") at
+// once: every replicate has its own pool buffers, state, look-back arrays and
+// input rings (RepParams), and the persistent kernels hand out tiles of all
+// active replicates from one ticket counter. A single simulation is a batch
+// of one.
 #pragma once
 #include <stdint.h>
+#include <string.h>
 #include "../../include/sampo.h"
 #include "sampo_math.h"
 #include "sampo_model.cuh"
@@ -11,6 +18,7 @@ constexpr int kBlock = 256;                 // threads per CTA
 constexpr int kItems = 4;                   // slots per thread per tile (striped by kBlock)
 constexpr int kTile = kBlock * kItems;      // slots per tile
 constexpr int kWarps = kBlock / 32;
+constexpr uint32_t kMaxRep = 1024;          // replicates per batch
 
 // One pool buffer: structure of arrays, one column per agent field.
 struct DevPool {
@@ -28,21 +36,26 @@ struct SimDev {
   uint32_t epoch;             // look-back flag value of the running step (never reused)
   uint32_t cnt[8];            // count pass: survivors by next state
   uint32_t newEggs;           // count pass: eggs laid (EggsNbiomass.newEggs)
-  uint32_t ticket1;           // count pass tile ticket
-  uint32_t ticket2, done2;    // scatter pass tile ticket / finished CTAs
   uint32_t acc_bnc[4];        // scatter pass: numCycles, sumCycles, numBites, numInfectBites
   uint32_t acc_L1de, acc_fem, acc_inf, acc_dmin, acc_dmax;  // stats of the next pool
   uint32_t error;             // sticky SAMPO_DEV_ERR_* bits
   uint32_t warn;              // sticky SAMPO_DEV_WARN_* bits
   uint32_t capacity;
   float cc;                   // carrying capacity (constant per run, src/abms.c:19,132)
-  float aquaticHMR;
-  float adultHMR[100];
-  float larvaHMR[100];        // for the current step; NaN outside the larvae's age range
-  float eggBatchScale[kEggBatchTable];
+  uint32_t active;            // 1: the replicate takes part in the batch's steps
+  uint32_t stop_step;         // becomes inactive once step reaches this
+  StepCtx ctx;                // constants of step `step` (valid while active)
+  float larvaHMR[100];        // larval hourly mortality of step `step` by age in days
 };
 
-struct KParams {
+// Batch-wide counters of the persistent kernels (reset by k_publish).
+struct BatchDev {
+  uint32_t ticket1;           // count pass tile ticket
+  uint32_t ticket2;           // scatter pass tile ticket
+};
+
+// Everything the kernels need of one replicate.
+struct RepParams {
   SimDev* sim;
   DevPool pool[2];
   uint32_t* tileAgg;          // [maxTiles][8] per-tile survivor counts (count pass)
@@ -57,32 +70,59 @@ struct KParams {
   uint32_t maxTiles;
 };
 
+struct KParams {
+  const RepParams* reps;      // device array [nrep]
+  uint32_t nrep;
+  BatchDev* bat;
+  const ModelConst* mc;
+};
+
 // Hourly mortality tables that do not change during a run
 // (kernel/killAgents.cl:84-115,135-147), computed on the host with the same
 // deterministic functions the device uses.
-inline void fill_constant_tables(SimDev& h) {
+inline void fill_constant_tables(ModelConst& h) {
   for (int d = 0; d < 100; d++) {
     const float a = 0.1f, B = 25.0f, sg = 0.1f;
     float e = sampo_expf((float)(uint32_t)d / B);
     float dmr = (a * e) / (1.0f + (a * B * sg * (e - 1.0f)));
     float dsr = 1.0f - dmr;
     float hsr = sampo_powf(dsr, 1.0f / 24.0f);
-    h.adultHMR[d] = 1.0f - hsr;
-    h.larvaHMR[d] = SAMPO_NAN_F;
+    h.kill.adultHMR[d] = 1.0f - hsr;
   }
   float dmr = 0.1f;
   float dsr = 1.0f - dmr;
-  h.aquaticHMR = 1.0f - sampo_powf(dsr, 1.0f / 24.0f);
+  h.kill.aquaticHMR = 1.0f - sampo_powf(dsr, 1.0f / 24.0f);
   for (uint32_t k = 0; k < kEggBatchTable; k++) h.eggBatchScale[k] = egg_batch_scale(k);
 }
 
-// Launch helpers (sampo_kernels.cu).
-int grid_blocks_count();
-int grid_blocks_scatter();
+// Initial device state of a simulation (before its pool is published).
+inline SimDev initial_sim_state(uint32_t capacity, float cc) {
+  SimDev h;
+  memset(&h, 0, sizeof(h));
+  h.capacity = capacity;
+  h.cc = cc;
+  h.acc_dmin = 0xffffffffu;
+  h.epoch = 1;
+  h.stop_step = 0xffffffffu;
+  return h;
+}
+
+// Launch helpers (sampo_kernels.cu). The step kernels take every replicate of
+// p; init, pool statistics and the histogram take p.reps[0] only.
+// persistent grid sizes (CTAs resident on all SMs) for batches of nrep replicates
+int grid_blocks_count(uint32_t nrep);
+int grid_blocks_scatter(uint32_t nrep);
 cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st);
 cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st);
+// k_publish over every replicate of p: PUB_AFTER_STEP turns the step's counts
+// into the next pool's start; PUB_INITIAL publishes the current pool (after
+// init/load); PUB_REFRESH recomputes the coming step's input-dependent
+// constants (run it after writing that step's inputs).
+enum : int { PUB_INITIAL = 0, PUB_AFTER_STEP = 1, PUB_REFRESH = 2 };
+cudaError_t launch_publish(const KParams& p, int mode, cudaStream_t st);
 cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev,
                              int age_days_max, uint64_t age_seed, cudaStream_t st);
+// statistics of p.reps[0]'s current pool, then its publish (PUB_INITIAL)
 cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);

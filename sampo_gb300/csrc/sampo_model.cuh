@@ -45,8 +45,22 @@ struct Rec {
 // evaluates them afterwards in dense warps (finish_box_muller).
 enum : uint32_t { BM_NONE = 0, BM_LARVA_DELAY = 1, BM_EGG_BATCH = 2 };
 
-// Per-step constants shared by every agent of a step (lives in shared memory).
-struct StepCtx {
+// Tables that do not change during a run and are the same for every
+// simulation (kernel/killAgents.cl:84-115,135-147; include/properties.h:262).
+// The count pass needs only the mortality part (KillConst, a prefix).
+struct KillConst {
+  float aquaticHMR;            // eggs and pupae (kernel/killAgents.cl:103-115,135-147)
+  float adultHMR[100];
+};
+struct ModelConst {
+  KillConst kill;
+  float eggBatchScale[kEggBatchTable];  // egg_batch_scale(n)
+};
+
+// Per-step constants of one simulation, shared by every agent of the step.
+// Computed once per step (k_publish) and copied to shared memory by the
+// kernels that step the simulation.
+struct alignas(16) StepCtx {
   // HybridTaus (include/gpuRand.h:33-50): z1 and z3 do not depend on the
   // work-item, so their Tausworthe steps are folded per seed slot.
   uint32_t rng_c13[4], rng_z2[4], rng_z4[4];
@@ -54,7 +68,6 @@ struct StepCtx {
   float T;
   uint32_t wt;                 // world time = step % 24
   uint32_t totalBiomass;       // kernel/killAgents.cl:42-43
-  float aquaticHMR;            // eggs and pupae (kernel/killAgents.cl:103-115,135-147)
   float eggIncubation;         // eggsIncubation(T)
   float larvaDev;              // larvaDevelopment(T)
   float pupaDelay, immatureDelay, bmdDelay;
@@ -62,9 +75,7 @@ struct StepCtx {
   float sporoH, sporoM, sporoL;  // sporoInc = sporoH + sporoM + sporoL exactly
   uint32_t sporoOn;            // T > 16
   uint32_t devOOB;             // T >= 44: the reference reads past devRates
-  float adultHMR[100];
-  float larvaHMR[100];
-  float eggBatchScale[kEggBatchTable];  // egg_batch_scale(n)
+  const float* larvaHMR;       // [100] in global memory; NaN outside the larvae's age range of the step
 };
 
 // Counters an agent update contributes to (BitesNcycles, EggsNbiomass).
@@ -146,18 +157,18 @@ __device__ __forceinline__ uint32_t age_days_uncapped(float age) {
 // Kill then update one valid agent of range rg at slot gid.
 // Returns the next state (0..7), or -1 when the agent dies this step.
 template <bool FULL>
-__device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t gid, Rec& a, Acc& acc) {
+__device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& mc, int rg, uint32_t gid, Rec& a, Acc& acc) {
   // ---- killAgents (kernel/killAgents.cl:52-147) ----
   {
     float prob = rng(c, 0, gid);
     float hmr;
     if (rg >= IMMATURE) {
-      hmr = c.adultHMR[age_days(a.age)];
+      hmr = mc.adultHMR[age_days(a.age)];
     } else if (rg == LARVA) {
-      hmr = c.larvaHMR[age_days(a.age)];
+      hmr = __ldg(c.larvaHMR + age_days(a.age));
       if (hmr != hmr) acc.bad = 1;  // table entry not prepared
     } else {
-      hmr = c.aquaticHMR;
+      hmr = mc.aquaticHMR;
     }
     if (prob <= hmr) return -1;
   }
@@ -277,11 +288,12 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, int rg, uint32_t g
 // The owed draw of an agent at slot gid: larvaDelay (include/properties.h:87-91)
 // returns the new delay bits; generateEggs (:257-266) returns availableEggs,
 // given numEggBatches after its increment.
-__device__ __forceinline__ uint32_t finish_box_muller(const StepCtx& c, uint32_t gid, uint32_t kind, uint32_t batches_after) {
+__device__ __forceinline__ uint32_t finish_box_muller(const StepCtx& c, const ModelConst& mc, uint32_t gid, uint32_t kind,
+                                                      uint32_t batches_after) {
   if (kind == BM_LARVA_DELAY) return __float_as_uint(box_muller(c, gid, 1.0f, 0.1f));
   uint32_t eggs = f2u_sat_fast(box_muller(c, gid, 170.0f, 30.0f) + 0.5f);
   const uint32_t n = batches_after - 1u;
-  const float scale = n < kEggBatchTable ? c.eggBatchScale[n] : egg_batch_scale(n);
+  const float scale = n < kEggBatchTable ? mc.eggBatchScale[n] : egg_batch_scale(n);
   return f2u_sat_fast(u32_to_f32_rn(eggs) * scale + 0.5f);
 }
 

@@ -32,6 +32,9 @@ struct InputBlock {
 struct Scratch {
   uint32_t tiles[kMaxTiles * 17];  // survivor counts [8] | inclusive prefixes [8] | epoch flag, per tile
   SimDev sim;
+  RepParams rep;
+  BatchDev bat;
+  ModelConst mc;
   sampo_stats_row rows[2];
   InputBlock in;
 };
@@ -85,15 +88,14 @@ static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sam
   if (scratch_address(device, &base) != cudaSuccess) return SAMPO_ERR_CUDA;
   Scratch* sc = (Scratch*)base;
 
-  SimDev h;
-  memset(&h, 0, sizeof(h));
-  fill_constant_tables(h);
+  SimDev h = initial_sim_state(out_capacity, cc);
   h.pop = *pop_in;
   h.pop.numLarvae1DayEquiv = h.pop.numFemale = h.pop.numPotentiallyInfective = 0;
-  h.capacity = out_capacity;
-  h.cc = cc;
-  h.acc_dmin = 0xffffffffu;
-  h.epoch = 1;
+  h.active = 1;
+  ModelConst mc;
+  fill_constant_tables(mc);
+  BatchDev bat;
+  memset(&bat, 0, sizeof(bat));
   InputBlock ib;
   memset(&ib, 0, sizeof(ib));
   ib.T[0] = temperature;
@@ -105,28 +107,38 @@ static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sam
   // the epoch flags of the tiles this step uses (a stale flag equal to this
   // step's epoch would be taken for a published prefix).
   const uint32_t ntiles = (pop_in->r[7].end + kTile - 1) / kTile;
-  if (cudaMemcpyAsync(&sc->sim, &h, sizeof(h), cudaMemcpyHostToDevice, st) != cudaSuccess) return SAMPO_ERR_CUDA;
-  if (cudaMemcpyAsync(&sc->in, &ib, sizeof(ib), cudaMemcpyHostToDevice, st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  RepParams rp;
+  rp.sim = &sc->sim;
+  rp.pool[0] = to_dev(in);
+  rp.pool[1] = to_dev(out);
+  rp.tileAgg = sc->tiles;
+  rp.tileIncl = sc->tiles + (size_t)kMaxTiles * 8;
+  rp.tileFlag = sc->tiles + (size_t)kMaxTiles * 16;
+  rp.T = sc->in.T;
+  rp.env = sc->in.env;
+  rp.seeds = sc->in.seeds;
+  rp.wt = sc->in.wt;
+  rp.rows = sc->rows;
+  rp.ring = 2;
+  rp.maxTiles = kMaxTiles;
+  if (cudaMemcpyAsync(&sc->sim, &h, sizeof(h), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(&sc->rep, &rp, sizeof(rp), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(&sc->bat, &bat, sizeof(bat), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(&sc->mc, &mc, sizeof(mc), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(&sc->in, &ib, sizeof(ib), cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return SAMPO_ERR_CUDA;
   if (ntiles && cudaMemsetAsync(sc->tiles + (size_t)kMaxTiles * 16, 0, (size_t)ntiles * 4, st) != cudaSuccess)
     return SAMPO_ERR_CUDA;
 
   KParams p;
-  p.sim = &sc->sim;
-  p.pool[0] = to_dev(in);
-  p.pool[1] = to_dev(out);
-  p.tileAgg = sc->tiles;
-  p.tileIncl = sc->tiles + (size_t)kMaxTiles * 8;
-  p.tileFlag = sc->tiles + (size_t)kMaxTiles * 16;
-  p.T = sc->in.T;
-  p.env = sc->in.env;
-  p.seeds = sc->in.seeds;
-  p.wt = sc->in.wt;
-  p.rows = sc->rows;
-  p.ring = 2;
-  p.maxTiles = kMaxTiles;
+  p.reps = &sc->rep;
+  p.nrep = 1;
+  p.bat = &sc->bat;
+  p.mc = &sc->mc;
   if (launch_publish_start(p, st) != cudaSuccess) return SAMPO_ERR_CUDA;
-  if (launch_count(p, grid_blocks_count(), st) != cudaSuccess) return SAMPO_ERR_CUDA;
-  if (launch_scatter(p, grid_blocks_scatter(), st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (launch_count(p, grid_blocks_count(1), st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (launch_scatter(p, grid_blocks_scatter(1), st) != cudaSuccess) return SAMPO_ERR_CUDA;
+  if (launch_publish(p, PUB_AFTER_STEP, st) != cudaSuccess) return SAMPO_ERR_CUDA;
 
   uint32_t err = 0;
   if (cudaMemcpyAsync(row, &sc->rows[0], sizeof(*row), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
