@@ -10,7 +10,15 @@ capacity 5 x 1e6. agent-days = sum over hourly steps of the live agents at
 the step's start / 24.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload plain-large|roofline|plain-small]
+                  [--workload plain-large|roofline|plain-small|ensemble|served]
+
+--workload ensemble: 512 replicates (sizes log-uniform in [1e3, 1e6] eggs, each
+with its own seed and weather) stepped as one batch for W + K days against
+the same replicates run one at a time through the plain path; every
+replicate's rows are compared bit for bit.
+--workload served: Poisson request streams (--rates) served with continuous
+batching under an HBM budget against one-at-a-time plain service; reports
+p50/p95/p99 latency and sims/s per rate.
 
 --impl reference times the reference's own per-step algorithm on the host
 cores (the CPU restatement in oracle/, pinned to the reference's code by the
@@ -320,17 +328,168 @@ def all_reduce(vals, op):
     return t.tolist()
 
 
+def ensemble_arm(args):
+    """BASELINE config 3 over a window of days: batched vs one at a time."""
+    from sampo_gb300.batch import Batch, ensemble_specs
+    from sampo_gb300.sim import Simulation, seed_stream
+    days = args.warmup + args.steps
+    n = args.replicates
+    # the hottest replicates reach 12x their initial size by day 15 (oracle)
+    specs = ensemble_specs(n, seed=4, days=days, growth=20.0)
+    prep = []
+    for s in specs:
+        T, env = s.inputs()
+        init, seeds = seed_stream(s.seed, s.steps)
+        prep.append((T, env, init, seeds))
+    ring = days * 24 + 1
+    # ---- batched ----
+    t0 = time.perf_counter()
+    b = Batch(n, ring)
+    slots = []
+    for s, (T, env, init, seeds) in zip(specs, prep):
+        slot = b.add(s.capacity, s.cc, stop_step=s.steps)
+        b.set_inputs(slot, T, env)
+        b.set_seeds(slot, 0, seeds)
+        b.init_population(slot, s.initial, init, age_days_max=s.age_days_max, age_seed=s.seed)
+        slots.append(slot)
+    b.sync()
+    setup_batch = time.perf_counter() - t0
+    b.run(24 * args.warmup)
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        b.run(24 * args.steps)
+        wall_batch = time.perf_counter() - t0
+    dev_batch = b.last_run_ms() / 1e3
+    rows_b, bits_b = [], []
+    for slot, s in zip(slots, specs):
+        rows_b.append(b.rows(slot, 0, s.steps + 1))
+        bits_b.append(b.state(slot)[2])
+    b.close()
+    # ---- one at a time through the plain path ----
+    from sampo_gb300._lib import SampoError
+    plain_run_s, plain_total_s, exact, live_sum, overflow = 0.0, 0.0, 0, 0, 0
+    for i, (s, (T, env, init, seeds)) in enumerate(zip(specs, prep)):
+        t0 = time.perf_counter()
+        with Simulation(capacity=s.capacity, carrying_capacity=s.cc, max_steps=s.steps + 1) as sim:
+            sim.set_inputs(T, env)
+            sim.set_seeds(0, seeds)
+            sim.init_population(s.initial, init, age_days_max=s.age_days_max, age_seed=s.seed)
+            try:
+                r0 = sim.run(24 * args.warmup)
+                t1 = time.perf_counter()
+                r1 = sim.run(24 * args.steps)
+                plain_run_s += time.perf_counter() - t1
+                rows = np.concatenate([r0, r1, [sim.current_row()]])
+                live_sum += int(live_counts(r1).sum())
+            except SampoError:  # outgrew its pool: compare the status bits only
+                rows, overflow = None, overflow + 1
+            bits = sim.device_status()
+        plain_total_s += time.perf_counter() - t0
+        exact += int((rows is None or rows.tobytes() == rows_b[i].tobytes()) and bits == bits_b[i])
+    sizes = np.array([s.initial for s in specs])
+    value = n * args.steps / dev_batch
+    return {
+        "metric": "replicate-days/s", "value": value, "unit": "replicate-days/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_batch * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
+        "config": {"workload": f"ensemble: {n} replicates, initial eggs log-uniform in [1e3, 1e6] aged U{{0..3}} days, "
+                               "own seed and weather each (mean T U[20,30] C, amplitude U[2,8] C, sd 0.5), "
+                               f"days {args.warmup}..{days} of a 365-day run; capacity 20 x initial + 65536",
+                   "step": "one simulated day of every replicate (24 hourly steps, one CUDA graph)",
+                   "initial_agents_total": int(sizes.sum()), "agent_days_timed": live_sum / 24.0,
+                   "l2": "pools far larger than L2"},
+        "batched": {"replicate_days_per_s": value, "sims_per_s_365d_equiv": value / 365.0,
+                    "agent_days_per_s": live_sum / 24.0 / dev_batch, "wall_s": wall_batch, "device_s": dev_batch,
+                    "setup_s": setup_batch},
+        "one_at_a_time": {"replicate_days_per_s": n * args.steps / plain_run_s, "run_s": plain_run_s,
+                          "with_setup_s": plain_total_s},
+        "speedup_vs_one_at_a_time": plain_run_s / dev_batch,
+        "speedup_incl_setup": plain_total_s / (dev_batch + setup_batch),
+        "bit_exact_replicates": f"{exact}/{n}",
+        "replicates_out_of_capacity": overflow,
+        "e2e": {"value": n * args.steps / wall_batch, "unit": "replicate-days/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": 1 + 73 * args.steps,
+        "clocks": clk.summary(),
+    }
+
+
+def served_arm(args):
+    """BASELINE config 4, a bounded number of requests per rate."""
+    from sampo_gb300.serve import Server, latency_summary, one_at_a_time, request_stream
+    rates = [float(x) for x in args.rates.split(",")]
+    out = {"metric": "sims/s", "unit": "sims/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic", "steps": args.requests, "warmup": 0}
+    per_rate = {}
+    plain = None
+    for rate in rates:
+        reqs = request_stream(args.requests, rate, seed=7, days_range=(args.min_days, args.max_days))
+        srv = Server(budget_bytes=int(args.budget_gb * 1e9), max_days=args.max_days)
+        t0 = time.perf_counter()
+        res = srv.serve(reqs)
+        makespan = max(r.completed for r in res) - min(r.arrival for r in res)
+        srv.close()
+        if plain is None:  # service times do not depend on the arrival rate
+            plain = {p["rid"]: p for p in one_at_a_time(reqs)}
+        prev, lat_plain = 0.0, []
+        for r in sorted(reqs, key=lambda r: r.arrival):
+            prev = max(r.arrival, prev) + plain[r.rid]["service"]
+            lat_plain.append(prev - r.arrival)
+        plain_makespan = prev - min(r.arrival for r in reqs)
+        def same(x):
+            p = plain[x.rid]
+            if x.status != p["status"]:
+                return False
+            if p["rows"] is None:  # both outgrew their pools at the same step
+                return True
+            return x.rows is not None and x.rows.tobytes() == p["rows"].tobytes()
+        exact = sum(int(same(x)) for x in res)
+        per_rate[str(rate)] = {
+            "sims_per_s": len(res) / makespan, "latency_s": latency_summary([r.latency for r in res]),
+            "one_at_a_time": {"sims_per_s": len(reqs) / plain_makespan, "latency_s": latency_summary(lat_plain)},
+            "speedup_sims_per_s": (len(res) / makespan) / (len(reqs) / plain_makespan),
+            "bit_exact": f"{exact}/{len(res)}", "peak_resident": srv.peak_resident,
+            "peak_hbm_gb": srv.peak_bytes / 1e9, "days_stepped": srv.days_run, "wall_s": time.perf_counter() - t0}
+    first = per_rate[str(rates[0])]
+    out.update({"value": first["sims_per_s"], "ms_per_step": None,
+                "config": {"workload": f"served stream: {args.requests} requests per rate, Poisson arrivals, initial eggs "
+                                       f"log-uniform in [1e2, 5e6], horizons U{{{args.min_days}..{args.max_days}}} days, "
+                                       f"own seed and weather each, {args.budget_gb:g} GB HBM budget, capacity 96 x initial + 65536",
+                           "rates_per_s": rates},
+                "per_rate": per_rate,
+                "e2e": {"value": first["sims_per_s"], "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=727)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain-large", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="plain-large", choices=list(WORKLOADS) + ["ensemble", "served"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--replicates", type=int, default=512, help="ensemble: replicates")
+    ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
+    ap.add_argument("--rates", default="10,100,1000", help="served: arrival rates per second")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM budget")
+    ap.add_argument("--min-days", type=int, default=30)
+    ap.add_argument("--max-days", type=int, default=365)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
+    if args.workload in ("ensemble", "served"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference runs one simulation per process; "
+                              "its arm is the plain workloads"}))
+            return
+        if args.workload == "ensemble":
+            if "--steps" not in sys.argv:
+                args.steps = 12
+            print(json.dumps(ensemble_arm(args)))
+        else:
+            print(json.dumps(served_arm(args)))
+        return
     wl = WORKLOADS[args.workload]
     rank, world, local = dist_env()
     dist_init(world)

@@ -1,0 +1,47 @@
+"""Serving with continuous batching (sampo_gb300.serve): requests that arrive
+while others run are admitted as memory and slots free up, share the batch's
+day steps, and each result - stats rows of every step, age histogram and
+status - is the same as the request run alone through the plain path."""
+import numpy as np
+import pytest
+
+from sampo_gb300.serve import latency_summary, request_stream
+
+
+def test_request_stream_follows_its_distributions():
+    reqs = request_stream(2000, rate=100.0, seed=3, size_range=(1e2, 5e6), days_range=(30, 365))
+    t = np.array([r.arrival for r in reqs])
+    assert np.all(np.diff(t) >= 0)
+    assert 0.8 < 1.0 / np.diff(t).mean() / 100.0 < 1.2          # Poisson rate
+    sizes = np.log(np.array([r.spec.initial for r in reqs], dtype=np.float64))
+    assert sizes.min() >= np.log(1e2) - 0.01 and sizes.max() <= np.log(5e6) + 0.01
+    assert abs(sizes.mean() - 0.5 * (np.log(1e2) + np.log(5e6))) < 0.3   # log-uniform
+    days = np.array([r.spec.days for r in reqs])
+    assert days.min() >= 30 and days.max() <= 365
+    assert len({r.spec.seed for r in reqs}) > 1990
+    s = latency_summary([1.0, 2.0, 3.0, 4.0])
+    assert s["p50"] == 2.5 and s["max"] == 4.0
+
+
+@pytest.mark.gpu
+def test_served_results_equal_solo_runs(gpu_ready):
+    from sampo_gb300.serve import Server, plain_result
+    reqs = request_stream(10, rate=400.0, seed=5, size_range=(100, 5000), days_range=(2, 5), growth=64.0)
+    probe = Server(budget_bytes=1 << 40, max_days=5)
+    biggest = max(probe.bytes_for(r.spec) for r in reqs)
+    probe.close()
+    budget = int(2.2 * biggest)  # room for about two requests: the rest must queue
+    srv = Server(budget_bytes=budget, max_replicates=4, max_days=5)
+    results = srv.serve(reqs)
+    srv.close()
+    assert len(results) == len(reqs)
+    assert srv.peak_bytes <= budget and srv.peak_resident <= 4
+    assert srv.peak_resident >= 2, "requests must overlap on the device"
+    assert any(r.admitted > r.arrival for r in results), "some requests must wait for memory"
+    by_id = {r.rid: r for r in reqs}
+    for res in results:
+        rows, hist, status = plain_result(by_id[res.rid].spec)
+        assert res.rows.tobytes() == rows.tobytes(), f"request {res.rid}: rows differ from its solo run"
+        assert np.array_equal(res.histogram, hist), f"request {res.rid}: histogram differs"
+        assert res.status == status
+        assert res.completed >= res.admitted >= res.arrival
