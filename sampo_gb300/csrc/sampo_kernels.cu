@@ -24,8 +24,11 @@
 // Both kernels stream tiles through shared memory with TMA bulk copies
 // (cp.async.bulk + mbarrier, double-buffered: tile j+1 is in flight while
 // tile j is processed). k_count loads only the columns the tile's ranges
-// need; k_scatter reuses the input stage as the output staging area, sorted
-// by next state, and writes each state's run with coalesced stores.
+// need. In k_scatter a producer warp claims and describes tiles ahead and
+// issues their loads; the eight consumer warps release a stage as soon as
+// they have read it and write every survivor from registers straight to its
+// slot in the next buffer (a next state's survivors are contiguous within a
+// warp, so these stores coalesce).
 //
 // This replaces the reference's 19 kernels per step (killAgents,
 // updateAgents, initAgents, 3 x preScan + 3 x Bolt scan-by-key,
@@ -45,12 +48,7 @@ __device__ const float kDevRates[32] = {
 
 constexpr uint32_t kColBytes = kTile * 4;                    // one 4-byte column of a tile
 constexpr uint32_t kCountStage = 5 * kColBytes + kTile;      // age, his, delay, uni, avail, flags
-// Output staging: each next-state run starts at a staging element with the
-// same residue modulo 16 as its destination slot, so that shared and global
-// addresses of a run agree modulo 16 bytes for every column (the condition
-// for bulk stores); 8 runs add at most 8 x 30 elements of padding.
-constexpr uint32_t kStg = kTile + 256;                       // staging elements per column
-constexpr uint32_t kScatterStage = 9 * kStg * 4 + kStg;      // >= the input layout (9 x kColBytes + kTile)
+constexpr uint32_t kScatterStage = 9 * kColBytes + kTile;    // the nine 4-byte columns and the flags
 constexpr uint32_t kWaitLimit = 1u << 22;                    // bounded mbarrier waits
 
 // ---------------- memory-model and TMA helpers ----------------
@@ -102,17 +100,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
-// 1-D bulk copy shared -> global in the issuing thread's bulk group (both
-// addresses 16-byte aligned, bytes a multiple of 16).
-__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// the shared-memory sources of this thread's bulk stores may be overwritten
-__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-// this thread's bulk stores are complete
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // Range of slot g in the current layout, -1 for gaps and the tail
 // (the validity test of every reference kernel, e.g. kernel/killAgents.cl:28-35).
@@ -625,8 +612,14 @@ __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epo
   }
 }
 
-// Named barrier of the eight consumer warps (the producer warp is not in it).
-__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+// Named barrier of the eight consumer warps (the producer warp is not in it),
+// returning whether any consumer passed v = true.
+__device__ __forceinline__ bool consumer_sync_or(bool v) {
+  uint32_t r;
+  asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, 256, q;\n\tselp.u32 %0, 1, 0, p;\n}"
+               : "=r"(r) : "r"((uint32_t)v) : "memory");
+  return r != 0;
+}
 __device__ __forceinline__ void mbar_init_count(uint64_t* bar, uint32_t n) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(n) : "memory");
 }
@@ -635,11 +628,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one producer warp
-static_assert(kBlock == 256, "consumer_sync() names 256 threads");
+static_assert(kBlock == 256, "consumer_sync_or() names 256 threads");
+static_assert(kItems * kWarps == 32, "one (round, warp) count entry per lane");
 enum : uint32_t { TK_OLD = 0, TK_EGG = 1, TK_END = 2 };
 
-// What the producer warp hands the consumers with a stage. The replicate's
-// part (c .. base) is reloaded only when the stage changes replicate.
+// What the producer warp hands the consumers with a tile. The replicate's
+// part (c .. base) is reloaded only when the slot changes replicate.
 struct alignas(16) ScatterStage {
   StepCtx c;                 // the replicate's step constants
   sampo_population pop;      // its current ranges
@@ -648,24 +642,31 @@ struct alignas(16) ScatterStage {
   uint32_t rep, end, newEggs, nold, epoch;  // replicate, pool end, eggs laid, old tiles, look-back epoch
   uint32_t base[8];          // first slot of each next-state range
   uint32_t kind, lo;         // TK_*, first slot (old tile) or first egg id (egg tile)
-  uint32_t d0[8], sb[8], cnt[8];  // per next state: first slot, staging start, survivors
+  uint32_t d0[8], cnt[8];    // per next state: the tile's first slot in it, survivors
 };
+constexpr int kDescSlots = 4;  // tile descriptions: the producer describes three tiles ahead
 
-// The producer warp keeps two tiles in flight ahead of the consumers: it
-// takes tickets, issues the TMA loads, runs the look-back and lays out the
-// staging runs (full[s]: its expect-tx arrival + one arrival once the stage
-// description is written); after the consumers have staged a tile (empty[s]:
-// 256 arrivals) it sends the runs with bulk stores and refills the stage.
+// A survivor's owed normal draw (include/gpuRand.h:56-63): its slot in the
+// next buffer, its slot in the current one (the generator's gid), its
+// numEggBatches after the step, BM_*.
+struct BmEntry { uint32_t d, gid, batches, kind; };
+
+// The producer warp describes tiles three ahead (ticket, replicate data,
+// look-back, layout) and hands each to the consumers in a free stage with
+// its TMA loads (full[s]: the expect-tx arrival + the arrival that publishes
+// the description). Consumers release a stage (empty[s], 256 arrivals) as
+// soon as they have read its inputs, then write every survivor straight to
+// its slot in the next buffer: the survivors of one next state are
+// contiguous within a warp, so the stores coalesce.
 __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
-  __shared__ ScatterStage s_si[2];
+  __shared__ ScatterStage s_si[kDescSlots];
   __shared__ ModelConst s_mc;
   __shared__ uint32_t s_w[33];
   uint32_t* s_pre = reinterpret_cast<uint32_t*>(dsm + kScatterSmem);
   __shared__ __align__(8) uint64_t full[2], empty[2];
-  __shared__ uint32_t s_fullok[2];
-  __shared__ uint32_t s_off[kItems][kWarps][8];
-  __shared__ uint32_t s_bmq[kTile], s_bmn;  // owed Box-Muller draws: staging slot | item << 11 | kind << 21
+  __shared__ uint4 s_cnt4[2][kItems * kWarps];      // per stage and (round, warp): survivors by state, 16-bit packed
+  __shared__ BmEntry s_bmq[kWarps][kItems * 32];    // per warp: owed draws of the tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   load_model_const(p.mc, s_mc);
   plan_tickets(p.nrep, s_pre, s_w, [&](uint32_t r) -> uint32_t {
@@ -687,30 +688,29 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     mbar_init_count(&empty[0], kBlock);
     mbar_init_count(&empty[1], kBlock);
     fence_mbar_init();
-    s_si[0].rep = s_si[1].rep = 0xffffffffu;
+    for (int k = 0; k < kDescSlots; k++) s_si[k].rep = 0xffffffffu;
   }
   __syncthreads();
 
   uint32_t fail = 0, fail_rep = 0;
   if (warp == kWarps) {
     // ================= producer warp =================
-    // fill stage s with the next ticket's tile; returns its kind
-    auto fill = [&](uint32_t s) -> uint32_t {
+    // describe tile `seq` (slot seq % kDescSlots): take a ticket, load the
+    // replicate's data when the slot changes replicate, run the look-back,
+    // lay out the tile's runs. Touches no stage.
+    auto describe = [&](uint32_t seq) -> uint32_t {
       uint32_t t = 0;
       if (lane == 0) t = atomicAdd(&p.bat->ticket2, 1u);
       t = __shfl_sync(0xffffffffu, t, 0);
-      ScatterStage& si = s_si[s];
+      ScatterStage& si = s_si[seq % kDescSlots];
       if (t >= total) {
-        if (lane == 0) {
-          si.kind = TK_END;
-          mbar_arrive(&full[s]);
-          mbar_arrive(&full[s]);
-        }
+        if (lane == 0) si.kind = TK_END;
+        __syncwarp();
         return TK_END;
       }
       const uint32_t r = find_rep(s_pre, p.nrep, t);
       const uint32_t j = t - s_pre[r];
-      if (si.rep != r) {  // uniform: the stage's replicate data, once per replicate
+      if (si.rep != r) {  // uniform: the slot's replicate data, once per replicate
         const RepParams& rp = p.reps[r];
         SimDev* sim = rp.sim;
         copy16(&si.c, &sim->ctx, (int)sizeof(StepCtx), lane, 32);
@@ -736,94 +736,70 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         if (lane == 0) si.rep = r;
         __syncwarp();
       }
-      const uint32_t end = si.end, nold = si.nold;
-      if (j < nold) {
-        if (lane == 0) {
-          fence_proxy_async();  // the stage was last written through the generic proxy
-          issue_scatter_tile(si.src, dsm + s * kScatterStage, &full[s], j * kTile, min((uint32_t)kTile, end - j * kTile));
-        }
+      if (j < si.nold) {
         uint32_t ex[8], cnt[8];
         tile_lookback(si.lb, j, si.epoch, lane, ex, cnt);
         if (lane == 0) {
-          uint32_t pos = 0;
 #pragma unroll
           for (int b = 0; b < 8; b++) {
-            const uint32_t d0 = si.base[b] + ex[b];
-            const uint32_t sb = ((pos + 15u) & ~15u) + (d0 & 15u);
-            si.d0[b] = d0;
-            si.sb[b] = sb;
+            si.d0[b] = si.base[b] + ex[b];
             si.cnt[b] = cnt[b];
-            pos = sb + cnt[b];
           }
           si.kind = TK_OLD;
           si.lo = j * kTile;
         }
         __syncwarp();
-        if (lane == 0) mbar_arrive(&full[s]);  // stage described (release)
         return TK_OLD;
       }
       if (lane == 0) {
         si.kind = TK_EGG;
-        si.lo = (j - nold) * kTile;
+        si.lo = (j - si.nold) * kTile;
       }
       __syncwarp();
-      if (lane == 0) {
-        mbar_arrive(&full[s]);
-        mbar_arrive(&full[s]);
-      }
       return TK_EGG;
     };
-    uint32_t kind0 = fill(0), kind1 = fill(1), ph = 0;
-    for (uint32_t it = 0;; it++) {
-      const uint32_t s = it & 1u;
-      const uint32_t k = s ? kind1 : kind0;
-      if (k == TK_END) break;
-      uint32_t ok = 1;
-      if (lane == 0) ok = mbar_wait(&empty[s], (ph >> s) & 1u) ? 1u : 0u;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) { fail = 1; fail_rep = s_si[s].rep; break; }
-      ph ^= 1u << s;
-      if (k == TK_OLD && lane == 0) {
-        // ---- each state's run to its slots in the next buffer ----
-        // staging and destination agree modulo 16 bytes: the aligned body of
-        // every run and column leaves with one bulk store; the consumers
-        // wrote the unaligned heads and tails. Runs lie inside the next
-        // layout by construction (d0 + count <= range end).
-        const ScatterStage& si = s_si[s];
-        const DevPool& dst = si.dst;
-        uint8_t* st = dsm + s * kScatterStage;
-        fence_proxy_async();  // staging written through the generic proxy
-#pragma unroll 1
-        for (int b = 0; b < 8; b++) {
-          const uint32_t n = si.cnt[b], d0 = si.d0[b], sb = si.sb[b];
-          if (!n) continue;
-          const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
-          if (n4) {
-            const uint32_t o = h4, by = n4 * 4, so = (sb + o) * 4;
-            bulk_store(dst.age + d0 + o, st + 0 * kStg * 4 + so, by);
-            bulk_store(dst.his + d0 + o, st + 1 * kStg * 4 + so, by);
-            bulk_store(dst.delay + d0 + o, st + 2 * kStg * 4 + so, by);
-            bulk_store(dst.sporo + d0 + o, st + 3 * kStg * 4 + so, by);
-            bulk_store(dst.uni + d0 + o, st + 4 * kStg * 4 + so, by);
-            bulk_store(dst.avail + d0 + o, st + 5 * kStg * 4 + so, by);
-            bulk_store(dst.cycle + d0 + o, st + 6 * kStg * 4 + so, by);
-            bulk_store(dst.hbc + d0 + o, st + 7 * kStg * 4 + so, by);
-            bulk_store(dst.batches + d0 + o, st + 8 * kStg * 4 + so, by);
-          }
-          const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
-          if (n1) bulk_store(dst.flags + d0 + h1, st + 9 * kStg * 4 + sb + h1, n1);
+    // hand tile `seq` to the consumers in stage seq & 1 (free): its loads
+    // (expect-tx arrival) and the arrival that publishes its description
+    auto issue = [&](uint32_t seq) {
+      const uint32_t s = seq & 1u;
+      const ScatterStage& si = s_si[seq % kDescSlots];
+      if (lane == 0) {
+        if (si.kind == TK_OLD) {
+          fence_proxy_async();  // the stage was last read through the generic proxy
+          issue_scatter_tile(si.src, dsm + s * kScatterStage, &full[s], si.lo, min((uint32_t)kTile, si.end - si.lo));
+        } else {
+          mbar_arrive(&full[s]);
         }
-        bulk_commit();
+        mbar_arrive(&full[s]);  // description written (release)
       }
-      if (lane == 0) bulk_wait_read();  // the stage's sources are read: it may be refilled
-      __syncwarp();
-      const uint32_t nk = fill(s);
-      if (s) kind1 = nk;
-      else kind0 = nk;
+    };
+    uint32_t kinds = 0, ph = 0;  // 2 bits per described tile, slot seq % kDescSlots
+    auto kind_of = [&](uint32_t seq) { return (kinds >> (2 * (seq % kDescSlots))) & 3u; };
+    auto set_kind = [&](uint32_t seq, uint32_t k) {
+      const uint32_t sh = 2 * (seq % kDescSlots);
+      kinds = (kinds & ~(3u << sh)) | (k << sh);
+    };
+    set_kind(0, describe(0));
+    issue(0);
+    set_kind(1, describe(1));
+    issue(1);
+    set_kind(2, describe(2));
+    for (uint32_t seq = 0;; seq++) {
+      const uint32_t s = seq & 1u;
+      if (kind_of(seq) == TK_END) break;
+      uint32_t ok = 1;
+      if (lane == 0) ok = mbar_wait(&empty[s], (ph >> s) & 1u) ? 1u : 0u;  // tile seq's inputs are read
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) { fail = 1; fail_rep = s_si[seq % kDescSlots].rep; break; }
+      ph ^= 1u << s;
+      issue(seq + 2);
+      // slot (seq + 3) % 4 held tile seq - 1, whose consumers are done: they
+      // released tile seq's inputs after finishing it
+      set_kind(seq + 3, describe(seq + 3));
     }
-    if (lane == 0) bulk_wait_all();  // this CTA's bulk stores are complete
   } else {
     // ================= consumer warps =================
+    // One named barrier per tile (after the survivor counts).
     const ModelConst& mc = s_mc;
     Acc acc = {0, 0, 0, 0, 0, 0};
     uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0;
@@ -854,27 +830,21 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     uint32_t ph = 0;
     for (uint32_t it = 0;; it++) {
       const uint32_t s = it & 1u;
-      uint8_t* st = dsm + s * kScatterStage;
-      for (int q = tid; q < kItems * kWarps * 8; q += kBlock) (&s_off[0][0][0])[q] = 0u;
-      if (tid == 0) {
-        s_bmn = 0;
-        s_fullok[s] = mbar_wait(&full[s], (ph >> s) & 1u) ? 1u : 0u;
-      }
-      consumer_sync();
-      if (!s_fullok[s]) { fail = 1; fail_rep = cur_rep == 0xffffffffu ? 0u : cur_rep; break; }
-      (void)mbar_try_wait(&full[s], (ph >> s) & 1u);  // the completed phase, observed by this thread
+      const uint8_t* st = dsm + s * kScatterStage;
+      const bool ok = mbar_wait(&full[s], (ph >> s) & 1u);  // bounded; acquires the stage
       ph ^= 1u << s;
-      const ScatterStage& si = s_si[s];
-      const uint32_t kind = si.kind;
-      if (kind == TK_END) break;
-      if (si.rep != cur_rep) {
+      const ScatterStage& si = s_si[it % kDescSlots];
+      const uint32_t kind = ok ? si.kind : TK_END;
+      if (kind != TK_END && si.rep != cur_rep) {
         if (cur_rep != 0xffffffffu) flush(cur_rep);
         cur_rep = si.rep;
       }
-      const StepCtx& c = si.c;
-      const DevPool& dst = si.dst;
+      // ---- phase A (old tiles): recompute the step for the tile's agents and
+      //      count the survivors of each (round, warp) by next state ----
+      Rec a[kItems];
+      int nb[kItems];
+      uint32_t rk[kItems];
       if (kind == TK_OLD) {
-        // ---- recompute the step for the tile's agents (inputs from shared memory) ----
         const float* c_age = (const float*)(st + 0 * kColBytes);
         const float* c_his = (const float*)(st + 1 * kColBytes);
         const float* c_delay = (const float*)(st + 2 * kColBytes);
@@ -885,10 +855,8 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
         const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
         const uint8_t* c_flags = st + 9 * kColBytes;
+        const StepCtx& c = si.c;
         const uint32_t lo = si.lo, end = si.end;
-        Rec a[kItems];
-        int nb[kItems];
-        uint32_t rk[kItems];
 #pragma unroll
         for (int k = 0; k < kItems; k++) {
           const uint32_t i = k * kBlock + tid;
@@ -906,57 +874,76 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           }
           const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
           rk[k] = __popc(peers & lanemask_lt());
-          if (nb[k] < 8 && lane == __ffs(peers) - 1) s_off[k][warp][nb[k]] = __popc(peers);
+          // survivors of this (round, warp) by state, 16 bits each: word j holds states 2j, 2j+1
+          const uint32_t one = nb[k] < 8 ? 1u << (16 * (nb[k] & 1)) : 0u;
+          const uint32_t wsel = (uint32_t)nb[k] >> 1;
+          const uint32_t c0 = __reduce_add_sync(0xffffffffu, wsel == 0 ? one : 0u);
+          const uint32_t c1 = __reduce_add_sync(0xffffffffu, wsel == 1 ? one : 0u);
+          const uint32_t c2 = __reduce_add_sync(0xffffffffu, wsel == 2 ? one : 0u);
+          const uint32_t c3 = __reduce_add_sync(0xffffffffu, wsel == 3 ? one : 0u);
+          if (lane == 0) s_cnt4[s][k * kWarps + warp] = make_uint4(c0, c1, c2, c3);
         }
-        consumer_sync();  // inputs consumed (the stage becomes the output staging area), counts written
-        // ---- exclusive scan of the (round, warp) counts, one warp per state ----
-        {
-          const int b = warp;
-          const uint32_t v = (&s_off[0][0][0])[lane * 8 + b];  // entry (round, warp) = lane, kItems*kWarps == 32
-          uint32_t incl = v;
+      }
+      if (kind != TK_END) mbar_arrive(&empty[s]);  // this thread is done with the stage's inputs
+      // every (round, warp) count is in place; the barrier also agrees on a
+      // failed wait (then every consumer stops)
+      if (consumer_sync_or(!ok)) { fail = 1; fail_rep = cur_rep == 0xffffffffu ? 0u : cur_rep; break; }
+      if (kind == TK_END) break;
+      const StepCtx& c = si.c;
+      const DevPool& dst = si.dst;
+      if (kind == TK_OLD) {
+        // ---- phase B: exclusive prefix of the 32 (round, warp) entries, by
+        //      every warp for its own entries (4 x 16-bit-packed scans) ----
+        const uint4 e = s_cnt4[s][lane];
+        uint32_t i0 = e.x, i1 = e.y, i2 = e.z, i3 = e.w;
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-          }
-          (&s_off[0][0][0])[lane * 8 + b] = incl - v;
-          if (lane == 31 && incl != si.cnt[b]) tilebad = 1;
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y0 = __shfl_up_sync(0xffffffffu, i0, o), y1 = __shfl_up_sync(0xffffffffu, i1, o);
+          const uint32_t y2 = __shfl_up_sync(0xffffffffu, i2, o), y3 = __shfl_up_sync(0xffffffffu, i3, o);
+          if (lane >= o) { i0 += y0; i1 += y1; i2 += y2; i3 += y3; }
         }
-        consumer_sync();
-        float* g_age = (float*)(st + 0 * kStg * 4);
-        float* g_his = (float*)(st + 1 * kStg * 4);
-        float* g_delay = (float*)(st + 2 * kStg * 4);
-        float* g_sporo = (float*)(st + 3 * kStg * 4);
-        uint32_t* g_uni = (uint32_t*)(st + 4 * kStg * 4);
-        uint32_t* g_avail = (uint32_t*)(st + 5 * kStg * 4);
-        uint32_t* g_cycle = (uint32_t*)(st + 6 * kStg * 4);
-        uint32_t* g_hbc = (uint32_t*)(st + 7 * kStg * 4);
-        uint32_t* g_batches = (uint32_t*)(st + 8 * kStg * 4);
-        uint8_t* g_flags = st + 9 * kStg * 4;
-        // ---- survivors into the staging area, sorted by next state ----
+        {  // tile totals against the count pass
+          const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t1 = __shfl_sync(0xffffffffu, i1, 31);
+          const uint32_t t2 = __shfl_sync(0xffffffffu, i2, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
+          if (lane == 0 && warp == 0) {
+            const uint32_t tw[4] = {t0, t1, t2, t3};
+#pragma unroll
+            for (int b = 0; b < 8; b++)
+              if (((tw[b >> 1] >> (16 * (b & 1))) & 0xffffu) != si.cnt[b]) tilebad = 1;
+          }
+        }
+        const uint32_t x0 = i0 - e.x, x1 = i1 - e.y, x2 = i2 - e.z, x3 = i3 - e.w;
+        BmEntry* bmq = s_bmq[warp];
+        uint32_t nq = 0;
+        // ---- every survivor to its slot in the next buffer ----
 #pragma unroll
         for (int k = 0; k < kItems; k++) {
+          const int ent = k * kWarps + warp;
+          const uint32_t p0 = __shfl_sync(0xffffffffu, x0, ent), p1 = __shfl_sync(0xffffffffu, x1, ent);
+          const uint32_t p2 = __shfl_sync(0xffffffffu, x2, ent), p3 = __shfl_sync(0xffffffffu, x3, ent);
           const int b = nb[k];
-          uint32_t q = 0xffffffffu;
+          uint32_t d = 0xffffffffu;
           if (b < 8) {
-            const uint32_t j = s_off[k][warp][b] + rk[k];
-            if (j < si.cnt[b]) q = si.sb[b] + j;
+            const uint32_t pw = (b >> 1) == 0 ? p0 : (b >> 1) == 1 ? p1 : (b >> 1) == 2 ? p2 : p3;
+            const uint32_t j = ((pw >> (16 * (b & 1))) & 0xffffu) + rk[k];
+            if (j < si.cnt[b]) d = si.d0[b] + j;
             else tilebad = 1;  // the two passes disagree: stay inside this state's run
           }
-          // queue the owed Box-Muller draws (warp-aggregated slot reservation)
-          const bool owe = q != 0xffffffffu && a[k].bm != BM_NONE;
-          const uint32_t om = __ballot_sync(0xffffffffu, owe);
-          if (om) {
-            uint32_t qb = 0;
-            if (lane == __ffs(om) - 1) qb = atomicAdd(&s_bmn, (uint32_t)__popc(om));
-            qb = __shfl_sync(0xffffffffu, qb, __ffs(om) - 1);
-            if (owe) s_bmq[qb + __popc(om & lanemask_lt())] = q | ((uint32_t)(k * kBlock + tid) << 11) | (a[k].bm << 21);
+          // queue this warp's owed draws; their column is written after the draw
+          const uint32_t owed = d != 0xffffffffu ? a[k].bm : BM_NONE;
+          const uint32_t om = __ballot_sync(0xffffffffu, owed != BM_NONE);
+          if (owed != BM_NONE) {
+            BmEntry q;
+            q.d = d; q.gid = si.lo + k * kBlock + tid; q.batches = a[k].batches; q.kind = owed;
+            bmq[nq + __popc(om & lanemask_lt())] = q;
           }
-          if (q != 0xffffffffu) {
-            g_age[q] = a[k].age; g_his[q] = a[k].his; g_delay[q] = a[k].delay; g_sporo[q] = a[k].sporo;
-            g_uni[q] = a[k].uni; g_avail[q] = a[k].avail; g_cycle[q] = a[k].cycle; g_hbc[q] = a[k].hbc;
-            g_batches[q] = a[k].batches;
-            g_flags[q] = (uint8_t)(b | (a[k].female << 3));
+          nq += __popc(om);
+          if (d != 0xffffffffu) {
+            dst.age[d] = a[k].age; dst.his[d] = a[k].his; dst.sporo[d] = a[k].sporo; dst.uni[d] = a[k].uni;
+            dst.cycle[d] = a[k].cycle; dst.hbc[d] = a[k].hbc; dst.batches[d] = a[k].batches;
+            dst.flags[d] = (uint8_t)(b | (a[k].female << 3));
+            if (owed != BM_LARVA_DELAY) dst.delay[d] = a[k].delay;
+            if (owed != BM_EGG_BATCH) dst.avail[d] = a[k].avail;
             // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
             if (b == LARVA) {
               l1 += age_days_uncapped(a[k].age);
@@ -968,36 +955,16 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
             }
           }
         }
-        consumer_sync();
-        // ---- the owed Box-Muller draws, in dense warps, patched into the staging area ----
-        const uint32_t nbm = s_bmn;
-        if (nbm) {
-          for (uint32_t j = tid; j < nbm; j += kBlock) {
-            const uint32_t e = s_bmq[j];
-            const uint32_t q = e & 2047u, kind_bm = e >> 21;
-            const uint32_t v = finish_box_muller(c, mc, lo + ((e >> 11) & 1023u), kind_bm, g_batches[q]);
-            if (kind_bm == BM_LARVA_DELAY) g_delay[q] = __uint_as_float(v);
-            else g_avail[q] = v;
+        // ---- the warp's owed draws, dense over its lanes ----
+        if (nq) {
+          __syncwarp();
+          for (uint32_t jq = lane; jq < nq; jq += 32) {
+            const BmEntry q = bmq[jq];
+            const uint32_t v = finish_box_muller(c, mc, q.gid, q.kind, q.batches);
+            if (q.kind == BM_LARVA_DELAY) dst.delay[q.d] = __uint_as_float(v);
+            else dst.avail[q.d] = v;
           }
-          consumer_sync();
-        }
-        // ---- heads and tails of the runs: per state at most 15 + 15 flag
-        //      elements, of which the four-byte columns need at most 3 + 3 ----
-        {
-          const int b = warp, e = lane;
-          const uint32_t n = si.cnt[b], d0 = si.d0[b], sb = si.sb[b];
-          const uint32_t h4 = min((4u - (d0 & 3u)) & 3u, n), n4 = (n - h4) & ~3u;
-          const uint32_t h1 = min((16u - (d0 & 15u)) & 15u, n), n1 = (n - h1) & ~15u;
-          const uint32_t j = (uint32_t)e < h1 ? (uint32_t)e : h1 + n1 + ((uint32_t)e - h1);
-          if (e < 30 && j < n) {
-            const uint32_t q = sb + j, d = d0 + j;
-            dst.flags[d] = g_flags[q];
-            if (j < h4 || j >= h4 + n4) {
-              dst.age[d] = g_age[q]; dst.his[d] = g_his[q]; dst.delay[d] = g_delay[q]; dst.sporo[d] = g_sporo[q];
-              dst.uni[d] = g_uni[q]; dst.avail[d] = g_avail[q]; dst.cycle[d] = g_cycle[q]; dst.hbc[d] = g_hbc[q];
-              dst.batches[d] = g_batches[q];
-            }
-          }
+          __syncwarp();  // the queue is rewritten by the next tile
         }
       } else {
         // ---- new eggs at [0, newEggs) of the next buffer ----
@@ -1015,7 +982,6 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           }
         }
       }
-      mbar_arrive(&empty[s]);  // staged (release): the producer may send and refill the stage
     }
     if (cur_rep != 0xffffffffu) flush(cur_rep);
     if (fail && tid == 0) {
