@@ -1,0 +1,226 @@
+/*
+ * sampo_main.c - the sampo command: SAMPO's driver (src/abms.c: main,
+ * readArguments, run) with the OpenCL device code replaced by the GB300
+ * library libsampo_cuda.so through its C ABI (include/sampo.h).
+ *
+ *   sampo [options] [temperatureFile [environmentFile [speciesHeader]]]
+ *
+ * Same positional arguments, defaults, input parsing and output as the
+ * reference: the three header lines, one stats line per hourly step
+ * (printStats, src/abms.c:67-81), the final ranges (printPopulation, :83-92),
+ * histogram.txt (storeHistogram, :160-183) and the execution time. The seeds
+ * come from the C library's rand() after srand(seed) in the reference's call
+ * order (src/abms.c:145-150, 611, 671, 511): 16 draws before the initial
+ * population, then 16 per step.
+ *
+ * Options (extensions; the reference hard-codes these):
+ *   --seed S        srand seed (default: time(NULL), as the reference)
+ *   --initial N     initial eggs (default 32000 = initialAgentCount)
+ *   --cc X          carrying capacity (default 160000 = carryingCapacity)
+ *   --steps K       hourly steps (default 8760 = maxSteps)
+ *   --capacity C    slots per pool buffer (default 6000000 = maxAgents)
+ *   --age-days D    initial egg ages 24*U{0..D} hours (seeded by --age-seed)
+ *   --age-seed A
+ *   --per-step      one library call per step (the reference's host loop);
+ *                   default: day graphs in chunks, rows printed per chunk
+ *   --device D      CUDA device
+ * Only the built-in species (properties.h) is compiled in; another species
+ * header is refused.
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "sampo.h"
+
+static double now_ms(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+static void print_range(const sampo_range* r) {
+  printf("[%d\t%d]\t%d\r\n", (int)r->start, (int)r->end, (int)(r->end - r->start));
+}
+
+static void print_population(const sampo_population* p) {
+  static const char* names[8] = {"Eggs \t\t", "Larvae \t\t", "Pupae \t\t", "Immatures \t",
+                                 "MateSeeking \t", "BMS \t\t", "BMD \t\t", "Gravids \t"};
+  for (int k = 0; k < 8; k++) {
+    printf("%s", names[k]);
+    print_range(&p->r[k]);
+  }
+}
+
+static uint32_t num(const sampo_population* p, int k) { return p->r[k].end - p->r[k].start; }
+
+/* calcStats (src/abms.c:230-310) from the row of a step's start and printStats
+ * (:67-81). The adult-range test uses the population of the previous step
+ * (*prev), as the reference's host copy does. Returns the live agent count. */
+static uint32_t print_stats(const sampo_stats_row* row, const sampo_population* prev, uint32_t step, float T) {
+  const sampo_population* p = &row->pop;
+  uint32_t ub = prev->r[SAMPO_IMMATURE].end;
+  if (prev->r[SAMPO_BMS].end > ub) ub = prev->r[SAMPO_BMS].end;
+  if (prev->r[SAMPO_BMD].end > ub) ub = prev->r[SAMPO_BMD].end;
+  if (prev->r[SAMPO_GRAVID].end > ub) ub = prev->r[SAMPO_GRAVID].end;
+  const uint32_t adults_range = ub - prev->r[SAMPO_IMMATURE].start;
+  const uint32_t eggs = num(p, 0), larvae = num(p, 1), pupae = num(p, 2), imm = num(p, 3), mat = num(p, 4);
+  const uint32_t bms = num(p, 5), bmd = num(p, 6), ovi = num(p, 7);
+  const uint32_t l1 = larvae > 0 ? p->numLarvae1DayEquiv : 0;
+  const uint32_t fem = adults_range > 0 ? p->numFemale : 0;
+  const uint32_t inf = adults_range > 0 ? p->numPotentiallyInfective : 0;
+  const uint32_t mature = imm + mat + bms + bmd + ovi;
+  const float hours = 1.0f * (float)step;
+  printf("%0.1f, %0.1f", hours, T);
+  printf(", %d, %d, %d, %d, %d, %d, %d, %d, %d", (int)mature, (int)imm, (int)mat, (int)bms, (int)bmd, (int)ovi, (int)fem,
+         (int)inf, (int)(mature - fem));
+  printf(", %d, %d, %d, %d, %d, ", (int)eggs, (int)larvae, (int)pupae, (int)l1, (int)(l1 + eggs + pupae));
+  const sampo_bites_cycles* b = &row->bnc;
+  printf("%d, %d, %d\r\n", b->numCyclesReported > 0 ? (int)(b->sumCyclesReported / b->numCyclesReported) : 0,
+         (int)b->numBitesReported, (int)b->numInfectBitesReported);
+  return eggs + larvae + pupae + imm + mat + bms + bmd + ovi;
+}
+
+/* The reference's two asserts of calcStats (src/abms.c:306-307). */
+static void check_agents(uint32_t n, uint64_t capacity) {
+  if (!(n <= capacity * 0.95)) {
+    fflush(stdout);
+    fprintf(stderr, "sampo: Assertion `nAgents <= maxAgents * 0.95 && \"not enough capacity\"' failed.\n");
+    abort();
+  }
+  if (!(n > 0)) {
+    fflush(stdout);
+    fprintf(stderr, "sampo: Assertion `nAgents > 0 && \"No more agents left\"' failed.\n");
+    abort();
+  }
+}
+
+static void draw_seeds(sampo_seeds* s) { /* generateSeeds (src/abms.c:145-150) */
+  for (int i = 0; i < 4; i++) {
+    s[i].z1 = (uint32_t)rand();
+    s[i].z2 = (uint32_t)rand();
+    s[i].z3 = (uint32_t)rand();
+    s[i].z4 = (uint32_t)rand();
+  }
+}
+
+static void fail(sampo_sim* s, const char* what, int rc) {
+  fflush(stdout);
+  fprintf(stderr, "sampo: %s failed (%d): %s\n", what, rc, s ? sampo_last_error(s) : "");
+  exit(1);
+}
+
+int main(int argc, char** argv) {
+  unsigned seed = (unsigned)time(NULL);
+  uint32_t initial = 32000, steps = 8760;
+  uint64_t capacity = 6000000ull, age_seed = 0;
+  float cc = 160000.0f;
+  int age_days = -1, per_step = 0, device = 0;
+  const char* pos[3] = {"temp.txt", "environment.txt", "properties.h"};
+  int np = 0;
+  for (int i = 1; i < argc; i++) {
+    if (!strcmp(argv[i], "-h")) {
+      printf("Usage: bin\\abms temperatueFileName environmentFileName speciesHeaderFileName\n");
+      return 0;
+    } else if (!strcmp(argv[i], "--seed") && i + 1 < argc) seed = (unsigned)strtoul(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--initial") && i + 1 < argc) initial = (uint32_t)strtoul(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--cc") && i + 1 < argc) cc = strtof(argv[++i], 0);
+    else if (!strcmp(argv[i], "--steps") && i + 1 < argc) steps = (uint32_t)strtoul(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--capacity") && i + 1 < argc) capacity = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--age-days") && i + 1 < argc) age_days = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--age-seed") && i + 1 < argc) age_seed = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--per-step")) per_step = 1;
+    else if (!strcmp(argv[i], "--device") && i + 1 < argc) device = atoi(argv[++i]);
+    else if (np < 3 && argv[i][0] != '-') pos[np++] = argv[i];
+    else {
+      fprintf(stderr, "sampo: unexpected argument %s\n", argv[i]);
+      return 2;
+    }
+  }
+  printf("Temperature:\t%s\nEnvironment:\t%s\nSpecies:\t%s\n", pos[0], pos[1], pos[2]);
+  const char* base = strrchr(pos[2], '/');
+  base = base ? base + 1 : pos[2];
+  if (strcmp(base, "properties.h") != 0) {
+    fprintf(stderr, "sampo: only the built-in species (properties.h) is compiled into this build\n");
+    return 2;
+  }
+  if (steps == 0) return 0;
+  srand(seed);
+
+  float* T = (float*)malloc(sizeof(float) * steps);
+  sampo_environment* env = (sampo_environment*)malloc(sizeof(sampo_environment) * steps);
+  if (!T || !env) return 1;
+  /* readSingleValFile / readEnvironment (src/abms.c:94-137) */
+  if (sampo_read_temperature_file(pos[0], T, steps) != SAMPO_OK) {
+    printf("Cannot open %s. Check temperature file path\n", pos[0]);
+    return -1;
+  }
+  if (sampo_read_environment_file(pos[1], env, steps, cc) != SAMPO_OK) {
+    printf("Cannot open %s. Check environment file path\n", pos[1]);
+    return -1;
+  }
+
+  const double t0 = now_ms();
+  sampo_config cfg = {capacity, cc, device, steps + 1};
+  sampo_sim* s = NULL;
+  if (sampo_create(&cfg, &s) != SAMPO_OK) {
+    printf("Cannot find any CUDA device\n");
+    return 0;
+  }
+  int rc;
+  if ((rc = sampo_set_inputs(s, 0, T, env, steps)) != SAMPO_OK) fail(s, "inputs", rc);
+  sampo_seeds init[4];
+  draw_seeds(init);
+  sampo_seeds* seeds = (sampo_seeds*)malloc(sizeof(sampo_seeds) * 4 * (size_t)steps);
+  if (!seeds) return 1;
+  for (uint32_t i = 0; i < steps; i++) draw_seeds(seeds + 4 * (size_t)i);
+  if ((rc = sampo_set_seeds(s, 0, seeds, steps)) != SAMPO_OK) fail(s, "seeds", rc);
+  if ((rc = sampo_init_population(s, initial, init, age_days, age_seed)) != SAMPO_OK) fail(s, "initial population", rc);
+  sampo_population prev;
+  if ((rc = sampo_read_pool(s, &prev, NULL)) != SAMPO_OK) fail(s, "population", rc);
+
+  if (per_step) {
+    for (uint32_t i = 0; i < steps; i++) {
+      sampo_stats_row row;
+      /* the row of step i is the state the step starts from: print and
+       * check it first, as the reference does before its update */
+      if ((rc = sampo_current_row(s, &row)) != SAMPO_OK) fail(s, "row", rc);
+      check_agents(print_stats(&row, &prev, i, T[i]), capacity);
+      prev = row.pop;
+      if ((rc = sampo_step(s, &env[i], T[i], i % 24u, seeds + 4 * (size_t)i, NULL)) != SAMPO_OK) fail(s, "step", rc);
+    }
+  } else {
+    const uint32_t chunk = 24 * 30;
+    sampo_stats_row* rows = (sampo_stats_row*)sampo_host_alloc(sizeof(sampo_stats_row) * chunk);
+    if (!rows) return 1;
+    for (uint32_t first = 0; first < steps; first += chunk) {
+      const uint32_t n = steps - first < chunk ? steps - first : chunk;
+      rc = sampo_run(s, n, rows);
+      for (uint32_t j = 0; j < n && (rc == SAMPO_OK || j + 1 < n); j++) {
+        check_agents(print_stats(&rows[j], &prev, first + j, T[first + j]), capacity);
+        prev = rows[j].pop;
+      }
+      if (rc != SAMPO_OK) fail(s, "run", rc);
+    }
+    sampo_host_free(rows);
+  }
+
+  sampo_population final;
+  if ((rc = sampo_read_pool(s, &final, NULL)) != SAMPO_OK) fail(s, "population", rc);
+  print_population(&final);
+  uint32_t hist[100];
+  if ((rc = sampo_histogram(s, hist)) != SAMPO_OK) fail(s, "histogram", rc);
+  FILE* h = fopen("histogram.txt", "w");
+  if (h) {
+    for (int i = 0; i < 100; i++) fprintf(h, "%d, ", (int)hist[i]);
+    fclose(h);
+  }
+  sampo_destroy(s);
+  printf("Execution time: %f ms\n", now_ms() - t0);
+  free(seeds);
+  free(T);
+  free(env);
+  return 0;
+}
