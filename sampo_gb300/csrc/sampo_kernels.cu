@@ -328,9 +328,13 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
   uint32_t fail_rep = 0;
   bool failed = false;
 
-  // thread 0: take the next ticket into stage sidx and start its copies
+  // thread 0: take the next ticket into stage sidx and start its copies. The
+  // ticket was drawn one claim earlier, so the atomic's round trip overlaps
+  // a tile's work.
+  uint32_t t_next = 0;
   auto claim = [&](uint32_t sidx) {
-    const uint32_t t = atomicAdd(&p.bat->ticket1, 1u);
+    const uint32_t t = t_next;
+    t_next = atomicAdd(&p.bat->ticket1, 1u);
     s_tick[sidx] = t;
     if (t >= total) return;
     const uint32_t r = find_rep(s_pre, p.nrep, t);
@@ -378,6 +382,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     fence_mbar_init();
     s_cs[0].loaded = s_cs[1].loaded = 0xffffffffu;
     s_cs[0].rep = s_cs[1].rep = 0xffffffffu;
+    t_next = atomicAdd(&p.bat->ticket1, 1u);
     claim(0);
   }
   __syncthreads();
