@@ -147,6 +147,17 @@ int sampo_histogram(sampo_sim* s, uint32_t out[100]);
  * agent buffers; used for parity tests). The view's arrays must hold
  * pop.r[GRAVID].end entries; pass NULL to read the ranges only. */
 int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_view* pool);
+
+/* Checkpoint / resume at a step boundary (no counterpart in the reference,
+ * which runs a simulation to the end in one process). The file holds the
+ * step index, the population with its statistics, the counters the next stats
+ * row reports and every live slot; a simulation resumed from it continues bit
+ * for bit as if it had not stopped, given the same inputs and seeds for the
+ * later steps (seeds are the caller's: with srand/rand they are the stream
+ * after 16 x (step + 1) draws). Loading needs a handle with the file's
+ * carrying capacity and room for its pool. */
+int sampo_checkpoint_save(sampo_sim* s, const char* path);
+int sampo_checkpoint_load(sampo_sim* s, const char* path);
 /* Sticky device status bits (SAMPO_DEV_*) since creation or the last clear. */
 int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear);
 

@@ -129,6 +129,8 @@ SIGNATURES = {
                                      C.POINTER(Population), C.POINTER(Environment), C.c_float, C.c_uint32, _P,
                                      C.c_float, C.POINTER(StatsRow), C.POINTER(Population), C.POINTER(BitesCycles),
                                      C.c_int, _P]),
+    "sampo_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
+    "sampo_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
     "sampo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),
     "sampo_batch_destroy": (C.c_int, [_P]),
     "sampo_batch_last_error": (C.c_char_p, [_P]),

@@ -558,6 +558,104 @@ extern "C" int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_v
   return SAMPO_OK;
 }
 
+// ---- checkpoints: "SAMPOCK1", u32 version, u32 step, f32 cc, population,
+//      bites/cycles, u32 n, u32 0, then nine columns of n 4-byte values and
+//      the n flag bytes (state | isFemale << 3) ----
+namespace {
+const char kCkMagic[8] = {'S', 'A', 'M', 'P', 'O', 'C', 'K', '1'};
+struct CkHeader {
+  char magic[8];
+  uint32_t version, step;
+  float cc;
+  sampo_population pop;
+  sampo_bites_cycles bnc;
+  uint32_t n, reserved;
+};
+}  // namespace
+
+extern "C" int sampo_checkpoint_save(sampo_sim* s, const char* path) {
+  if (!s || !path) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
+  cudaSetDevice(s->device);
+  SimDev h;
+  CK(cudaMemcpyAsync(&h, s->sim_dev, sizeof(SimDev), cudaMemcpyDeviceToHost, s->stream), "state");
+  CK(cudaStreamSynchronize(s->stream), "state");
+  CkHeader hd;
+  memset(&hd, 0, sizeof(hd));
+  memcpy(hd.magic, kCkMagic, 8);
+  hd.version = 1;
+  hd.step = h.step;
+  hd.cc = s->cc;
+  hd.pop = h.pop;
+  hd.bnc = h.bnc;
+  hd.n = h.pop.r[7].end;
+  const size_t n = hd.n;
+  std::vector<uint8_t> buf(n * 4);
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(s, SAMPO_ERR_IO, std::string("cannot write ") + path);
+  bool ok = fwrite(&hd, sizeof(hd), 1, f) == 1;
+  const DevPool& P = s->pool[h.cur & 1u];
+  void* cols[9] = {P.age, P.his, P.delay, P.sporo, P.uni, P.avail, P.cycle, P.hbc, P.batches};
+  for (int c = 0; c < 9 && ok; c++) {
+    if (n && cudaMemcpy(buf.data(), cols[c], n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+    if (ok && n) ok = fwrite(buf.data(), 4, n, f) == n;
+  }
+  if (ok && n && cudaMemcpy(buf.data(), P.flags, n, cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+  if (ok && n) ok = fwrite(buf.data(), 1, n, f) == n;
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return fail(s, SAMPO_ERR_IO, std::string("checkpoint write failed: ") + path);
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
+  if (!s || !path) return SAMPO_ERR_ARG;
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(s, SAMPO_ERR_IO, std::string("cannot read ") + path);
+  CkHeader hd;
+  if (fread(&hd, sizeof(hd), 1, f) != 1 || memcmp(hd.magic, kCkMagic, 8) != 0 || hd.version != 1) {
+    fclose(f);
+    return fail(s, SAMPO_ERR_IO, std::string("not a checkpoint: ") + path);
+  }
+  if (hd.cc != s->cc) { fclose(f); return fail(s, SAMPO_ERR_ARG, "checkpoint carrying capacity differs from the handle's"); }
+  if ((uint64_t)hd.n > s->capacity || hd.pop.r[7].end != hd.n) { fclose(f); return fail(s, SAMPO_ERR_CAPACITY, "checkpoint pool exceeds the capacity"); }
+  cudaSetDevice(s->device);
+  const size_t n = hd.n;
+  std::vector<uint8_t> buf(n * 4);
+  const DevPool& P = s->pool[0];
+  void* cols[9] = {P.age, P.his, P.delay, P.sporo, P.uni, P.avail, P.cycle, P.hbc, P.batches};
+  bool ok = true;
+  for (int c = 0; c < 9 && ok; c++) {
+    ok = fread(buf.data(), 4, n, f) == n;
+    if (ok && n) ok = cudaMemcpy(cols[c], buf.data(), n * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+  }
+  if (ok) ok = fread(buf.data(), 1, n, f) == n;
+  if (ok && n) ok = cudaMemcpy(P.flags, buf.data(), n, cudaMemcpyHostToDevice) == cudaSuccess;
+  fclose(f);
+  if (!ok) return fail(s, SAMPO_ERR_IO, std::string("checkpoint read failed: ") + path);
+  // the state as a step boundary left it: step, ranges, the counters the next
+  // row reports; the statistics and step constants are recomputed
+  SimDev h = s->host_state;
+  h.pop = hd.pop;
+  h.pop.numLarvae1DayEquiv = h.pop.numFemale = h.pop.numPotentiallyInfective = 0;
+  h.bnc = hd.bnc;
+  h.step = hd.step;
+  h.active = 1;
+  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream), "tile reset");
+  CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state");
+  s->step = hd.step;
+  const int rc = publish_initial(s);
+  if (rc) return rc;
+  sampo_population p;
+  SimDev back;
+  CK(cudaMemcpyAsync(&back, s->sim_dev, sizeof(SimDev), cudaMemcpyDeviceToHost, s->stream), "state");
+  CK(cudaStreamSynchronize(s->stream), "state");
+  p = back.pop;
+  if (p.numLarvae1DayEquiv != hd.pop.numLarvae1DayEquiv || p.numFemale != hd.pop.numFemale ||
+      p.numPotentiallyInfective != hd.pop.numPotentiallyInfective)
+    return fail(s, SAMPO_ERR_INTERNAL, "checkpoint statistics do not match its pool");
+  return SAMPO_OK;
+}
+
 extern "C" int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear) {
   if (!s || !bits) return SAMPO_ERR_ARG;
   cudaSetDevice(s->device);

@@ -14,6 +14,7 @@ Typical use, equivalent to `bin/abms temp.txt environment.txt`:
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -175,6 +176,19 @@ class Simulation:
 
     def flush_l2(self):
         self._check(self.lib.sampo_flush_l2(self.h))
+
+    def checkpoint(self, path: str):
+        """Save the simulation at the current step boundary."""
+        self._check(self.lib.sampo_checkpoint_save(self.h, os.fsencode(path)))
+
+    def resume(self, path: str):
+        """Continue from a checkpoint (the handle keeps its inputs and seeds)."""
+        self._check(self.lib.sampo_checkpoint_load(self.h, os.fsencode(path)))
+
+    def get_step(self) -> int:
+        v = C.c_uint32()
+        self._check(self.lib.sampo_get_step(self.h, C.byref(v)))
+        return v.value
 
     def run_into(self, nsteps: int, rows_ptr: int):
         """sampo_run writing rows into caller memory (e.g. page-locked)."""
