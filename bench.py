@@ -199,6 +199,10 @@ def gpu_arm(args, wl, rank, world, device):
         if args.warmup:
             sim.run(24 * args.warmup, want_rows=False)
 
+    # the autotuner picks the step kernels' grid sizes on the first timed day's
+    # state (it leaves the run unchanged); they stay for every phase below
+    fresh()
+    tuned = sim.autotune()
     # ---- value: device-resident inputs, day graphs, L2 flushed between days ----
     fresh()
     sim.flush_l2()
@@ -269,7 +273,7 @@ def gpu_arm(args, wl, rank, world, device):
     return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(),
                 gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
-                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days)
+                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned)
 
 
 def cpu_reference(wl, seconds: float, first_steps: int | None = None, warmup: int = 0):
@@ -369,6 +373,7 @@ def ensemble_arm(args):
     b.sync()
     setup_batch = time.perf_counter() - t0
     b.run(24 * args.warmup)
+    tuned = b.autotune()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
         b.run(24 * args.steps)
@@ -390,6 +395,7 @@ def ensemble_arm(args):
             sim.init_population(s.initial, init, age_days_max=s.age_days_max, age_seed=s.seed)
             try:
                 r0 = sim.run(24 * args.warmup)
+                sim.autotune()  # each replicate tuned on its own (outside the timed run)
                 t1 = time.perf_counter()
                 r1 = sim.run(24 * args.steps)
                 plain_run_s += time.perf_counter() - t1
@@ -411,6 +417,7 @@ def ensemble_arm(args):
                                f"days {args.warmup}..{days} of a 365-day run; capacity 20 x initial + 65536",
                    "step": "one simulated day of every replicate (24 hourly steps, one CUDA graph)",
                    "initial_agents_total": int(sizes.sum()), "agent_days_timed": live_sum / 24.0,
+                   "ctas_per_sm": {"count": tuned[0], "scatter": tuned[1], "picked_by": "sampo_batch_autotune"},
                    "l2": "pools far larger than L2"},
         "batched": {"replicate_days_per_s": value, "sims_per_s_365d_equiv": value / 365.0,
                     "agent_days_per_s": live_sum / 24.0 / dev_batch, "wall_s": wall_batch, "device_s": dev_batch,
@@ -538,7 +545,8 @@ def main():
     pool_bytes = live_tot * RECORD_BYTES
     cfg.update({"days_timed": args.steps, "live_agents_min": int(live_tot.min()), "live_agents_max": int(live_tot.max()),
                 "l2": "flushed between timed days (write of a buffer > 2x L2); pool bytes %.2e..%.2e" % (pool_bytes.min(), pool_bytes.max()),
-                "parallelism": f"replicas x{world}"})
+                "parallelism": f"replicas x{world}",
+                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1], "picked_by": "sampo_autotune"}})
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,

@@ -157,6 +157,12 @@ int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_view* pool);
  * after 16 x (step + 1) draws). Loading needs a handle with the file's
  * carrying capacity and room for its pool. */
 int sampo_checkpoint_save(sampo_sim* s, const char* path);
+/* Autotuner (no counterpart in the reference): times the step kernels on the
+ * coming step of this simulation at every persistent grid size the occupancy
+ * allows (CTAs per SM of the count and update/scatter passes), keeps the
+ * fastest for the following steps and returns them. The trials leave the
+ * simulation's course unchanged. Needs the coming step's inputs. */
+int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
 int sampo_checkpoint_load(sampo_sim* s, const char* path);
 /* Sticky device status bits (SAMPO_DEV_*) since creation or the last clear. */
 int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear);
@@ -289,6 +295,8 @@ int sampo_batch_rows(sampo_batch* b, uint32_t slot, uint32_t first, uint32_t n, 
 int sampo_batch_state(sampo_batch* b, uint32_t slot, uint32_t* step, uint32_t* active, uint32_t* status_bits);
 int sampo_batch_histogram(sampo_batch* b, uint32_t slot, uint32_t out[100]);
 int sampo_batch_read_pool(sampo_batch* b, uint32_t slot, sampo_population* pop, sampo_pool_view* v);
+/* The autotuner of sampo_autotune over the batch's coming step. */
+int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
 /* Device time of the last sampo_batch_run, in milliseconds (after sync). */
 int sampo_batch_last_run_ms(sampo_batch* b, double* ms);
 

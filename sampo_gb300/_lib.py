@@ -130,6 +130,8 @@ SIGNATURES = {
                                      C.c_float, C.POINTER(StatsRow), C.POINTER(Population), C.POINTER(BitesCycles),
                                      C.c_int, _P]),
     "sampo_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
+    "sampo_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "sampo_batch_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
     "sampo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),
     "sampo_batch_destroy": (C.c_int, [_P]),

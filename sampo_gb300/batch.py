@@ -114,6 +114,12 @@ class Batch:
         self._check(self.lib.sampo_batch_read_pool(self.h, slot, C.byref(p), C.byref(v)))
         return popd, arrays
 
+    def autotune(self) -> tuple[int, int]:
+        """sampo_batch_autotune: CTAs per SM of the count and update/scatter passes."""
+        c, s = C.c_uint32(), C.c_uint32()
+        self._check(self.lib.sampo_batch_autotune(self.h, C.byref(c), C.byref(s)))
+        return c.value, s.value
+
     def last_run_ms(self) -> float:
         v = C.c_double()
         self._check(self.lib.sampo_batch_last_run_ms(self.h, C.byref(v)))

@@ -656,6 +656,33 @@ extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
   return SAMPO_OK;
 }
 
+extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm) {
+  if (!s) return SAMPO_ERR_ARG;
+  if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
+  const uint32_t slot = s->step % s->ring;
+  if (!s->have_inputs[slot] || s->input_step[slot] != s->step || s->seed_step[slot] != s->step)
+    return fail(s, SAMPO_ERR_STATE, "no inputs or seeds for the coming step");
+  cudaSetDevice(s->device);
+  const KParams p = make_params(s);
+  CK(launch_publish(p, PUB_REFRESH, s->stream), "step constants");
+  int gc = 0, gs = 0;
+  CK(tune_grids(p, s->stream, &gc, &gs, nullptr), "autotune");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+  if (sms <= 0) sms = 1;
+  if (gc != s->grid_count || gs != s->grid_scatter) {
+    s->grid_count = gc;
+    s->grid_scatter = gs;
+    if (s->day_graph) {  // captured with the old grids
+      cudaGraphExecDestroy(s->day_graph);
+      s->day_graph = nullptr;
+    }
+  }
+  if (count_ctas_per_sm) *count_ctas_per_sm = (uint32_t)(gc / sms);
+  if (scatter_ctas_per_sm) *scatter_ctas_per_sm = (uint32_t)(gs / sms);
+  return check_device(s);
+}
+
 extern "C" int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear) {
   if (!s || !bits) return SAMPO_ERR_ARG;
   cudaSetDevice(s->device);

@@ -433,6 +433,36 @@ extern "C" int sampo_batch_run(sampo_batch* b, uint32_t nsteps, int wait) {
   return SAMPO_OK;
 }
 
+extern "C" int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm) {
+  if (!b) return SAMPO_ERR_ARG;
+  for (uint32_t i = 0; i < b->nslots; i++) {
+    const Replicate& r = b->reps[i];
+    if (!r.used || !r.have_pop || !r.active) continue;
+    const uint32_t rs = r.step % b->ring;
+    if (r.input_step[rs] != r.step || r.seed_step[rs] != r.step)
+      return bfail(b, SAMPO_ERR_STATE, "slot " + std::to_string(i) + ": no inputs or seeds for the coming step");
+  }
+  cudaSetDevice(b->device);
+  const KParams p = all_params(b);
+  BCK(launch_publish(p, PUB_REFRESH, b->stream), "step constants");
+  int gc = 0, gs = 0;
+  BCK(tune_grids(p, b->stream, &gc, &gs, nullptr), "autotune");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (sms <= 0) sms = 1;
+  if (gc != b->grid_count || gs != b->grid_scatter) {
+    b->grid_count = gc;
+    b->grid_scatter = gs;
+    if (b->day_graph) {
+      cudaGraphExecDestroy(b->day_graph);
+      b->day_graph = nullptr;
+    }
+  }
+  if (count_ctas_per_sm) *count_ctas_per_sm = (uint32_t)(gc / sms);
+  if (scatter_ctas_per_sm) *scatter_ctas_per_sm = (uint32_t)(gs / sms);
+  return SAMPO_OK;
+}
+
 extern "C" int sampo_batch_sync(sampo_batch* b) {
   if (!b) return SAMPO_ERR_ARG;
   cudaSetDevice(b->device);

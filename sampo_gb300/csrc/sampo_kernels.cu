@@ -1036,6 +1036,26 @@ __global__ void k_init_eggs(KParams p, uint32_t n, float T0, const sampo_seeds* 
   }
 }
 
+// Before and after a timing trial of the step kernels: zero what they add to
+// (survivor counts, eggs laid, next-pool statistics, tickets). Their other
+// writes - the next buffer, and tile counts and prefixes equal to the ones
+// the real step computes - leave the simulation's course unchanged.
+__global__ void k_trial_reset(KParams p) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < p.nrep; r += gridDim.x * blockDim.x) {
+    SimDev* sim = p.reps[r].sim;
+    for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
+    sim->newEggs = 0;
+    sim->acc_L1de = sim->acc_fem = sim->acc_inf = 0;
+    sim->acc_dmin = 0xffffffffu;
+    sim->acc_dmax = 0;
+    for (int k = 0; k < 4; k++) sim->acc_bnc[k] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.bat->ticket1 = 0;
+    p.bat->ticket2 = 0;
+  }
+}
+
 // Statistics of p.reps[0]'s current pool (grid-stride), accumulated into acc_*.
 __global__ void k_pool_stats(KParams p) {
   SimDev* sim = p.reps[0].sim;
@@ -1169,6 +1189,48 @@ cudaError_t launch_publish_start(const KParams& p, cudaStream_t st) {
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st) {
   k_histogram<<<sm_count() * 4, 256, 0, st>>>(p, hist_dev);
   return cudaGetLastError();
+}
+cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, double* best_ms) {
+  set_smem_attrs();
+  int max_c = 0, max_s = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_c, k_count, kBlock, kCountSmem + plan_bytes(p.nrep));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_s, k_scatter, kScatterThreads, kScatterSmem + plan_bytes(p.nrep));
+  if (max_c < 1) max_c = 1;
+  if (max_s < 1) max_s = 1;
+  const int sms = sm_count();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  double best = 1e30;
+  int bc = max_c, bs = max_s;
+  const int reset_grid = (int)((p.nrep + 255) / 256);
+  for (int c = 1; c <= max_c && e == cudaSuccess; c++) {
+    for (int s = 1; s <= max_s && e == cudaSuccess; s++) {
+      double t = 1e30;
+      for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+        k_trial_reset<<<reset_grid, 256, 0, st>>>(p);
+        if ((e = cudaEventRecord(e0, st)) != cudaSuccess) break;
+        if ((e = launch_count(p, c * sms, st)) != cudaSuccess) break;
+        if ((e = launch_scatter(p, s * sms, st)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(e1, st)) != cudaSuccess) break;
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < t) t = ms;
+      }
+      if (t < best) { best = t; bc = c; bs = s; }
+    }
+  }
+  if (e == cudaSuccess) {
+    k_trial_reset<<<reset_grid, 256, 0, st>>>(p);
+    e = cudaStreamSynchronize(st);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  *grid_count = bc * sms;
+  *grid_scatter = bs * sms;
+  if (best_ms) *best_ms = best;
+  return e;
 }
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {
   k_eval_math<<<sm_count() * 2, 256, 0, st>>>(fn, x, y, out, n);

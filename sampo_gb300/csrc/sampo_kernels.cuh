@@ -126,5 +126,10 @@ cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo
 cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
+// Times count + scatter of the coming step at every (count, scatter) number
+// of CTAs per SM the occupancy allows and returns the fastest grids. The
+// trials leave the simulations' course unchanged (k_trial_reset); the coming
+// step's constants must be current (PUB_REFRESH) before the call.
+cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, double* best_ms);
 
 }  // namespace sampo

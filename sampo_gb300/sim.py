@@ -177,6 +177,13 @@ class Simulation:
     def flush_l2(self):
         self._check(self.lib.sampo_flush_l2(self.h))
 
+    def autotune(self) -> tuple[int, int]:
+        """Pick the step kernels' grid sizes on the coming step; returns the
+        CTAs per SM of the count and update/scatter passes."""
+        c, s = C.c_uint32(), C.c_uint32()
+        self._check(self.lib.sampo_autotune(self.h, C.byref(c), C.byref(s)))
+        return c.value, s.value
+
     def checkpoint(self, path: str):
         """Save the simulation at the current step boundary."""
         self._check(self.lib.sampo_checkpoint_save(self.h, os.fsencode(path)))

@@ -1,0 +1,52 @@
+"""The grid autotuner times the step kernels on the coming step and keeps the
+fastest grid sizes; a run tuned half-way must equal the untuned run bit for bit
+(plain and batched)."""
+import numpy as np
+import pytest
+
+from tests.golden.cases import CASES, make_case_inputs
+
+
+@pytest.mark.gpu
+def test_autotune_leaves_the_run_unchanged(gpu_ready, tmp_path):
+    from sampo_gb300 import inputs
+    from sampo_gb300.sim import Simulation, seed_stream
+    c = CASES["small_a"]
+    n, k = c["steps"], 100
+    tp, ep, _ = make_case_inputs("small_a", str(tmp_path))
+    T = inputs.read_temperature(tp, n)
+    env = inputs.read_environment(ep, n, c["cc"])
+    init, seeds = seed_stream(c["seed"], n)
+    out = []
+    for tune in (False, True):
+        with Simulation(capacity=1 << 20, carrying_capacity=c["cc"], max_steps=n + 1) as sim:
+            sim.set_inputs(T, env)
+            sim.set_seeds(0, seeds)
+            sim.init_population(c["initial"], init, c["age_days"], c["age_seed"])
+            rows = [sim.run(k)]
+            if tune:
+                cc_, cs = sim.autotune()
+                assert 1 <= cc_ <= 8 and 1 <= cs <= 2
+            rows.append(sim.run(n - k))
+            pop, arrays = sim.read_pool()
+            out.append((np.concatenate(rows), pop, arrays, sim.histogram(), sim.device_status()))
+    (r0, p0, a0, h0, s0), (r1, p1, a1, h1, s1) = out
+    assert r0.tobytes() == r1.tobytes()
+    assert np.array_equal(p0["ranges"], p1["ranges"])
+    for name in a0:
+        assert a0[name].tobytes() == a1[name].tobytes(), name
+    assert np.array_equal(h0, h1) and s0 == s1 == 0
+
+
+@pytest.mark.gpu
+def test_batch_autotune_leaves_replicates_unchanged(gpu_ready):
+    from sampo_gb300.batch import Batch, admit
+    from tests.test_batch import SPECS, compare
+    with Batch(max_replicates=4, ring_steps=80) as b:
+        slots = [admit(b, s, 72) for s in SPECS[:3]]
+        b.run(24)
+        cc_, cs = b.autotune()
+        assert cc_ >= 1 and cs >= 1
+        b.run(48)
+        for slot, spec in zip(slots, SPECS[:3]):
+            compare(b, slot, spec, 72, f"replicate {spec.seed} tuned half-way")
