@@ -349,7 +349,7 @@ def all_reduce(vals, op):
 def ensemble_arm(args):
     """BASELINE config 3 over a window of days: batched vs one at a time."""
     from sampo_gb300.batch import Batch, ensemble_specs
-    from sampo_gb300.sim import Simulation, seed_stream
+    from sampo_gb300.sim import Simulation, rand_state, seed_stream
     days = args.warmup + args.steps
     n = args.replicates
     # the hottest replicates reach 12x their initial size by day 15 (oracle)
@@ -360,15 +360,16 @@ def ensemble_arm(args):
         init, seeds = seed_stream(s.seed, s.steps)
         prep.append((T, env, init, seeds))
     ring = days * 24 + 1
-    # ---- batched ----
+    # ---- batched (each replicate draws its seeds on the device) ----
     t0 = time.perf_counter()
     b = Batch(n, ring)
     slots = []
     for s, (T, env, init, seeds) in zip(specs, prep):
         slot = b.add(s.capacity, s.cc, stop_step=s.steps)
         b.set_inputs(slot, T, env)
-        b.set_seeds(slot, 0, seeds)
+        init, stream = rand_state(s.seed)
         b.init_population(slot, s.initial, init, age_days_max=s.age_days_max, age_seed=s.seed)
+        b.seed_stream(slot, stream)
         slots.append(slot)
     b.sync()
     setup_batch = time.perf_counter() - t0
@@ -416,6 +417,8 @@ def ensemble_arm(args):
                                "own seed and weather each (mean T U[20,30] C, amplitude U[2,8] C, sd 0.5), "
                                f"days {args.warmup}..{days} of a 365-day run; capacity 20 x initial + 65536",
                    "step": "one simulated day of every replicate (24 hourly steps, one CUDA graph)",
+                   "seeds": "batched: drawn on the device per replicate (sampo_batch_seed_stream); "
+                            "one at a time: uploaded",
                    "initial_agents_total": int(sizes.sum()), "agent_days_timed": live_sum / 24.0,
                    "ctas_per_sm": {"count": tuned[0], "scatter": tuned[1], "picked_by": "sampo_batch_autotune"},
                    "l2": "pools far larger than L2"},

@@ -283,6 +283,17 @@ int sampo_batch_set_seeds(sampo_batch* b, uint32_t slot, uint32_t first, const s
 /* As sampo_init_population; activates the replicate at step 0. */
 int sampo_batch_init_population(sampo_batch* b, uint32_t slot, uint32_t n, const sampo_seeds init_seeds[4],
                                 int age_days_max, uint64_t age_seed);
+/* Device-side seed stream (the host loop's srand/rand, src/abms.c:611 and
+ * 145-150, moved onto the GPU): from the replicate's coming step on, the
+ * seeds of every step are the next 16 draws of `st`, made on the device once
+ * per step, so no seeds travel per step. `st` is the stream right before the
+ * coming step's draws (after the 16 initial ones for a replicate at step 0).
+ * Call after sampo_batch_init_population; sampo_batch_set_seeds then fails
+ * for the slot. */
+int sampo_batch_seed_stream(sampo_batch* b, uint32_t slot, const sampo_rand_state* st);
+/* The slot's device stream after the draws of every step before *next_step
+ * (a state sampo_rand_next continues). */
+int sampo_batch_seed_state(sampo_batch* b, uint32_t slot, sampo_rand_state* st, uint32_t* next_step);
 /* Advances every active replicate by nsteps (a replicate stops at its
  * stop_step). Asynchronous unless wait != 0; status of the replicates is
  * read with sampo_batch_state after sampo_batch_sync. */

@@ -142,6 +142,8 @@ SIGNATURES = {
     "sampo_batch_set_inputs": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint32]),
     "sampo_batch_set_seeds": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32]),
     "sampo_batch_init_population": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_int, C.c_uint64]),
+    "sampo_batch_seed_stream": (C.c_int, [_P, C.c_uint32, C.POINTER(RandState)]),
+    "sampo_batch_seed_state": (C.c_int, [_P, C.c_uint32, C.POINTER(RandState), C.POINTER(C.c_uint32)]),
     "sampo_batch_run": (C.c_int, [_P, C.c_uint32, C.c_int]),
     "sampo_batch_sync": (C.c_int, [_P]),
     "sampo_batch_rows": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),

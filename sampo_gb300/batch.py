@@ -15,8 +15,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib, inputs
-from ._lib import ENV_DTYPE, ROW_DTYPE, BatchConfig, Population, ReplicateConfig, SampoError, ptr
-from .sim import make_pool_arrays, pool_view, pop_to_numpy, seed_stream
+from ._lib import ENV_DTYPE, ROW_DTYPE, BatchConfig, Population, RandState, ReplicateConfig, SampoError, ptr
+from .sim import make_pool_arrays, pool_view, pop_to_numpy, rand_state, seed_stream
 
 NEVER = 0xFFFFFFFF
 
@@ -80,6 +80,17 @@ class Batch:
     def init_population(self, slot: int, n: int, init_seeds: np.ndarray, age_days_max: int = -1, age_seed: int = 0):
         init_seeds = np.ascontiguousarray(init_seeds, dtype=np.uint32).reshape(4, 4)
         self._check(self.lib.sampo_batch_init_population(self.h, slot, n, ptr(init_seeds), age_days_max, age_seed))
+
+    def seed_stream(self, slot: int, st: RandState):
+        """sampo_batch_seed_stream: the slot draws each coming step's seeds
+        from its own copy of the rand() stream `st` on the device."""
+        self._check(self.lib.sampo_batch_seed_stream(self.h, slot, C.byref(st)))
+
+    def seed_state(self, slot: int) -> tuple[RandState, int]:
+        """(device stream state, first step whose seeds it has not drawn)."""
+        st, nxt = RandState(), C.c_uint32()
+        self._check(self.lib.sampo_batch_seed_state(self.h, slot, C.byref(st), C.byref(nxt)))
+        return st, nxt.value
 
     def run(self, nsteps: int, wait: bool = True):
         self._check(self.lib.sampo_batch_run(self.h, nsteps, 1 if wait else 0))
@@ -179,14 +190,20 @@ def ensemble_specs(n: int, seed: int, days: int, size_range=(1e3, 1e6), growth: 
     return out
 
 
-def admit(batch: Batch, spec: ReplicateSpec, steps: int | None = None) -> int:
-    """Add one replicate to the batch with all its inputs and seeds (the
-    batch's ring must hold steps + 1 entries); returns its slot."""
+def admit(batch: Batch, spec: ReplicateSpec, steps: int | None = None, device_seeds: bool = False) -> int:
+    """Add one replicate to the batch with all its inputs (the batch's ring
+    must hold steps + 1 entries) and its seeds: uploaded for every step, or
+    drawn on the device from its rand() stream (device_seeds); returns its slot."""
     steps = spec.steps if steps is None else steps
     slot = batch.add(spec.capacity, spec.cc, stop_step=steps)
     T, env = spec.inputs()
-    init, seeds = seed_stream(spec.seed, steps)
     batch.set_inputs(slot, T[:steps], env[:steps])
-    batch.set_seeds(slot, 0, seeds)
+    if device_seeds:
+        init, st = rand_state(spec.seed)
+    else:
+        init, seeds = seed_stream(spec.seed, steps)
+        batch.set_seeds(slot, 0, seeds)
     batch.init_population(slot, spec.initial, init, age_days_max=spec.age_days_max, age_seed=spec.seed)
+    if device_seeds:
+        batch.seed_stream(slot, st)
     return slot

@@ -54,6 +54,7 @@ struct Replicate {
   void* mem = nullptr;
   RepParams rp;                // host copy of the kernels' view
   std::vector<uint32_t> input_step, seed_step;  // per ring slot: absolute step held
+  bool dev_seeds = false;      // seeds drawn on the device (sampo_batch_seed_stream)
   std::vector<float> T_host;
 };
 
@@ -251,7 +252,7 @@ extern "C" int sampo_batch_add(sampo_batch* b, const sampo_replicate_config* rc,
   q += L.tiles;
   rp.T = (const float*)q; q += L.T;
   rp.env = (const sampo_environment*)q; q += L.env;
-  rp.seeds = (const sampo_seeds*)q; q += L.seeds;
+  rp.seeds = (sampo_seeds*)q; q += L.seeds;
   rp.wt = (const uint32_t*)q; q += L.wt;
   rp.rows = (sampo_stats_row*)q;
   rp.ring = b->ring;
@@ -317,6 +318,7 @@ extern "C" int sampo_batch_set_seeds(sampo_batch* b, uint32_t slot, uint32_t fir
   Replicate* r = get_slot(b, slot);
   if (!r || !seeds) return SAMPO_ERR_ARG;
   if (nsteps == 0 || nsteps > b->ring) return bfail(b, SAMPO_ERR_ARG, "nsteps exceeds the seed ring");
+  if (r->dev_seeds) return bfail(b, SAMPO_ERR_STATE, "the slot draws its seeds on the device");
   cudaSetDevice(b->device);
   uint32_t done = 0;
   while (done < nsteps) {
@@ -365,6 +367,37 @@ extern "C" int sampo_batch_init_population(sampo_batch* b, uint32_t slot, uint32
   r->have_pop = true;
   r->step = 0;
   r->active = r->stop_step > 0;
+  r->dev_seeds = false;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_seed_stream(sampo_batch* b, uint32_t slot, const sampo_rand_state* st) {
+  Replicate* r = get_slot(b, slot);
+  if (!r || !st) return SAMPO_ERR_ARG;
+  if (!r->have_pop) return bfail(b, SAMPO_ERR_STATE, "initialise the population first");
+  // rotate so that the oldest word comes first (the draw at position i reads
+  // r[i % 31] and r[(i - 3) % 31])
+  DevSeedStream h;
+  h.next = r->step;
+  for (uint32_t j = 0; j < 31; j++) h.st.r[j] = st->r[(st->i + j) % 31];
+  h.st.i = 31u * (st->i / 31u + 1u);
+  cudaSetDevice(b->device);
+  BCK(cudaMemcpyAsync(&b->sims_dev[slot].rnd, &h, sizeof(h), cudaMemcpyHostToDevice, b->stream), "seed stream");
+  BCK(cudaStreamSynchronize(b->stream), "seed stream");
+  r->dev_seeds = true;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_seed_state(sampo_batch* b, uint32_t slot, sampo_rand_state* st, uint32_t* next_step) {
+  Replicate* r = get_slot(b, slot);
+  if (!r || !st || !next_step) return SAMPO_ERR_ARG;
+  if (!r->dev_seeds) return bfail(b, SAMPO_ERR_STATE, "the slot has no device seed stream");
+  cudaSetDevice(b->device);
+  DevSeedStream h;
+  BCK(cudaMemcpyAsync(&h, &b->sims_dev[slot].rnd, sizeof(h), cudaMemcpyDeviceToHost, b->stream), "seed stream");
+  BCK(cudaStreamSynchronize(b->stream), "seed stream");
+  *st = h.st;
+  *next_step = h.next;
   return SAMPO_OK;
 }
 
@@ -407,7 +440,7 @@ extern "C" int sampo_batch_run(sampo_batch* b, uint32_t nsteps, int wait) {
     const uint32_t last = (uint32_t)std::min<uint64_t>((uint64_t)r.step + nsteps, r.stop_step);
     for (uint32_t st = r.step; st < last; st++) {
       const uint32_t rs = st % b->ring;
-      if (r.input_step[rs] != st || r.seed_step[rs] != st)
+      if (r.input_step[rs] != st || (!r.dev_seeds && r.seed_step[rs] != st))
         return bfail(b, SAMPO_ERR_STATE, "slot " + std::to_string(i) + ": no inputs or seeds for step " + std::to_string(st));
     }
   }
@@ -439,7 +472,7 @@ extern "C" int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm,
     const Replicate& r = b->reps[i];
     if (!r.used || !r.have_pop || !r.active) continue;
     const uint32_t rs = r.step % b->ring;
-    if (r.input_step[rs] != r.step || r.seed_step[rs] != r.step)
+    if (r.input_step[rs] != r.step || (!r.dev_seeds && r.seed_step[rs] != r.step))
       return bfail(b, SAMPO_ERR_STATE, "slot " + std::to_string(i) + ": no inputs or seeds for the coming step");
   }
   cudaSetDevice(b->device);

@@ -169,6 +169,30 @@ __device__ void compute_ctx(const RepParams& rp, const sampo_population& pop, ui
   sampo_split_double(c.sporoInc, &c.sporoH, &c.sporoM, &c.sporoL);
 }
 
+// generateSeeds (src/abms.c:145-150) on the device: the 16 rand() draws of a
+// step (z1..z4 of seed slots 0..3) from the replicate's rotated glibc TYPE_3
+// state, by one warp. Lane j holds r[j]; draw k is r[k] + r[k+28] for k < 3
+// and r[k] + draw(k-3) after that, resolved in five shuffle rounds. The draws
+// go to the step's ring slot (output = value >> 1) and the state keeps the 31
+// newest values, oldest first.
+__device__ void draw_step_seeds(const RepParams& rp, uint32_t step) {
+  DevSeedStream& s = rp.sim->rnd;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t x = lane < 31u ? s.st.r[lane] : 0u;
+  uint32_t v = x + __shfl_sync(0xffffffffu, x, (lane + 28u) & 31u);  // final on lanes 0..2
+#pragma unroll
+  for (int it = 0; it < 5; it++) {  // after round it, lanes below 3 * (it + 2) are final
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, v, 3);
+    if (lane >= 3u) v = x + prev;
+  }
+  uint32_t* out = reinterpret_cast<uint32_t*>(rp.seeds + (size_t)(step % rp.ring) * 4);
+  if (lane < 16u) out[lane] = v >> 1;
+  const uint32_t kept = __shfl_sync(0xffffffffu, x, (lane + 16u) & 31u);
+  const uint32_t drawn = __shfl_sync(0xffffffffu, v, (lane + 17u) & 31u);  // lane j >= 15: draw j - 15
+  if (lane < 31u) s.st.r[lane] = lane < 15u ? kept : drawn;
+  if (lane == 0u) s.next = step + 1u;
+}
+
 template <class T>
 __device__ void load_model_const(const T* g, T& s) {
   const float* src = reinterpret_cast<const float*>(g);
@@ -484,6 +508,12 @@ __global__ void k_publish(KParams p, int mode) {
   }
   const RepParams& rp = p.reps[blockIdx.x];
   SimDev* sim = rp.sim;
+  if (threadIdx.x < 32) {
+    // a device seed stream draws the coming step's seeds once, before thread 0 reads them
+    const uint32_t coming = sim->step + (mode == PUB_AFTER_STEP ? 1u : 0u);
+    if (sim->active && sim->rnd.next == coming && coming < sim->stop_step) draw_step_seeds(rp, coming);
+    __syncwarp();
+  }
   if (mode == PUB_REFRESH) {
     if (threadIdx.x == 0 && sim->active) compute_ctx(rp, sim->pop, sim->step, sim->ctx);
     return;

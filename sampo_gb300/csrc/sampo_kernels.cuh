@@ -28,6 +28,16 @@ struct DevPool {
 };
 
 // Device-resident state of one simulation.
+// A glibc rand() stream held on the device (generateSeeds, src/abms.c:145-150,
+// drawn by k_publish for each coming step). The 31 words are kept rotated so
+// that st.r[0] is the oldest (the next draw is r[0] + r[28]); st.i is a
+// multiple of 31, so the state also continues on the host's sampo_rand_next.
+struct DevSeedStream {
+  uint32_t next;              // step whose seeds are drawn next; kNoStream: seeds come from the host
+  sampo_rand_state st;
+};
+constexpr uint32_t kNoStream = 0xffffffffu;
+
 struct SimDev {
   sampo_population pop;       // ranges + stats of the current pool (reference pop[0] at step start)
   sampo_bites_cycles bnc;     // counters of the last update (printed with the next row)
@@ -44,6 +54,7 @@ struct SimDev {
   float cc;                   // carrying capacity (constant per run, src/abms.c:19,132)
   uint32_t active;            // 1: the replicate takes part in the batch's steps
   uint32_t stop_step;         // becomes inactive once step reaches this
+  DevSeedStream rnd;          // the replicate's own rand() stream, when its seeds are drawn on the device
   StepCtx ctx;                // constants of step `step` (valid while active)
   float larvaHMR[100];        // larval hourly mortality of step `step` by age in days
 };
@@ -63,7 +74,7 @@ struct RepParams {
   uint32_t* tileFlag;         // [maxTiles] epoch when tileIncl is valid
   const float* T;             // [ring] temperature per step
   const sampo_environment* env;  // [ring]
-  const sampo_seeds* seeds;   // [ring][4]
+  sampo_seeds* seeds;         // [ring][4] (written by the device for a device seed stream)
   const uint32_t* wt;         // [ring] world time per step
   sampo_stats_row* rows;      // [ring] stats at the start of each step
   uint32_t ring;
@@ -104,6 +115,7 @@ inline SimDev initial_sim_state(uint32_t capacity, float cc) {
   h.acc_dmin = 0xffffffffu;
   h.epoch = 1;
   h.stop_step = 0xffffffffu;
+  h.rnd.next = kNoStream;
   return h;
 }
 

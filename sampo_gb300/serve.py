@@ -21,7 +21,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .batch import Batch, ReplicateSpec
-from .sim import Simulation, seed_stream
+from ._lib import RandState
+from .sim import Simulation, rand_state, seed_stream
 
 
 @dataclass
@@ -72,7 +73,7 @@ class _Prepared:
     T: np.ndarray
     env: np.ndarray
     init: np.ndarray
-    seeds: np.ndarray
+    stream: RandState  # srand(seed) after the initial draws; the device draws the rest
 
 
 class Server:
@@ -96,16 +97,16 @@ class Server:
     @staticmethod
     def _prepare(spec: ReplicateSpec) -> _Prepared:
         T, env = spec.inputs()
-        init, seeds = seed_stream(spec.seed, spec.steps)
-        return _Prepared(T, env, init, seeds)
+        init, stream = rand_state(spec.seed)
+        return _Prepared(T, env, init, stream)
 
     def _admit(self, req: Request, prep: _Prepared, res: Result, now: float):
         s = req.spec
         b = self.batch
         slot = b.add(s.capacity, s.cc, stop_step=s.steps)
         b.set_inputs(slot, prep.T, prep.env)
-        b.set_seeds(slot, 0, prep.seeds)
         b.init_population(slot, s.initial, prep.init, age_days_max=s.age_days_max, age_seed=s.seed)
+        b.seed_stream(slot, prep.stream)
         nbytes = self.bytes_for(s)
         self.used += nbytes
         res.admitted = now

@@ -37,6 +37,17 @@ def seed_stream(seed: int, nsteps: int):
     return init, steps
 
 
+def rand_state(seed: int):
+    """srand(seed) and the 16 initial draws (src/abms.c:611,671): returns
+    (initial seeds (4,4), the stream positioned before step 0's draws)."""
+    lib = _lib.load()
+    st = RandState()
+    lib.sampo_rand_seed(C.byref(st), seed & 0xFFFFFFFF)
+    init = np.zeros((4, 4), dtype=np.uint32)
+    lib.sampo_rand_seeds(C.byref(st), ptr(init), 1)
+    return init, st
+
+
 def make_pool_arrays(n: int) -> dict:
     return {name: np.zeros(n, dtype=dt) for name, dt in POOL_COLUMNS}
 
