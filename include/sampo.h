@@ -206,10 +206,11 @@ int sampo_read_environment_file(const char* path, sampo_environment* out, uint32
  * code running where allocation is forbidden or unsafe (inside another
  * framework's memory pool or arena, a host that must not grow device memory
  * after start-up, a memory-capped sandbox). They bring their own pool
- * buffers; the step's scratch (step state, look-back tile counts, one step
- * of inputs and stats) lives in a fixed array inside the library, sized for
- * pools of up to SAMPO_NOALLOC_MAX_SLOTS slots (about 1.1 MB, held by every
- * GPU that loads the library until the process exits).
+ * buffers; the step's scratch (step state, per-tile prefix tables and
+ * look-back counts, one step of inputs and stats) lives in a fixed array
+ * inside the library, sized for pools of up to SAMPO_NOALLOC_MAX_SLOTS slots
+ * (about 12 MB, held by every GPU that loads the library until the process
+ * exits).
  *
  * in/out: device columns of two pool buffers; each column 16-byte aligned
  * with 16 bytes of slack after capacity elements; flags = state |

@@ -75,7 +75,7 @@ def build_cli(force: bool = False) -> str:
     lib = build_library()
     if force or _stale(CLI, [src, lib, os.path.join(REPO, "include", "sampo.h")]):
         _run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", f"-I{os.path.join(REPO, 'include')}", src,
-              "-o", CLI, f"-L{OUT}", "-lsampo_cuda", f"-Wl,-rpath,{OUT}", "-lm"])
+              "-o", CLI, f"-L{OUT}", "-lsampo_cuda", f"-Wl,-rpath,{OUT}", "-lm", "-pthread"])
     return CLI
 
 

@@ -79,16 +79,13 @@ static RepParams make_rep(sampo_sim* s) {
   r.sim = s->sim_dev;
   r.pool[0] = s->pool[0];
   r.pool[1] = s->pool[1];
-  r.tileAgg = s->tile_mem;
-  r.tileIncl = s->tile_mem + (size_t)s->max_tiles * 8;
-  r.tileFlag = s->tile_mem + (size_t)s->max_tiles * 16;
+  set_tile_arrays(r, s->tile_mem, s->max_tiles);
   r.T = s->T_dev;
   r.env = s->env_dev;
   r.seeds = s->seeds_dev;
   r.wt = s->wt_dev;
   r.rows = s->rows_dev;
   r.ring = s->ring;
-  r.maxTiles = s->max_tiles;
   return r;
 }
 
@@ -153,8 +150,8 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     }
     if (rc) break;
     s->max_tiles = (uint32_t)((C + kTile - 1) / kTile);
-    if ((e = cudaMalloc(&s->tile_mem, (size_t)s->max_tiles * 17 * 4)) != cudaSuccess) { rc = cuda_fail(s, e, "tile arrays"); break; }
-    cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream);
+    if ((e = cudaMalloc(&s->tile_mem, (size_t)s->max_tiles * kTileArrayWords * 4)) != cudaSuccess) { rc = cuda_fail(s, e, "tile arrays"); break; }
+    cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream);
     if ((e = cudaMalloc(&s->sim_dev, sizeof(SimDev))) != cudaSuccess ||
         (e = cudaMalloc(&s->rep_dev, sizeof(RepParams))) != cudaSuccess ||
         (e = cudaMalloc(&s->bat_dev, sizeof(BatchDev))) != cudaSuccess ||
@@ -260,7 +257,7 @@ static int reset_state(sampo_sim* s, const sampo_population& pop) {
   // running step's epoch. Epochs restart here, so flags left by an earlier
   // run must go: clear the tile arrays before the first step.
   h.epoch = 1;
-  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream), "tile reset");
+  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream), "tile reset");
   CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state reset");
   s->step = 0;
   return SAMPO_OK;
@@ -640,7 +637,7 @@ extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
   h.bnc = hd.bnc;
   h.step = hd.step;
   h.active = 1;
-  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * 17 * 4, s->stream), "tile reset");
+  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream), "tile reset");
   CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state");
   s->step = hd.step;
   const int rc = publish_initial(s);

@@ -33,7 +33,7 @@ struct RepLayout {
     col1 = align256(capacity + 16);
     pool = 9 * col4 + col1;
     max_tiles = (uint32_t)((capacity + kTile - 1) / kTile);
-    tiles = align256((size_t)max_tiles * 17 * 4);
+    tiles = align256((size_t)max_tiles * kTileArrayWords * 4);
     T = align256((size_t)ring * sizeof(float));
     env = align256((size_t)ring * sizeof(sampo_environment));
     seeds = align256((size_t)ring * 4 * sizeof(sampo_seeds));
@@ -246,9 +246,7 @@ extern "C" int sampo_batch_add(sampo_batch* b, const sampo_replicate_config* rc,
     P.flags = (uint8_t*)(q + 9 * L.col4);
   }
   char* q = m + 2 * L.pool;
-  rp.tileAgg = (uint32_t*)q;
-  rp.tileIncl = rp.tileAgg + (size_t)L.max_tiles * 8;
-  rp.tileFlag = rp.tileAgg + (size_t)L.max_tiles * 16;
+  set_tile_arrays(rp, (uint32_t*)q, L.max_tiles);
   q += L.tiles;
   rp.T = (const float*)q; q += L.T;
   rp.env = (const sampo_environment*)q; q += L.env;
@@ -256,8 +254,7 @@ extern "C" int sampo_batch_add(sampo_batch* b, const sampo_replicate_config* rc,
   rp.wt = (const uint32_t*)q; q += L.wt;
   rp.rows = (sampo_stats_row*)q;
   rp.ring = b->ring;
-  rp.maxTiles = L.max_tiles;
-  BCK(cudaMemsetAsync(rp.tileAgg, 0, (size_t)L.max_tiles * 17 * 4, b->stream), "tile arrays");
+  BCK(cudaMemsetAsync(rp.tilePre, 0, (size_t)L.max_tiles * kTileArrayWords * 4, b->stream), "tile arrays");
   SimDev h = initial_sim_state((uint32_t)rc->capacity, rc->carrying_capacity);
   h.stop_step = rc->stop_step;
   const int st = upload_slot(b, i, h);
@@ -358,7 +355,7 @@ extern "C" int sampo_batch_init_population(sampo_batch* b, uint32_t slot, uint32
   h.stop_step = r->stop_step;
   const int st = upload_slot(b, slot, h);
   if (st) return st;
-  BCK(cudaMemsetAsync(r->rp.tileAgg, 0, (size_t)r->rp.maxTiles * 17 * 4, b->stream), "tile arrays");
+  BCK(cudaMemsetAsync(r->rp.tilePre, 0, (size_t)r->rp.maxTiles * kTileArrayWords * 4, b->stream), "tile arrays");
   BCK(cudaMemcpyAsync(b->init_seeds_dev + (size_t)slot * 4, init_seeds, 4 * sizeof(sampo_seeds), cudaMemcpyHostToDevice, b->stream),
       "seeds");
   const KParams p = slot_params(b, slot);

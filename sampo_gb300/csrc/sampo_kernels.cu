@@ -48,7 +48,9 @@ __device__ const float kDevRates[32] = {
 
 constexpr uint32_t kColBytes = kTile * 4;                    // one 4-byte column of a tile
 constexpr uint32_t kCountStage = 5 * kColBytes + kTile;      // age, his, delay, uni, avail, flags
-constexpr uint32_t kScatterStage = 9 * kColBytes + kTile;    // the nine 4-byte columns and the flags
+constexpr uint32_t kPreOff = 9 * kColBytes + kTile;          // the nine 4-byte columns and the flags,
+constexpr uint32_t kScatterStage = kPreOff + kPreWords * 4;   // then the tile's prefix table
+static_assert(kPreOff % 16 == 0 && kScatterStage % 16 == 0, "bulk copies land on 16-byte boundaries");
 constexpr uint32_t kWaitLimit = 1u << 22;                    // bounded mbarrier waits
 
 // ---------------- memory-model and TMA helpers ----------------
@@ -319,6 +321,7 @@ struct alignas(16) CountStage {
   sampo_population pop;
   DevPool src;
   uint32_t* tileAgg;
+  uint32_t* tilePre;
   uint32_t rep, lt, end, larv;    // replicate, its tile index, its pool end, larvicide on
   uint32_t loaded;                // replicate whose c is loaded
 };
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
   uint32_t* s_pre = reinterpret_cast<uint32_t*>(dsm + kCountSmem);
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ uint32_t s_tick[2];
-  __shared__ uint32_t s_wcnt[kWarps][8];
+  __shared__ uint2 s_ent[kChunks];  // per (round, warp): survivors by state, 8-bit fields (states 0-3 | 4-7)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   load_model_const(&p.mc->kill, s_mc);
   plan_tickets(p.nrep, s_pre, s_w, [&](uint32_t r) -> uint32_t {
@@ -371,6 +374,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
       cs.end = cs.pop.r[GRAVID].end;
       cs.src = rp.pool[sim->cur];
       cs.tileAgg = rp.tileAgg;
+      cs.tilePre = rp.tilePre;
       cs.larv = sim->ctx.env.larvacideValue > 0.0f;
     }
     cs.lt = t - s_pre[r];
@@ -434,12 +438,12 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     const uint32_t* s_uni = (const uint32_t*)(st + 3 * kColBytes);
     const uint32_t* s_avail = (const uint32_t*)(st + 4 * kColBytes);
     const uint8_t* s_flags = st + 5 * kColBytes;
-    uint32_t pk0 = 0, pk1 = 0;  // 8-bit survivor counters: buckets 0-3, 4-7
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       const uint32_t i = k * kBlock + tid;
       const uint32_t g = lo + i;
       const int rg = (ok && g < end) ? range_of(cs.pop, g) : -1;
+      uint32_t pk0 = 0, pk1 = 0;  // this slot's next state as an 8-bit counter: states 0-3, 4-7
       if (rg >= 0) {
         Rec a;
         a.age = (rg == LARVA || rg >= IMMATURE) ? s_age[i] : 0.0f;
@@ -452,22 +456,54 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
         devoob |= (rg == LARVA) & c.devOOB;
         const int ns = update_agent<false>(c, s_mc, rg, g, a, acc);
         if (ns >= 0) {
-          if (ns < 4) pk0 += 1u << (8 * ns);
-          else pk1 += 1u << (8 * (ns - 4));
+          if (ns < 4) pk0 = 1u << (8 * ns);
+          else pk1 = 1u << (8 * (ns - 4));
         }
       }
+      pk0 = __reduce_add_sync(0xffffffffu, pk0);
+      pk1 = __reduce_add_sync(0xffffffffu, pk1);
+      if (lane == 0) s_ent[k * kWarps + warp] = make_uint2(pk0, pk1);
     }
-    pk0 = __reduce_add_sync(0xffffffffu, pk0);
-    pk1 = __reduce_add_sync(0xffffffffu, pk1);
-    if (lane < 8) s_wcnt[warp][lane] = ((lane < 4 ? pk0 : pk1) >> (8 * (lane & 3))) & 0xffu;
     __syncthreads();
     const uint32_t rep = cs.rep;
-    if (tid < 8) {
-      uint32_t sum = 0;
+    if (warp == 0) {
+      // the tile's prefix table: exclusive prefix of the 32 (round, warp)
+      // chunks, 16-bit packed, and the tile's totals (the update/scatter pass
+      // reads both; the totals also feed the look-back)
+      const uint2 e = s_ent[lane];
+      uint32_t w[5], x[5];
+      w[0] = (e.x & 0xffu) | ((e.x & 0xff00u) << 8);
+      w[1] = ((e.x >> 16) & 0xffu) | ((e.x >> 8) & 0xff0000u);
+      w[2] = (e.y & 0xffu) | ((e.y & 0xff00u) << 8);
+      w[3] = ((e.y >> 16) & 0xffu) | ((e.y >> 8) & 0xff0000u);
+      w[4] = ((e.x * 0x01010101u) >> 24) + ((e.y * 0x01010101u) >> 24);  // byte sums <= 32 cannot carry
 #pragma unroll
-      for (int w = 0; w < kWarps; w++) sum += s_wcnt[w][tid];
-      cs.tileAgg[(size_t)cs.lt * 8 + tid] = sum;
-      cta_cnt += sum;
+      for (int q = 0; q < 5; q++) x[q] = w[q];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, x[q], o);
+          if (lane >= o) x[q] += y;
+        }
+      }
+      uint32_t* pre = cs.tilePre + (size_t)cs.lt * kPreWords;
+#pragma unroll
+      for (int q = 0; q < 5; q++) pre[lane * kPreEntryWords + q] = x[q] - w[q];
+      if (lane == 31) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) pre[kChunks * kPreEntryWords + q] = x[q];
+      }
+      uint32_t tw = 0;  // lanes 0..7: the tile's survivors of next state `lane`
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint32_t t = __shfl_sync(0xffffffffu, x[q], 31);
+        if ((lane >> 1) == q) tw = (t >> (16 * (lane & 1))) & 0xffffu;
+      }
+      if (lane < 8) {
+        cs.tileAgg[(size_t)cs.lt * 8 + lane] = tw;
+        cta_cnt += tw;
+      }
     }
     if (!ok) fail_rep = rep;
     // the next tile was claimed above and is visible after the barrier
@@ -589,9 +625,10 @@ __global__ void k_publish(KParams p, int mode) {
 // ------------------------------------------------------------------------
 // Update + scatter pass
 // ------------------------------------------------------------------------
-__device__ void issue_scatter_tile(const DevPool& src, uint8_t* st, uint64_t* bar, uint32_t lo, uint32_t n) {
+__device__ void issue_scatter_tile(const DevPool& src, const uint32_t* pre, uint8_t* st, uint64_t* bar, uint32_t lo, uint32_t n) {
   const uint32_t b4 = (n * 4 + 15) & ~15u, b1 = (n + 15) & ~15u;
-  mbar_arrive_tx(bar, 9 * b4 + b1);
+  mbar_arrive_tx(bar, 9 * b4 + b1 + kPreWords * 4);
+  bulk_load(st + kPreOff, pre, kPreWords * 4, bar);
   bulk_load(st + 0 * kColBytes, src.age + lo, b4, bar);
   bulk_load(st + 1 * kColBytes, src.his + lo, b4, bar);
   bulk_load(st + 2 * kColBytes, src.delay + lo, b4, bar);
@@ -647,14 +684,6 @@ __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epo
   }
 }
 
-// Named barrier of the eight consumer warps (the producer warp is not in it),
-// returning whether any consumer passed v = true.
-__device__ __forceinline__ bool consumer_sync_or(bool v) {
-  uint32_t r;
-  asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, 256, q;\n\tselp.u32 %0, 1, 0, p;\n}"
-               : "=r"(r) : "r"((uint32_t)v) : "memory");
-  return r != 0;
-}
 __device__ __forceinline__ void mbar_init_count(uint64_t* bar, uint32_t n) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(n) : "memory");
 }
@@ -663,8 +692,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one producer warp
-static_assert(kBlock == 256, "consumer_sync_or() names 256 threads");
-static_assert(kItems * kWarps == 32, "one (round, warp) count entry per lane");
+static_assert(kChunks == 32, "one (round, warp) chunk per lane");
 enum : uint32_t { TK_OLD = 0, TK_EGG = 1, TK_END = 2 };
 
 // What the producer warp hands the consumers with a tile. The replicate's
@@ -674,6 +702,7 @@ struct alignas(16) ScatterStage {
   sampo_population pop;      // its current ranges
   DevPool dst, src;          // its next and current buffers
   LookbackArrays lb;         // its look-back arrays
+  const uint32_t* pre;       // its prefix tables
   uint32_t rep, end, newEggs, nold, epoch;  // replicate, pool end, eggs laid, old tiles, look-back epoch
   uint32_t base[8];          // first slot of each next-state range
   uint32_t kind, lo;         // TK_*, first slot (old tile) or first egg id (egg tile)
@@ -689,10 +718,13 @@ struct BmEntry { uint32_t d, gid, batches, kind; };
 // The producer warp describes tiles three ahead (ticket, replicate data,
 // look-back, layout) and hands each to the consumers in a free stage with
 // its TMA loads (full[s]: the expect-tx arrival + the arrival that publishes
-// the description). Consumers release a stage (empty[s], 256 arrivals) as
-// soon as they have read its inputs, then write every survivor straight to
-// its slot in the next buffer: the survivors of one next state are
-// contiguous within a warp, so the stores coalesce.
+// the description). A stage carries the tile's columns and the count pass's
+// prefix table of its (round, warp) chunks, so every consumer warp knows
+// where its survivors go without the other warps: the consumer warps share
+// no barrier. Each releases a stage (empty[s], 256 arrivals) as soon as it
+// has read its inputs, then writes every survivor straight to its slot in the
+// next buffer: the survivors of one next state are contiguous within a warp,
+// so the stores coalesce.
 __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ ScatterStage s_si[kDescSlots];
@@ -700,7 +732,6 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
   __shared__ uint32_t s_w[33];
   uint32_t* s_pre = reinterpret_cast<uint32_t*>(dsm + kScatterSmem);
   __shared__ __align__(8) uint64_t full[2], empty[2];
-  __shared__ uint4 s_cnt4[2][kItems * kWarps];      // per stage and (round, warp): survivors by state, 16-bit packed
   __shared__ BmEntry s_bmq[kWarps][kItems * 32];    // per warp: owed draws of the tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   load_model_const(p.mc, s_mc);
@@ -761,6 +792,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           si.lb.agg = rp.tileAgg;
           si.lb.incl = rp.tileIncl;
           si.lb.flag = rp.tileFlag;
+          si.pre = rp.tilePre;
           uint32_t tc[8], base[8];
           for (int k = 0; k < 8; k++) tc[k] = sim->cnt[k];
           sampo_population np;
@@ -801,7 +833,8 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
       if (lane == 0) {
         if (si.kind == TK_OLD) {
           fence_proxy_async();  // the stage was last read through the generic proxy
-          issue_scatter_tile(si.src, dsm + s * kScatterStage, &full[s], si.lo, min((uint32_t)kTile, si.end - si.lo));
+          issue_scatter_tile(si.src, si.pre + (size_t)(si.lo / kTile) * kPreWords, dsm + s * kScatterStage, &full[s], si.lo,
+                             min((uint32_t)kTile, si.end - si.lo));
         } else {
           mbar_arrive(&full[s]);
         }
@@ -834,7 +867,6 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     }
   } else {
     // ================= consumer warps =================
-    // One named barrier per tile (after the survivor counts).
     const ModelConst& mc = s_mc;
     Acc acc = {0, 0, 0, 0, 0, 0};
     uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0, tilebad = 0;
@@ -866,8 +898,8 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     for (uint32_t it = 0;; it++) {
       const uint32_t s = it & 1u;
       const uint8_t* st = dsm + s * kScatterStage;
-      const bool ok = mbar_wait(&full[s], (ph >> s) & 1u);  // bounded; acquires the stage
-      ph ^= 1u << s;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[s], (ph >> s) & 1u));  // bounded; acquires the stage
+      if (ok) ph ^= 1u << s;  // else the phase is still owed: the exit path waits for it again
       const ScatterStage& si = s_si[it % kDescSlots];
       const uint32_t kind = ok ? si.kind : TK_END;
       if (kind != TK_END && si.rep != cur_rep) {
@@ -875,10 +907,12 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         cur_rep = si.rep;
       }
       // ---- phase A (old tiles): recompute the step for the tile's agents and
-      //      count the survivors of each (round, warp) by next state ----
+      //      find each survivor's slot: the tile's first slot of its next
+      //      state + the survivors of that state in earlier (round, warp)
+      //      chunks (prefix table) + its rank within its chunk ----
       Rec a[kItems];
-      int nb[kItems];
-      uint32_t rk[kItems];
+      uint32_t nb[kItems];  // after phase A: next state (8: none) | female << 4 | owed draw << 5
+      uint32_t dk[kItems];
       if (kind == TK_OLD) {
         const float* c_age = (const float*)(st + 0 * kColBytes);
         const float* c_his = (const float*)(st + 1 * kColBytes);
@@ -890,6 +924,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
         const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
         const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
         const uint8_t* c_flags = st + 9 * kColBytes;
+        const uint32_t* c_pre = (const uint32_t*)(st + kPreOff);
         const StepCtx& c = si.c;
         const uint32_t lo = si.lo, end = si.end;
 #pragma unroll
@@ -899,6 +934,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           const int rg = g < end ? range_of(si.pop, g) : -1;
           nb[k] = 8;
           a[k].bm = BM_NONE;
+          a[k].female = 0u;
           if (rg >= 0) {
             a[k].age = c_age[i]; a[k].his = c_his[i]; a[k].delay = c_delay[i]; a[k].sporo = c_sporo[i];
             a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
@@ -908,64 +944,40 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
             if (ns >= 0) nb[k] = ns;
           }
           const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
-          rk[k] = __popc(peers & lanemask_lt());
-          // survivors of this (round, warp) by state, 16 bits each: word j holds states 2j, 2j+1
-          const uint32_t one = nb[k] < 8 ? 1u << (16 * (nb[k] & 1)) : 0u;
-          const uint32_t wsel = (uint32_t)nb[k] >> 1;
-          const uint32_t c0 = __reduce_add_sync(0xffffffffu, wsel == 0 ? one : 0u);
-          const uint32_t c1 = __reduce_add_sync(0xffffffffu, wsel == 1 ? one : 0u);
-          const uint32_t c2 = __reduce_add_sync(0xffffffffu, wsel == 2 ? one : 0u);
-          const uint32_t c3 = __reduce_add_sync(0xffffffffu, wsel == 3 ? one : 0u);
-          if (lane == 0) s_cnt4[s][k * kWarps + warp] = make_uint4(c0, c1, c2, c3);
+          const uint32_t rk = __popc(peers & lanemask_lt());
+          const uint32_t* e0 = c_pre + (k * kWarps + warp) * kPreEntryWords;  // this chunk's entry
+          const uint32_t* e1 = e0 + kPreEntryWords;                         // the next one
+          const int b = nb[k];
+          dk[k] = 0xffffffffu;
+          if (b < 8) {
+            const uint32_t sh = 16 * (b & 1);
+            const uint32_t j = ((e0[b >> 1] >> sh) & 0xffffu) + rk;
+            // the two passes disagree when a survivor falls outside its chunk's run
+            if (j < ((e1[b >> 1] >> sh) & 0xffffu)) dk[k] = si.d0[b] + j;
+            else tilebad = 1;
+          }
+          // ... or when the chunk's survivors are not the count pass's
+          const uint32_t ns = __popc(__ballot_sync(0xffffffffu, b < 8));
+          if (ns != e1[4] - e0[4]) tilebad = 1;
+          nb[k] = (uint32_t)b | (a[k].female << 4) | (a[k].bm << 5);
         }
       }
       if (kind != TK_END) mbar_arrive(&empty[s]);  // this thread is done with the stage's inputs
-      // every (round, warp) count is in place; the barrier also agrees on a
-      // failed wait (then every consumer stops)
-      if (consumer_sync_or(!ok)) { fail = 1; fail_rep = cur_rep == 0xffffffffu ? 0u : cur_rep; break; }
+      if (!ok) { fail = 1; fail_rep = cur_rep == 0xffffffffu ? 0u : cur_rep; break; }
       if (kind == TK_END) break;
       const StepCtx& c = si.c;
       const DevPool& dst = si.dst;
       if (kind == TK_OLD) {
-        // ---- phase B: exclusive prefix of the 32 (round, warp) entries, by
-        //      every warp for its own entries (4 x 16-bit-packed scans) ----
-        const uint4 e = s_cnt4[s][lane];
-        uint32_t i0 = e.x, i1 = e.y, i2 = e.z, i3 = e.w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y0 = __shfl_up_sync(0xffffffffu, i0, o), y1 = __shfl_up_sync(0xffffffffu, i1, o);
-          const uint32_t y2 = __shfl_up_sync(0xffffffffu, i2, o), y3 = __shfl_up_sync(0xffffffffu, i3, o);
-          if (lane >= o) { i0 += y0; i1 += y1; i2 += y2; i3 += y3; }
-        }
-        {  // tile totals against the count pass
-          const uint32_t t0 = __shfl_sync(0xffffffffu, i0, 31), t1 = __shfl_sync(0xffffffffu, i1, 31);
-          const uint32_t t2 = __shfl_sync(0xffffffffu, i2, 31), t3 = __shfl_sync(0xffffffffu, i3, 31);
-          if (lane == 0 && warp == 0) {
-            const uint32_t tw[4] = {t0, t1, t2, t3};
-#pragma unroll
-            for (int b = 0; b < 8; b++)
-              if (((tw[b >> 1] >> (16 * (b & 1))) & 0xffffu) != si.cnt[b]) tilebad = 1;
-          }
-        }
-        const uint32_t x0 = i0 - e.x, x1 = i1 - e.y, x2 = i2 - e.z, x3 = i3 - e.w;
         BmEntry* bmq = s_bmq[warp];
         uint32_t nq = 0;
-        // ---- every survivor to its slot in the next buffer ----
+        // ---- phase B: every survivor to its slot in the next buffer ----
 #pragma unroll
         for (int k = 0; k < kItems; k++) {
-          const int ent = k * kWarps + warp;
-          const uint32_t p0 = __shfl_sync(0xffffffffu, x0, ent), p1 = __shfl_sync(0xffffffffu, x1, ent);
-          const uint32_t p2 = __shfl_sync(0xffffffffu, x2, ent), p3 = __shfl_sync(0xffffffffu, x3, ent);
-          const int b = nb[k];
-          uint32_t d = 0xffffffffu;
-          if (b < 8) {
-            const uint32_t pw = (b >> 1) == 0 ? p0 : (b >> 1) == 1 ? p1 : (b >> 1) == 2 ? p2 : p3;
-            const uint32_t j = ((pw >> (16 * (b & 1))) & 0xffffu) + rk[k];
-            if (j < si.cnt[b]) d = si.d0[b] + j;
-            else tilebad = 1;  // the two passes disagree: stay inside this state's run
-          }
+          const int b = (int)(nb[k] & 15u);
+          const uint32_t female = (nb[k] >> 4) & 1u;
+          const uint32_t d = dk[k];
           // queue this warp's owed draws; their column is written after the draw
-          const uint32_t owed = d != 0xffffffffu ? a[k].bm : BM_NONE;
+          const uint32_t owed = d != 0xffffffffu ? nb[k] >> 5 : BM_NONE;
           const uint32_t om = __ballot_sync(0xffffffffu, owed != BM_NONE);
           if (owed != BM_NONE) {
             BmEntry q;
@@ -976,7 +988,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           if (d != 0xffffffffu) {
             dst.age[d] = a[k].age; dst.his[d] = a[k].his; dst.sporo[d] = a[k].sporo; dst.uni[d] = a[k].uni;
             dst.cycle[d] = a[k].cycle; dst.hbc[d] = a[k].hbc; dst.batches[d] = a[k].batches;
-            dst.flags[d] = (uint8_t)(b | (a[k].female << 3));
+            dst.flags[d] = (uint8_t)(b | (female << 3));
             if (owed != BM_LARVA_DELAY) dst.delay[d] = a[k].delay;
             if (owed != BM_EGG_BATCH) dst.avail[d] = a[k].avail;
             // statistics of the next pool (kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37)
@@ -984,7 +996,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
               l1 += age_days_uncapped(a[k].age);
               const uint32_t dd = age_days(a[k].age);
               dmin = min(dmin, dd); dmax = max(dmax, dd);
-            } else if (b >= IMMATURE && a[k].female) {
+            } else if (b >= IMMATURE && female) {
               fem += 1u;
               inf += a[k].sporo >= 1.0f ? 1u : 0u;
             }
@@ -1019,7 +1031,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
       }
     }
     if (cur_rep != 0xffffffffu) flush(cur_rep);
-    if (fail && tid == 0) {
+    if (fail && lane == 0) {
       // let loads still in flight land before the CTA exits (bounded waits)
       for (int s = 0; s < 2; s++) (void)mbar_wait(&full[s], (ph >> s) & 1u);
     }

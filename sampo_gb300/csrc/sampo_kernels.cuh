@@ -65,10 +65,22 @@ struct BatchDev {
   uint32_t ticket2;           // scatter pass tile ticket
 };
 
+// The count pass's in-tile prefix table of one tile: for each (round, warp)
+// chunk of 32 slots (slot k * kBlock + tid is round k of warp tid / 32) and a
+// final entry for the whole tile, the survivors of the chunks before it by next
+// state (16-bit pairs: states 0-1, 2-3, 4-5, 6-7) and over all states.
+constexpr uint32_t kChunks = kItems * kWarps;
+constexpr uint32_t kPreEntryWords = 5;
+constexpr uint32_t kPreWords = ((kChunks + 1) * kPreEntryWords + 3) / 4 * 4;  // whole 16-byte units
+// Words per tile of a pool's tile arrays: prefix table, aggregates (8),
+// inclusive prefixes (8), epoch flag.
+constexpr uint32_t kTileArrayWords = kPreWords + 17;
+
 // Everything the kernels need of one replicate.
 struct RepParams {
   SimDev* sim;
   DevPool pool[2];
+  uint32_t* tilePre;          // [maxTiles][kPreWords] in-tile prefix tables (count pass)
   uint32_t* tileAgg;          // [maxTiles][8] per-tile survivor counts (count pass)
   uint32_t* tileIncl;         // [maxTiles][8] inclusive prefixes (scatter pass)
   uint32_t* tileFlag;         // [maxTiles] epoch when tileIncl is valid
@@ -107,6 +119,17 @@ inline void fill_constant_tables(ModelConst& h) {
 }
 
 // Initial device state of a simulation (before its pool is published).
+// The tile arrays of a pool of max_tiles tiles at base (16-byte aligned, for
+// the bulk copies of the prefix tables): [max_tiles][kPreWords] prefix tables,
+// then aggregates, inclusive prefixes and epoch flags.
+inline void set_tile_arrays(RepParams& r, uint32_t* base, uint32_t max_tiles) {
+  r.tilePre = base;
+  r.tileAgg = base + (size_t)max_tiles * kPreWords;
+  r.tileIncl = r.tileAgg + (size_t)max_tiles * 8;
+  r.tileFlag = r.tileAgg + (size_t)max_tiles * 16;
+  r.maxTiles = max_tiles;
+}
+
 inline SimDev initial_sim_state(uint32_t capacity, float cc) {
   SimDev h;
   memset(&h, 0, sizeof(h));

@@ -30,7 +30,7 @@ struct InputBlock {
 };
 
 struct Scratch {
-  uint32_t tiles[kMaxTiles * 17];  // survivor counts [8] | inclusive prefixes [8] | epoch flag, per tile
+  __align__(16) uint32_t tiles[kMaxTiles * kTileArrayWords];  // prefix tables | counts | inclusive prefixes | epoch flags
   SimDev sim;
   RepParams rep;
   BatchDev bat;
@@ -111,23 +111,20 @@ static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sam
   rp.sim = &sc->sim;
   rp.pool[0] = to_dev(in);
   rp.pool[1] = to_dev(out);
-  rp.tileAgg = sc->tiles;
-  rp.tileIncl = sc->tiles + (size_t)kMaxTiles * 8;
-  rp.tileFlag = sc->tiles + (size_t)kMaxTiles * 16;
+  set_tile_arrays(rp, sc->tiles, kMaxTiles);
   rp.T = sc->in.T;
   rp.env = sc->in.env;
   rp.seeds = sc->in.seeds;
   rp.wt = sc->in.wt;
   rp.rows = sc->rows;
   rp.ring = 2;
-  rp.maxTiles = kMaxTiles;
   if (cudaMemcpyAsync(&sc->sim, &h, sizeof(h), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(&sc->rep, &rp, sizeof(rp), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(&sc->bat, &bat, sizeof(bat), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(&sc->mc, &mc, sizeof(mc), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(&sc->in, &ib, sizeof(ib), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return SAMPO_ERR_CUDA;
-  if (ntiles && cudaMemsetAsync(sc->tiles + (size_t)kMaxTiles * 16, 0, (size_t)ntiles * 4, st) != cudaSuccess)
+  if (ntiles && cudaMemsetAsync(rp.tileFlag, 0, (size_t)ntiles * 4, st) != cudaSuccess)
     return SAMPO_ERR_CUDA;
 
   KParams p;

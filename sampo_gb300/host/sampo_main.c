@@ -22,11 +22,14 @@
  *   --age-days D    initial egg ages 24*U{0..D} hours (seeded by --age-seed)
  *   --age-seed A
  *   --per-step      one library call per step (the reference's host loop);
- *                   default: day graphs in chunks, rows printed per chunk
+ *                   default: day graphs in 30-day chunks; a printer thread
+ *                   formats chunk k from one pinned row buffer while the GPU
+ *                   runs chunk k + 1 into the other
  *   --device D      CUDA device
  * Only the built-in species (properties.h) is compiled in; another species
  * header is refused.
  */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -104,6 +107,60 @@ static void draw_seeds(sampo_seeds* s) { /* generateSeeds (src/abms.c:145-150) *
     s[i].z3 = (uint32_t)rand();
     s[i].z4 = (uint32_t)rand();
   }
+}
+
+/* The stats printer of the chunked mode: prints and checks the rows of one
+ * chunk at a time, in step order, on its own thread. */
+typedef struct {
+  pthread_mutex_t mu;
+  pthread_cond_t cv;
+  const sampo_stats_row* rows;  /* chunk handed over, or NULL when idle */
+  uint32_t first, n;
+  int quit;
+  const float* T;
+  uint64_t capacity;
+  sampo_population prev;        /* population of the last printed row */
+} printer_t;
+
+static void print_rows(printer_t* p, const sampo_stats_row* rows, uint32_t first, uint32_t n) {
+  for (uint32_t j = 0; j < n; j++) {
+    check_agents(print_stats(&rows[j], &p->prev, first + j, p->T[first + j]), p->capacity);
+    p->prev = rows[j].pop;
+  }
+}
+
+static void* printer_main(void* arg) {
+  printer_t* p = (printer_t*)arg;
+  pthread_mutex_lock(&p->mu);
+  for (;;) {
+    while (!p->rows && !p->quit) pthread_cond_wait(&p->cv, &p->mu);
+    if (!p->rows) break;
+    const sampo_stats_row* rows = p->rows;
+    const uint32_t first = p->first, n = p->n;
+    pthread_mutex_unlock(&p->mu);
+    print_rows(p, rows, first, n);
+    pthread_mutex_lock(&p->mu);
+    p->rows = NULL;
+    pthread_cond_broadcast(&p->cv);
+  }
+  pthread_mutex_unlock(&p->mu);
+  return NULL;
+}
+
+/* Waits until the printer has finished the chunk it holds. */
+static void printer_idle(printer_t* p) {
+  pthread_mutex_lock(&p->mu);
+  while (p->rows) pthread_cond_wait(&p->cv, &p->mu);
+  pthread_mutex_unlock(&p->mu);
+}
+
+static void printer_submit(printer_t* p, const sampo_stats_row* rows, uint32_t first, uint32_t n) {
+  pthread_mutex_lock(&p->mu);
+  p->rows = rows;
+  p->first = first;
+  p->n = n;
+  pthread_cond_broadcast(&p->cv);
+  pthread_mutex_unlock(&p->mu);
 }
 
 static void fail(sampo_sim* s, const char* what, int rc) {
@@ -193,18 +250,38 @@ int main(int argc, char** argv) {
     }
   } else {
     const uint32_t chunk = 24 * 30;
-    sampo_stats_row* rows = (sampo_stats_row*)sampo_host_alloc(sizeof(sampo_stats_row) * chunk);
-    if (!rows) return 1;
-    for (uint32_t first = 0; first < steps; first += chunk) {
+    sampo_stats_row* rows[2];
+    rows[0] = (sampo_stats_row*)sampo_host_alloc(sizeof(sampo_stats_row) * chunk);
+    rows[1] = (sampo_stats_row*)sampo_host_alloc(sizeof(sampo_stats_row) * chunk);
+    if (!rows[0] || !rows[1]) return 1;
+    printer_t pr;
+    memset(&pr, 0, sizeof(pr));
+    pthread_mutex_init(&pr.mu, NULL);
+    pthread_cond_init(&pr.cv, NULL);
+    pr.T = T;
+    pr.capacity = capacity;
+    pr.prev = prev;
+    pthread_t th;
+    if (pthread_create(&th, NULL, printer_main, &pr) != 0) return 1;
+    uint32_t k = 0;
+    for (uint32_t first = 0; first < steps; first += chunk, k ^= 1u) {
       const uint32_t n = steps - first < chunk ? steps - first : chunk;
-      rc = sampo_run(s, n, rows);
-      for (uint32_t j = 0; j < n && (rc == SAMPO_OK || j + 1 < n); j++) {
-        check_agents(print_stats(&rows[j], &prev, first + j, T[first + j]), capacity);
-        prev = rows[j].pop;
+      rc = sampo_run(s, n, rows[k]);  /* meanwhile the printer formats the other buffer */
+      printer_idle(&pr);
+      if (rc != SAMPO_OK) {
+        print_rows(&pr, rows[k], first, n - 1);  /* the rows before the failed step */
+        fail(s, "run", rc);
       }
-      if (rc != SAMPO_OK) fail(s, "run", rc);
+      printer_submit(&pr, rows[k], first, n);
     }
-    sampo_host_free(rows);
+    printer_idle(&pr);
+    pthread_mutex_lock(&pr.mu);
+    pr.quit = 1;
+    pthread_cond_broadcast(&pr.cv);
+    pthread_mutex_unlock(&pr.mu);
+    pthread_join(th, NULL);
+    sampo_host_free(rows[0]);
+    sampo_host_free(rows[1]);
   }
 
   sampo_population final;
