@@ -54,21 +54,10 @@ static_assert(kPreOff % 16 == 0 && kScatterStage % 16 == 0, "bulk copies land on
 constexpr uint32_t kWaitLimit = 1u << 22;                    // bounded mbarrier waits
 
 // ---------------- memory-model and TMA helpers ----------------
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ uint4 ld_cg_v4(const uint32_t* p) {
   uint4 v;
   asm volatile("ld.global.cg.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p) : "memory");
   return v;
-}
-__device__ __forceinline__ void st_cg_v4(uint32_t* p, uint4 v) {
-  asm volatile("st.global.cg.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
 }
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
@@ -470,7 +459,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
       // the tile's prefix table: exclusive prefix of the 32 (round, warp)
       // chunks, 16-bit packed, and the tile's totals (the update/scatter pass
       // reads both; the totals also feed the look-back)
-      const uint2 e = s_ent[lane];
+      const uint2 e = lane < kChunks ? s_ent[lane] : make_uint2(0u, 0u);
       uint32_t w[5], x[5];
       w[0] = (e.x & 0xffu) | ((e.x & 0xff00u) << 8);
       w[1] = ((e.x >> 16) & 0xffu) | ((e.x >> 8) & 0xff0000u);
@@ -488,16 +477,18 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
         }
       }
       uint32_t* pre = cs.tilePre + (size_t)cs.lt * kPreWords;
+      if (lane < kChunks) {
 #pragma unroll
-      for (int q = 0; q < 5; q++) pre[lane * kPreEntryWords + q] = x[q] - w[q];
-      if (lane == 31) {
+        for (int q = 0; q < 5; q++) pre[lane * kPreEntryWords + q] = x[q] - w[q];
+      }
+      if (lane == kChunks - 1) {
 #pragma unroll
         for (int q = 0; q < 5; q++) pre[kChunks * kPreEntryWords + q] = x[q];
       }
       uint32_t tw = 0;  // lanes 0..7: the tile's survivors of next state `lane`
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        const uint32_t t = __shfl_sync(0xffffffffu, x[q], 31);
+        const uint32_t t = __shfl_sync(0xffffffffu, x[q], kChunks - 1);
         if ((lane >> 1) == q) tw = (t >> (16 * (lane & 1))) & 0xffffu;
       }
       if (lane < 8) {
@@ -643,13 +634,23 @@ __device__ void issue_scatter_tile(const DevPool& src, const uint32_t* pre, uint
 
 // Decoupled look-back for tile t of one replicate by one warp over the count
 // pass's tile aggregates: sums earlier tiles' aggregates back to the nearest
-// published inclusive prefix (no waiting). Lane 0 publishes t's inclusive
-// prefix. Every lane returns the exclusive prefix ex[] and t's counts cnt[].
+// published inclusive prefix (no waiting). A published prefix is eight 64-bit
+// words, each holding a state's inclusive prefix and the step's epoch: every
+// word is written and read whole (single-copy atomic), so a reader validates
+// each by its epoch and no fence or flag is needed on either side. Lane 0
+// publishes t's words. Every lane returns the exclusive prefix ex[] and t's
+// counts cnt[].
 struct LookbackArrays {
-  uint32_t* agg;   // count pass tile aggregates
-  uint32_t* incl;  // inclusive prefixes
-  uint32_t* flag;  // epoch flags
+  uint32_t* agg;             // count pass tile aggregates
+  unsigned long long* incl;  // inclusive prefixes: value | epoch << 32
 };
+
+__device__ __forceinline__ void ld_relaxed_v2u64(const unsigned long long* p, unsigned long long& a, unsigned long long& b) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0,%1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_v2u64(unsigned long long* p, unsigned long long a, unsigned long long b) {
+  asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1,%2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
 
 __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epoch, int lane, uint32_t ex[8], uint32_t cnt[8]) {
 #pragma unroll
@@ -658,19 +659,30 @@ __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epo
   while (pos >= 0) {
     const int64_t idx = pos - lane;
     const bool valid = idx >= 0;
-    const uint32_t f = valid ? ld_acquire_u32(&rp.flag[idx]) : 0u;
-    const uint32_t m = __ballot_sync(0xffffffffu, !valid || f == epoch);
-    const int stop = m ? __ffs(m) - 1 : 32;
-    uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
-    if (valid && lane <= stop) {
-      const uint32_t* q = (lane == stop ? rp.incl : rp.agg) + (size_t)idx * 8;
-      v0 = ld_cg_v4(q);
-      v1 = ld_cg_v4(q + 4);
+    uint32_t v[8];
+    bool pub = false;
+#pragma unroll
+    for (int b = 0; b < 8; b++) v[b] = 0;
+    if (valid) {
+      const uint4 a0 = ld_cg_v4(rp.agg + (size_t)idx * 8), a1 = ld_cg_v4(rp.agg + (size_t)idx * 8 + 4);
+      unsigned long long w[8];
+#pragma unroll
+      for (int q = 0; q < 4; q++) ld_relaxed_v2u64(rp.incl + (size_t)idx * 8 + 2 * q, w[2 * q], w[2 * q + 1]);
+      pub = true;
+#pragma unroll
+      for (int b = 0; b < 8; b++) pub = pub && (uint32_t)(w[b] >> 32) == epoch;
+      const uint32_t ag[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+      for (int b = 0; b < 8; b++) v[b] = pub ? (uint32_t)w[b] : ag[b];
     }
-    ex[0] += __reduce_add_sync(0xffffffffu, v0.x); ex[1] += __reduce_add_sync(0xffffffffu, v0.y);
-    ex[2] += __reduce_add_sync(0xffffffffu, v0.z); ex[3] += __reduce_add_sync(0xffffffffu, v0.w);
-    ex[4] += __reduce_add_sync(0xffffffffu, v1.x); ex[5] += __reduce_add_sync(0xffffffffu, v1.y);
-    ex[6] += __reduce_add_sync(0xffffffffu, v1.z); ex[7] += __reduce_add_sync(0xffffffffu, v1.w);
+    const uint32_t m = __ballot_sync(0xffffffffu, !valid || pub);
+    const int stop = m ? __ffs(m) - 1 : 32;
+    if (lane > stop) {  // beyond the nearest published tile (or the first tile)
+#pragma unroll
+      for (int b = 0; b < 8; b++) v[b] = 0;
+    }
+#pragma unroll
+    for (int b = 0; b < 8; b++) ex[b] += __reduce_add_sync(0xffffffffu, v[b]);
     if (m) break;
     pos -= 32;
   }
@@ -678,9 +690,10 @@ __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epo
   const uint4 a0 = ld_cg_v4(ag), a1 = ld_cg_v4(ag + 4);
   cnt[0] = a0.x; cnt[1] = a0.y; cnt[2] = a0.z; cnt[3] = a0.w; cnt[4] = a1.x; cnt[5] = a1.y; cnt[6] = a1.z; cnt[7] = a1.w;
   if (lane == 0) {
-    st_cg_v4(rp.incl + (size_t)t * 8, make_uint4(ex[0] + a0.x, ex[1] + a0.y, ex[2] + a0.z, ex[3] + a0.w));
-    st_cg_v4(rp.incl + (size_t)t * 8 + 4, make_uint4(ex[4] + a1.x, ex[5] + a1.y, ex[6] + a1.z, ex[7] + a1.w));
-    st_release_u32(&rp.flag[t], epoch);
+    const unsigned long long e = (unsigned long long)epoch << 32;
+    unsigned long long* q = rp.incl + (size_t)t * 8;
+#pragma unroll
+    for (int b = 0; b < 8; b += 2) st_relaxed_v2u64(q + b, e | (ex[b] + cnt[b]), e | (ex[b + 1] + cnt[b + 1]));
   }
 }
 
@@ -692,7 +705,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one producer warp
-static_assert(kChunks == 32, "one (round, warp) chunk per lane");
+static_assert(kChunks <= 32, "one (round, warp) chunk per lane");
+constexpr int kScatterMinBlocks = kItems >= 4 ? 2 : 3;  // resident CTAs per SM the registers are sized for
 enum : uint32_t { TK_OLD = 0, TK_EGG = 1, TK_END = 2 };
 
 // What the producer warp hands the consumers with a tile. The replicate's
@@ -708,7 +722,11 @@ struct alignas(16) ScatterStage {
   uint32_t kind, lo;         // TK_*, first slot (old tile) or first egg id (egg tile)
   uint32_t d0[8], cnt[8];    // per next state: the tile's first slot in it, survivors
 };
-constexpr int kDescSlots = 4;  // tile descriptions: the producer describes three tiles ahead
+constexpr int kAhead = 3;                 // the producer describes tiles this far ahead of the consumers
+constexpr int kDescSlots = kAhead + 1;    // tile descriptions in flight
+// Each pass of the loop issues tile seq + 2; with kAhead >= 3 it was described
+// by an earlier pass, with kAhead == 2 the pass describes it first.
+static_assert(kAhead >= 2 && kDescSlots <= 16, "issue() needs tile seq + 2 described; 2 kind bits per slot");
 
 // A survivor's owed normal draw (include/gpuRand.h:56-63): its slot in the
 // next buffer, its slot in the current one (the generator's gid), its
@@ -725,7 +743,7 @@ struct BmEntry { uint32_t d, gid, batches, kind; };
 // has read its inputs, then writes every survivor straight to its slot in the
 // next buffer: the survivors of one next state are contiguous within a warp,
 // so the stores coalesce.
-__global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
+__global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ ScatterStage s_si[kDescSlots];
   __shared__ ModelConst s_mc;
@@ -764,9 +782,16 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     // describe tile `seq` (slot seq % kDescSlots): take a ticket, load the
     // replicate's data when the slot changes replicate, run the look-back,
     // lay out the tile's runs. Touches no stage.
+    // lane 0 draws each ticket one description ahead, so the atomic's round
+    // trip overlaps a tile
+    uint32_t t_next = 0;
+    if (lane == 0) t_next = atomicAdd(&p.bat->ticket2, 1u);
     auto describe = [&](uint32_t seq) -> uint32_t {
       uint32_t t = 0;
-      if (lane == 0) t = atomicAdd(&p.bat->ticket2, 1u);
+      if (lane == 0) {
+        t = t_next;
+        t_next = atomicAdd(&p.bat->ticket2, 1u);
+      }
       t = __shfl_sync(0xffffffffu, t, 0);
       ScatterStage& si = s_si[seq % kDescSlots];
       if (t >= total) {
@@ -791,7 +816,6 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
           si.dst = rp.pool[cur ^ 1u];
           si.lb.agg = rp.tileAgg;
           si.lb.incl = rp.tileIncl;
-          si.lb.flag = rp.tileFlag;
           si.pre = rp.tilePre;
           uint32_t tc[8], base[8];
           for (int k = 0; k < 8; k++) tc[k] = sim->cnt[k];
@@ -851,7 +875,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
     issue(0);
     set_kind(1, describe(1));
     issue(1);
-    set_kind(2, describe(2));
+    for (uint32_t seq = 2; seq < (uint32_t)kAhead; seq++) set_kind(seq, describe(seq));
     for (uint32_t seq = 0;; seq++) {
       const uint32_t s = seq & 1u;
       if (kind_of(seq) == TK_END) break;
@@ -860,10 +884,15 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_scatter(KParams p) {
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) { fail = 1; fail_rep = s_si[seq % kDescSlots].rep; break; }
       ph ^= 1u << s;
-      issue(seq + 2);
-      // slot (seq + 3) % 4 held tile seq - 1, whose consumers are done: they
-      // released tile seq's inputs after finishing it
-      set_kind(seq + 3, describe(seq + 3));
+      // slot (seq + kAhead) % kDescSlots held tile seq - 1, whose consumers
+      // are done: they released tile seq's inputs after finishing it
+      if (kAhead == 2) {
+        set_kind(seq + 2, describe(seq + 2));
+        issue(seq + 2);
+      } else {
+        issue(seq + 2);
+        set_kind(seq + kAhead, describe(seq + kAhead));
+      }
     }
   } else {
     // ================= consumer warps =================
@@ -1240,38 +1269,50 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
   if (max_c < 1) max_c = 1;
   if (max_s < 1) max_s = 1;
   const int sms = sm_count();
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaError_t e = cudaEventCreate(&e0);
-  if (e == cudaSuccess) e = cudaEventCreate(&e1);
-  double best = 1e30;
-  int bc = max_c, bs = max_s;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
+  // each kernel's time is taken on its own (the best count grid does not
+  // depend on the scatter grid), minimum over every trial that ran it; one
+  // untimed trial first
+  double tc[9], ts[9];
+  for (int i = 0; i < 9; i++) tc[i] = ts[i] = 1e30;
+  max_c = max_c > 8 ? 8 : max_c;
+  max_s = max_s > 8 ? 8 : max_s;
   const int reset_grid = (int)((p.nrep + 255) / 256);
   for (int c = 1; c <= max_c && e == cudaSuccess; c++) {
     for (int s = 1; s <= max_s && e == cudaSuccess; s++) {
-      double t = 1e30;
-      for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+      for (int rep = (c == 1 && s == 1) ? -1 : 0; rep < 3 && e == cudaSuccess; rep++) {
         k_trial_reset<<<reset_grid, 256, 0, st>>>(p);
-        if ((e = cudaEventRecord(e0, st)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) break;
         if ((e = launch_count(p, c * sms, st)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(ev[1], st)) != cudaSuccess) break;
         if ((e = launch_scatter(p, s * sms, st)) != cudaSuccess) break;
-        if ((e = cudaEventRecord(e1, st)) != cudaSuccess) break;
-        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < t) t = ms;
+        if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) break;
+        if ((e = cudaEventSynchronize(ev[2])) != cudaSuccess) break;
+        if (rep < 0) continue;
+        float m0 = 0, m1 = 0;
+        cudaEventElapsedTime(&m0, ev[0], ev[1]);
+        cudaEventElapsedTime(&m1, ev[1], ev[2]);
+        if (m0 < tc[c]) tc[c] = m0;
+        if (m1 < ts[s]) ts[s] = m1;
       }
-      if (t < best) { best = t; bc = c; bs = s; }
     }
   }
+  int bc = max_c, bs = max_s;
+  for (int c = 1; c <= max_c; c++)
+    if (tc[c] < tc[bc]) bc = c;
+  for (int s = 1; s <= max_s; s++)
+    if (ts[s] < ts[bs]) bs = s;
   if (e == cudaSuccess) {
     k_trial_reset<<<reset_grid, 256, 0, st>>>(p);
     e = cudaStreamSynchronize(st);
   }
-  if (e0) cudaEventDestroy(e0);
-  if (e1) cudaEventDestroy(e1);
+  for (int i = 0; i < 3; i++)
+    if (ev[i]) cudaEventDestroy(ev[i]);
   *grid_count = bc * sms;
   *grid_scatter = bs * sms;
-  if (best_ms) *best_ms = best;
+  if (best_ms) *best_ms = tc[bc] + ts[bs];
   return e;
 }
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {

@@ -73,8 +73,8 @@ constexpr uint32_t kChunks = kItems * kWarps;
 constexpr uint32_t kPreEntryWords = 5;
 constexpr uint32_t kPreWords = ((kChunks + 1) * kPreEntryWords + 3) / 4 * 4;  // whole 16-byte units
 // Words per tile of a pool's tile arrays: prefix table, aggregates (8),
-// inclusive prefixes (8), epoch flag.
-constexpr uint32_t kTileArrayWords = kPreWords + 17;
+// inclusive prefixes with their epochs (8 x 64 bits).
+constexpr uint32_t kTileArrayWords = kPreWords + 8 + 16;
 
 // Everything the kernels need of one replicate.
 struct RepParams {
@@ -82,8 +82,7 @@ struct RepParams {
   DevPool pool[2];
   uint32_t* tilePre;          // [maxTiles][kPreWords] in-tile prefix tables (count pass)
   uint32_t* tileAgg;          // [maxTiles][8] per-tile survivor counts (count pass)
-  uint32_t* tileIncl;         // [maxTiles][8] inclusive prefixes (scatter pass)
-  uint32_t* tileFlag;         // [maxTiles] epoch when tileIncl is valid
+  unsigned long long* tileIncl;  // [maxTiles][8] inclusive prefixes | epoch << 32 (scatter pass)
   const float* T;             // [ring] temperature per step
   const sampo_environment* env;  // [ring]
   sampo_seeds* seeds;         // [ring][4] (written by the device for a device seed stream)
@@ -121,12 +120,12 @@ inline void fill_constant_tables(ModelConst& h) {
 // Initial device state of a simulation (before its pool is published).
 // The tile arrays of a pool of max_tiles tiles at base (16-byte aligned, for
 // the bulk copies of the prefix tables): [max_tiles][kPreWords] prefix tables,
-// then aggregates, inclusive prefixes and epoch flags.
+// then aggregates and inclusive prefixes.
 inline void set_tile_arrays(RepParams& r, uint32_t* base, uint32_t max_tiles) {
+  static_assert(kPreWords % 4 == 0, "the inclusive prefixes start on a 16-byte boundary");
   r.tilePre = base;
   r.tileAgg = base + (size_t)max_tiles * kPreWords;
-  r.tileIncl = r.tileAgg + (size_t)max_tiles * 8;
-  r.tileFlag = r.tileAgg + (size_t)max_tiles * 16;
+  r.tileIncl = reinterpret_cast<unsigned long long*>(r.tileAgg + (size_t)max_tiles * 8);
   r.maxTiles = max_tiles;
 }
 

@@ -30,7 +30,7 @@ struct InputBlock {
 };
 
 struct Scratch {
-  __align__(16) uint32_t tiles[kMaxTiles * kTileArrayWords];  // prefix tables | counts | inclusive prefixes | epoch flags
+  __align__(16) uint32_t tiles[kMaxTiles * kTileArrayWords];  // prefix tables | counts | inclusive prefixes
   SimDev sim;
   RepParams rep;
   BatchDev bat;
@@ -104,8 +104,8 @@ static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sam
   for (int k = 0; k < 4; k++) ib.seeds[k] = seeds[k];
 
   // The array keeps the previous call's contents: reset the state, and clear
-  // the epoch flags of the tiles this step uses (a stale flag equal to this
-  // step's epoch would be taken for a published prefix).
+  // the inclusive prefixes of the tiles this step uses (a stale word carrying
+  // this step's epoch would be taken for a published prefix).
   const uint32_t ntiles = (pop_in->r[7].end + kTile - 1) / kTile;
   RepParams rp;
   rp.sim = &sc->sim;
@@ -124,7 +124,7 @@ static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sam
       cudaMemcpyAsync(&sc->mc, &mc, sizeof(mc), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(&sc->in, &ib, sizeof(ib), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return SAMPO_ERR_CUDA;
-  if (ntiles && cudaMemsetAsync(rp.tileFlag, 0, (size_t)ntiles * 4, st) != cudaSuccess)
+  if (ntiles && cudaMemsetAsync(rp.tileIncl, 0, (size_t)ntiles * 8 * sizeof(unsigned long long), st) != cudaSuccess)
     return SAMPO_ERR_CUDA;
 
   KParams p;

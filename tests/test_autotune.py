@@ -26,7 +26,7 @@ def test_autotune_leaves_the_run_unchanged(gpu_ready, tmp_path):
             rows = [sim.run(k)]
             if tune:
                 cc_, cs = sim.autotune()
-                assert 1 <= cc_ <= 8 and 1 <= cs <= 2
+                assert 1 <= cc_ <= 8 and 1 <= cs <= 4
             rows.append(sim.run(n - k))
             pop, arrays = sim.read_pool()
             out.append((np.concatenate(rows), pop, arrays, sim.histogram(), sim.device_status()))
