@@ -200,9 +200,15 @@ def gpu_arm(args, wl, rank, world, device):
             sim.run(24 * args.warmup, want_rows=False)
 
     # the autotuner picks the step kernels' grid sizes on the first timed day's
-    # state (it leaves the run unchanged); they stay for every phase below
+    # state (it leaves the run unchanged); they stay for every phase below.
+    # --ctas-per-sm fixes them instead (profiling runs, where timings under
+    # the profiler would mislead the tuner)
     fresh()
-    tuned = sim.autotune()
+    if args.ctas_per_sm:
+        tuned = tuple(int(x) for x in args.ctas_per_sm.split(","))
+        sim.set_grids(*tuned)
+    else:
+        tuned = sim.autotune()
     # ---- value: device-resident inputs, day graphs, L2 flushed between days ----
     fresh()
     sim.flush_l2()
@@ -493,6 +499,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plain-large", choices=list(WORKLOADS) + ["ensemble", "served"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ctas-per-sm", default="",
+                    help="COUNT,SCATTER: fixed grid sizes of the plain-path workloads instead of the autotuner")
     ap.add_argument("--replicates", type=int, default=512, help="ensemble: replicates")
     ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
     ap.add_argument("--rates", default="10,100,1000", help="served: arrival rates per second")
@@ -549,7 +557,8 @@ def main():
     cfg.update({"days_timed": args.steps, "live_agents_min": int(live_tot.min()), "live_agents_max": int(live_tot.max()),
                 "l2": "flushed between timed days (write of a buffer > 2x L2); pool bytes %.2e..%.2e" % (pool_bytes.min(), pool_bytes.max()),
                 "parallelism": f"replicas x{world}",
-                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1], "picked_by": "sampo_autotune"}})
+                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1],
+                                "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"}})
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,

@@ -163,6 +163,9 @@ int sampo_checkpoint_save(sampo_sim* s, const char* path);
  * fastest for the following steps and returns them. The trials leave the
  * simulation's course unchanged. Needs the coming step's inputs. */
 int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
+/* Sets the grid sizes sampo_autotune would pick, e.g. a choice tuned earlier
+ * on the same workload: 1 .. the occupancy limit of each pass. */
+int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
 int sampo_checkpoint_load(sampo_sim* s, const char* path);
 /* Sticky device status bits (SAMPO_DEV_*) since creation or the last clear. */
 int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear);
@@ -309,6 +312,7 @@ int sampo_batch_histogram(sampo_batch* b, uint32_t slot, uint32_t out[100]);
 int sampo_batch_read_pool(sampo_batch* b, uint32_t slot, sampo_population* pop, sampo_pool_view* v);
 /* The autotuner of sampo_autotune over the batch's coming step. */
 int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
+int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
 /* Device time of the last sampo_batch_run, in milliseconds (after sync). */
 int sampo_batch_last_run_ms(sampo_batch* b, double* ms);
 

@@ -131,6 +131,7 @@ SIGNATURES = {
                                      C.c_int, _P]),
     "sampo_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
     "sampo_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "sampo_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "sampo_batch_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
     "sampo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),
@@ -142,6 +143,7 @@ SIGNATURES = {
     "sampo_batch_set_inputs": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, C.c_uint32]),
     "sampo_batch_set_seeds": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32]),
     "sampo_batch_init_population": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_int, C.c_uint64]),
+    "sampo_batch_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "sampo_batch_seed_stream": (C.c_int, [_P, C.c_uint32, C.POINTER(RandState)]),
     "sampo_batch_seed_state": (C.c_int, [_P, C.c_uint32, C.POINTER(RandState), C.POINTER(C.c_uint32)]),
     "sampo_batch_run": (C.c_int, [_P, C.c_uint32, C.c_int]),

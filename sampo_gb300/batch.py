@@ -131,6 +131,10 @@ class Batch:
         self._check(self.lib.sampo_batch_autotune(self.h, C.byref(c), C.byref(s)))
         return c.value, s.value
 
+    def set_grids(self, count_ctas_per_sm: int, scatter_ctas_per_sm: int):
+        """sampo_batch_set_grids: fix the grid sizes without tuning."""
+        self._check(self.lib.sampo_batch_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))
+
     def last_run_ms(self) -> float:
         v = C.c_double()
         self._check(self.lib.sampo_batch_last_run_ms(self.h, C.byref(v)))

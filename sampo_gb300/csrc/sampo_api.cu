@@ -680,6 +680,28 @@ extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_
   return check_device(s);
 }
 
+extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm) {
+  if (!s) return SAMPO_ERR_ARG;
+  cudaSetDevice(s->device);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+  if (sms <= 0) sms = 1;
+  const uint32_t max_c = (uint32_t)(grid_blocks_count(1) / sms), max_s = (uint32_t)(grid_blocks_scatter(1) / sms);
+  if (count_ctas_per_sm < 1 || count_ctas_per_sm > max_c || scatter_ctas_per_sm < 1 || scatter_ctas_per_sm > max_s)
+    return fail(s, SAMPO_ERR_ARG, "CTAs per SM outside 1.." + std::to_string(max_c) + " (count) / 1.." + std::to_string(max_s) +
+                                      " (update/scatter)");
+  const int gc = (int)count_ctas_per_sm * sms, gs = (int)scatter_ctas_per_sm * sms;
+  if (gc != s->grid_count || gs != s->grid_scatter) {
+    s->grid_count = gc;
+    s->grid_scatter = gs;
+    if (s->day_graph) {  // captured with the old grids
+      cudaGraphExecDestroy(s->day_graph);
+      s->day_graph = nullptr;
+    }
+  }
+  return SAMPO_OK;
+}
+
 extern "C" int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear) {
   if (!s || !bits) return SAMPO_ERR_ARG;
   cudaSetDevice(s->device);

@@ -493,6 +493,29 @@ extern "C" int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm,
   return SAMPO_OK;
 }
 
+extern "C" int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm) {
+  if (!b) return SAMPO_ERR_ARG;
+  cudaSetDevice(b->device);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (sms <= 0) sms = 1;
+  const uint32_t max_c = (uint32_t)(grid_blocks_count(b->nslots) / sms);
+  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(b->nslots) / sms);
+  if (count_ctas_per_sm < 1 || count_ctas_per_sm > max_c || scatter_ctas_per_sm < 1 || scatter_ctas_per_sm > max_s)
+    return bfail(b, SAMPO_ERR_ARG, "CTAs per SM outside 1.." + std::to_string(max_c) + " (count) / 1.." +
+                                       std::to_string(max_s) + " (update/scatter)");
+  const int gc = (int)count_ctas_per_sm * sms, gs = (int)scatter_ctas_per_sm * sms;
+  if (gc != b->grid_count || gs != b->grid_scatter) {
+    b->grid_count = gc;
+    b->grid_scatter = gs;
+    if (b->day_graph) {
+      cudaGraphExecDestroy(b->day_graph);
+      b->day_graph = nullptr;
+    }
+  }
+  return SAMPO_OK;
+}
+
 extern "C" int sampo_batch_sync(sampo_batch* b) {
   if (!b) return SAMPO_ERR_ARG;
   cudaSetDevice(b->device);

@@ -346,11 +346,13 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
 
   // thread 0: take the next ticket into stage sidx and start its copies. The
   // ticket was drawn one claim earlier, so the atomic's round trip overlaps
-  // a tile's work.
+  // a tile's work. A step with no more tiles than CTAs gives CTA b tile b
+  // (no CTA queues a second tile while others have none).
+  const bool one_each = total <= gridDim.x;
   uint32_t t_next = 0;
   auto claim = [&](uint32_t sidx) {
     const uint32_t t = t_next;
-    t_next = atomicAdd(&p.bat->ticket1, 1u);
+    t_next = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket1, 1u);
     s_tick[sidx] = t;
     if (t >= total) return;
     const uint32_t r = find_rep(s_pre, p.nrep, t);
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     fence_mbar_init();
     s_cs[0].loaded = s_cs[1].loaded = 0xffffffffu;
     s_cs[0].rep = s_cs[1].rep = 0xffffffffu;
-    t_next = atomicAdd(&p.bat->ticket1, 1u);
+    t_next = one_each ? blockIdx.x : atomicAdd(&p.bat->ticket1, 1u);
     claim(0);
   }
   __syncthreads();
@@ -783,14 +785,16 @@ __global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(
     // replicate's data when the slot changes replicate, run the look-back,
     // lay out the tile's runs. Touches no stage.
     // lane 0 draws each ticket one description ahead, so the atomic's round
-    // trip overlaps a tile
+    // trip overlaps a tile; a step with no more tiles than CTAs gives CTA b
+    // tile b (no CTA queues several tiles while others have none)
+    const bool one_each = total <= gridDim.x;
     uint32_t t_next = 0;
-    if (lane == 0) t_next = atomicAdd(&p.bat->ticket2, 1u);
+    if (lane == 0) t_next = one_each ? blockIdx.x : atomicAdd(&p.bat->ticket2, 1u);
     auto describe = [&](uint32_t seq) -> uint32_t {
       uint32_t t = 0;
       if (lane == 0) {
         t = t_next;
-        t_next = atomicAdd(&p.bat->ticket2, 1u);
+        t_next = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket2, 1u);
       }
       t = __shfl_sync(0xffffffffu, t, 0);
       ScatterStage& si = s_si[seq % kDescSlots];

@@ -195,6 +195,10 @@ class Simulation:
         self._check(self.lib.sampo_autotune(self.h, C.byref(c), C.byref(s)))
         return c.value, s.value
 
+    def set_grids(self, count_ctas_per_sm: int, scatter_ctas_per_sm: int):
+        """Fix the grid sizes (CTAs per SM of the two passes) without tuning."""
+        self._check(self.lib.sampo_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))
+
     def checkpoint(self, path: str):
         """Save the simulation at the current step boundary."""
         self._check(self.lib.sampo_checkpoint_save(self.h, os.fsencode(path)))

@@ -50,3 +50,32 @@ def test_batch_autotune_leaves_replicates_unchanged(gpu_ready):
         b.run(48)
         for slot, spec in zip(slots, SPECS[:3]):
             compare(b, slot, spec, 72, f"replicate {spec.seed} tuned half-way")
+
+
+@pytest.mark.gpu
+def test_set_grids_pins_the_choice(gpu_ready, tmp_path):
+    """sampo_set_grids: any grid inside the occupancy limits gives the same run;
+    values outside them are refused."""
+    from sampo_gb300._lib import SampoError
+    from sampo_gb300 import inputs
+    from sampo_gb300.sim import Simulation, seed_stream
+    c = CASES["small_a"]
+    n = 96
+    tp, ep, _ = make_case_inputs("small_a", str(tmp_path))
+    T = inputs.read_temperature(tp, n)
+    env = inputs.read_environment(ep, n, c["cc"])
+    init, seeds = seed_stream(c["seed"], n)
+    out = []
+    for grids in (None, (1, 1), (3, 2)):
+        with Simulation(capacity=1 << 20, carrying_capacity=c["cc"], max_steps=n + 1) as sim:
+            sim.set_inputs(T, env)
+            sim.set_seeds(0, seeds)
+            sim.init_population(c["initial"], init, c["age_days"], c["age_seed"])
+            if grids:
+                sim.set_grids(*grids)
+            out.append(sim.run(n).tobytes())
+            with pytest.raises(SampoError):
+                sim.set_grids(0, 1)
+            with pytest.raises(SampoError):
+                sim.set_grids(1, 64)
+    assert out[1] == out[0] and out[2] == out[0]
