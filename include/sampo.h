@@ -32,6 +32,8 @@ extern "C" {
 #define SAMPO_ERR_STATE -5        /* call out of order (no population yet, inputs missing) */
 #define SAMPO_ERR_INTERNAL -6     /* a device-side consistency check failed */
 #define SAMPO_ERR_IO -7           /* input file missing or short */
+#define SAMPO_ERR_SPECIES -8      /* the species header did not compile (see the log) */
+#define SAMPO_ERR_UNSUPPORTED -9  /* NVRTC or the CUDA driver entry points are unavailable */
 
 /* ---- device error bits (sampo_device_status) ---- */
 #define SAMPO_DEV_ERR_CAPACITY   0x1u
@@ -167,6 +169,29 @@ int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_
  * on the same workload: 1 .. the occupancy limit of each pass. */
 int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
 int sampo_checkpoint_load(sampo_sim* s, const char* path);
+/* ---- species headers compiled at run time ----
+ * The reference compiles its kernels at start-up with the species header
+ * named by argv[3] (src/abms.c:565-568; default properties.h, which is built
+ * into this library). sampo_species_compile compiles the step kernels with
+ * NVRTC against a properties.h-style header (OpenCL C: the functions
+ * eggsIncubation ... layEggs and the *_PROBABILITY macros of
+ * include/properties.h, with include/gpuRand.h's HybridTaus and BoxMuller
+ * and OpenCL math) for the given device; log (may be NULL) receives the
+ * compiler's messages. A simulation or batch uses it after
+ * sampo_set_species / sampo_batch_set_species (set it before
+ * sampo_init_population: the initial eggs use the species too); NULL
+ * returns to the built-in species. Free it after the handles that use it.
+ * sampo_step_noalloc always uses the built-in species. */
+typedef struct sampo_species sampo_species;
+int sampo_species_compile(const char* header_path, int device, char* log, size_t log_size, sampo_species** out);
+int sampo_species_compile_text(const char* name, const char* text, int device, char* log, size_t log_size,
+                               sampo_species** out);
+void sampo_species_free(sampo_species* sp);
+/* Compiles without loading, for sm_<sm>a (e.g. 103): a syntax check that
+ * needs no GPU. */
+int sampo_species_check_text(const char* name, const char* text, int sm, char* log, size_t log_size);
+int sampo_set_species(sampo_sim* s, const sampo_species* sp);
+
 /* Sticky device status bits (SAMPO_DEV_*) since creation or the last clear. */
 int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear);
 
@@ -313,6 +338,9 @@ int sampo_batch_read_pool(sampo_batch* b, uint32_t slot, sampo_population* pop, 
 /* The autotuner of sampo_autotune over the batch's coming step. */
 int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
 int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
+/* The species of every replicate of the batch (NULL: built in); as
+ * sampo_set_species. */
+int sampo_batch_set_species(sampo_batch* b, const sampo_species* sp);
 /* Device time of the last sampo_batch_run, in milliseconds (after sync). */
 int sampo_batch_last_run_ms(sampo_batch* b, double* ms);
 

@@ -159,10 +159,15 @@ void icl_release_buffers(cl_uint num, ...) {
   va_end(ap);
 }
 
+// the species header the kernel objects were compiled with (-DSPECIES)
+#ifndef REF_SPECIES_NAME
+#define REF_SPECIES_NAME "properties.h"
+#endif
+
 struct EKernel { std::string name; };
 
 icl_kernel* icl_create_kernel(icl_device* dev, const char* file, const char* name, const char* opts, icl_create_kernel_flag) {
-  if (opts && !strstr(opts, "SPECIES=properties.h")) {
+  if (opts && !strstr(opts, "SPECIES=" REF_SPECIES_NAME)) {
     fprintf(stderr, "icl_emul: only the shipped species header is compiled in (%s)\n", opts);
     exit(-1);
   }

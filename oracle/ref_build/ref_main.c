@@ -8,7 +8,10 @@
  * the emulator (icl_emul.cpp).
  *
  *   sampo_ref [--seed S] [--initial N] [--cc CC] [--steps K]
- *             [--age-days D --age-seed A] [--hash-file F] TEMP ENV
+ *             [--age-days D --age-seed A] [--hash-file F] TEMP ENV [SPECIES]
+ *
+ * SPECIES is passed on as abms.c's argv[3]; the kernels were compiled with
+ * the species header at build time (ref_build/Makefile, target species).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -24,7 +27,7 @@ extern const char* sampo_ref_hash_file;
 int abms_main(int argc, char** argv);
 
 int main(int argc, char** argv) {
-  char* pos[3] = {argv[0], NULL, NULL};
+  char* pos[4] = {argv[0], NULL, NULL, NULL};
   int np = 1;
   for (int i = 1; i < argc; i++) {
     if (!strcmp(argv[i], "--seed") && i + 1 < argc) sampo_ref_seed = (unsigned)strtoul(argv[++i], 0, 10);
@@ -34,9 +37,9 @@ int main(int argc, char** argv) {
     else if (!strcmp(argv[i], "--age-days") && i + 1 < argc) sampo_ref_age_days = atoi(argv[++i]);
     else if (!strcmp(argv[i], "--age-seed") && i + 1 < argc) sampo_ref_age_seed = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--hash-file") && i + 1 < argc) sampo_ref_hash_file = argv[++i];
-    else if (np < 3) pos[np++] = argv[i];
+    else if (np < 4) pos[np++] = argv[i];
     else { fprintf(stderr, "sampo_ref: unexpected argument %s\n", argv[i]); return 2; }
   }
-  if (np != 3) { fprintf(stderr, "usage: sampo_ref [options] TEMP ENV\n"); return 2; }
-  return abms_main(3, pos);
+  if (np < 3) { fprintf(stderr, "usage: sampo_ref [options] TEMP ENV [SPECIES]\n"); return 2; }
+  return abms_main(np, pos);
 }

@@ -16,7 +16,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libsampo_cuda.so")
 
 OK = 0
 ERR_NAMES = {-1: "SAMPO_ERR_ARG", -2: "SAMPO_ERR_CUDA", -3: "SAMPO_ERR_CAPACITY", -4: "SAMPO_ERR_TEMPERATURE",
-             -5: "SAMPO_ERR_STATE", -6: "SAMPO_ERR_INTERNAL", -7: "SAMPO_ERR_IO"}
+             -5: "SAMPO_ERR_STATE", -6: "SAMPO_ERR_INTERNAL", -7: "SAMPO_ERR_IO", -8: "SAMPO_ERR_SPECIES",
+             -9: "SAMPO_ERR_UNSUPPORTED"}
 DEV_ERR_CAPACITY, DEV_ERR_DEVRATES, DEV_ERR_TILECOUNT, DEV_ERR_LARVATABLE = 0x1, 0x2, 0x4, 0x8
 DEV_WARN_REF_LAYOUT = 0x100
 STATE_NAMES = ("EGG", "LARVA", "PUPA", "IMMATURE", "MATESEEKING", "BMS", "BMD", "GRAVID")
@@ -132,6 +133,12 @@ SIGNATURES = {
     "sampo_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
     "sampo_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "sampo_species_compile": (C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(_P)]),
+    "sampo_species_compile_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(_P)]),
+    "sampo_species_check_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_size_t]),
+    "sampo_species_free": (None, [_P]),
+    "sampo_set_species": (C.c_int, [_P, _P]),
+    "sampo_batch_set_species": (C.c_int, [_P, _P]),
     "sampo_batch_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_checkpoint_load": (C.c_int, [_P, C.c_char_p]),
     "sampo_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.POINTER(_P)]),

@@ -131,6 +131,11 @@ class Batch:
         self._check(self.lib.sampo_batch_autotune(self.h, C.byref(c), C.byref(s)))
         return c.value, s.value
 
+    def set_species(self, species):
+        """sampo_batch_set_species: every replicate uses this species (None: built in)."""
+        self._check(self.lib.sampo_batch_set_species(self.h, species.h if species is not None else None))
+        self._species = species
+
     def set_grids(self, count_ctas_per_sm: int, scatter_ctas_per_sm: int):
         """sampo_batch_set_grids: fix the grid sizes without tuning."""
         self._check(self.lib.sampo_batch_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))

@@ -18,6 +18,7 @@ using namespace sampo;
 
 struct sampo_sim {
   int device = 0;
+  const void* species = nullptr;     // kernels compiled for a user species, or null (built in)
   cudaStream_t stream = nullptr;
   uint64_t capacity = 0;
   uint32_t ring = 0;
@@ -95,6 +96,7 @@ static KParams make_params(sampo_sim* s) {
   p.nrep = 1;
   p.bat = s->bat_dev;
   p.mc = s->mc_dev;
+  p.ks = s->species;
   return p;
 }
 
@@ -680,13 +682,28 @@ extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_
   return check_device(s);
 }
 
+extern "C" int sampo_set_species(sampo_sim* s, const sampo_species* sp) {
+  if (!s) return SAMPO_ERR_ARG;
+  cudaSetDevice(s->device);
+  if (s->species == sp) return SAMPO_OK;
+  s->species = sp;
+  s->grid_count = grid_blocks_count(1, sp);
+  s->grid_scatter = grid_blocks_scatter(1, sp);
+  if (s->day_graph) {  // captured with the other kernels
+    cudaGraphExecDestroy(s->day_graph);
+    s->day_graph = nullptr;
+  }
+  return SAMPO_OK;
+}
+
 extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm) {
   if (!s) return SAMPO_ERR_ARG;
   cudaSetDevice(s->device);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
   if (sms <= 0) sms = 1;
-  const uint32_t max_c = (uint32_t)(grid_blocks_count(1) / sms), max_s = (uint32_t)(grid_blocks_scatter(1) / sms);
+  const uint32_t max_c = (uint32_t)(grid_blocks_count(1, s->species) / sms);
+  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(1, s->species) / sms);
   if (count_ctas_per_sm < 1 || count_ctas_per_sm > max_c || scatter_ctas_per_sm < 1 || scatter_ctas_per_sm > max_s)
     return fail(s, SAMPO_ERR_ARG, "CTAs per SM outside 1.." + std::to_string(max_c) + " (count) / 1.." + std::to_string(max_s) +
                                       " (update/scatter)");

@@ -62,6 +62,7 @@ struct Replicate {
 
 struct sampo_batch {
   int device = 0;
+  const void* species = nullptr;     // kernels compiled for a user species, or null (built in)
   cudaStream_t stream = nullptr;
   cudaMemPool_t mempool = nullptr;
   uint32_t nslots = 0, ring = 0;
@@ -96,6 +97,7 @@ static KParams all_params(sampo_batch* b) {
   p.nrep = b->nslots;
   p.bat = b->bat_dev;
   p.mc = b->mc_dev;
+  p.ks = b->species;
   return p;
 }
 static KParams slot_params(sampo_batch* b, uint32_t slot) {
@@ -493,14 +495,28 @@ extern "C" int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm,
   return SAMPO_OK;
 }
 
+extern "C" int sampo_batch_set_species(sampo_batch* b, const sampo_species* sp) {
+  if (!b) return SAMPO_ERR_ARG;
+  cudaSetDevice(b->device);
+  if (b->species == sp) return SAMPO_OK;
+  b->species = sp;
+  b->grid_count = grid_blocks_count(b->nslots, sp);
+  b->grid_scatter = grid_blocks_scatter(b->nslots, sp);
+  if (b->day_graph) {
+    cudaGraphExecDestroy(b->day_graph);
+    b->day_graph = nullptr;
+  }
+  return SAMPO_OK;
+}
+
 extern "C" int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm) {
   if (!b) return SAMPO_ERR_ARG;
   cudaSetDevice(b->device);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   if (sms <= 0) sms = 1;
-  const uint32_t max_c = (uint32_t)(grid_blocks_count(b->nslots) / sms);
-  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(b->nslots) / sms);
+  const uint32_t max_c = (uint32_t)(grid_blocks_count(b->nslots, b->species) / sms);
+  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(b->nslots, b->species) / sms);
   if (count_ctas_per_sm < 1 || count_ctas_per_sm > max_c || scatter_ctas_per_sm < 1 || scatter_ctas_per_sm > max_s)
     return bfail(b, SAMPO_ERR_ARG, "CTAs per SM outside 1.." + std::to_string(max_c) + " (count) / 1.." +
                                        std::to_string(max_s) + " (update/scatter)");

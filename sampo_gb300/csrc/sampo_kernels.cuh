@@ -7,7 +7,9 @@
 // of one.
 #pragma once
 #include <stdint.h>
+#ifndef __CUDACC_RTC__
 #include <string.h>
+#endif
 #include "../../include/sampo.h"
 #include "sampo_math.h"
 #include "sampo_model.cuh"
@@ -97,7 +99,16 @@ struct KParams {
   uint32_t nrep;
   BatchDev* bat;
   const ModelConst* mc;
+  const void* ks;             // host: the kernels compiled for a user species (sampo_species.cu), or null
 };
+
+// Modes of k_publish: PUB_AFTER_STEP turns the step's counts into the next
+// pool's start; PUB_INITIAL publishes the current pool (after init/load);
+// PUB_REFRESH recomputes the coming step's input-dependent constants (run it
+// after writing that step's inputs).
+enum : int { PUB_INITIAL = 0, PUB_AFTER_STEP = 1, PUB_REFRESH = 2 };
+
+#ifndef __CUDACC_RTC__  // host side (the run-time compiler sees the device part only)
 
 // Hourly mortality tables that do not change during a run
 // (kernel/killAgents.cl:84-115,135-147), computed on the host with the same
@@ -142,17 +153,22 @@ inline SimDev initial_sim_state(uint32_t capacity, float cc) {
 }
 
 // Launch helpers (sampo_kernels.cu). The step kernels take every replicate of
-// p; init, pool statistics and the histogram take p.reps[0] only.
+// p; init, pool statistics and the histogram take p.reps[0] only. They launch
+// the built-in kernels, or p.ks's when a species was compiled at run time.
 // persistent grid sizes (CTAs resident on all SMs) for batches of nrep replicates
-int grid_blocks_count(uint32_t nrep);
-int grid_blocks_scatter(uint32_t nrep);
+int grid_blocks_count(uint32_t nrep, const void* ks = nullptr);
+int grid_blocks_scatter(uint32_t nrep, const void* ks = nullptr);
+// The kernels of a run-time species (sampo_species.cu): launch one, and its
+// resident CTAs per SM.
+enum : int { KID_COUNT, KID_SCATTER, KID_PUBLISH, KID_INIT_EGGS, KID_POOL_STATS, KID_HISTOGRAM, KID_TRIAL_RESET, KID_N };
+cudaError_t species_launch(const void* ks, int kid, dim3 grid, dim3 block, size_t smem, cudaStream_t st, void** args);
+int species_occupancy(const void* ks, int kid, int threads, size_t smem);
+// dynamic shared memory the persistent kernels may request
+size_t count_smem_max();
+size_t scatter_smem_max();
 cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st);
 cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st);
-// k_publish over every replicate of p: PUB_AFTER_STEP turns the step's counts
-// into the next pool's start; PUB_INITIAL publishes the current pool (after
-// init/load); PUB_REFRESH recomputes the coming step's input-dependent
-// constants (run it after writing that step's inputs).
-enum : int { PUB_INITIAL = 0, PUB_AFTER_STEP = 1, PUB_REFRESH = 2 };
+// k_publish over every replicate of p (modes PUB_*, above).
 cudaError_t launch_publish(const KParams& p, int mode, cudaStream_t st);
 cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev,
                              int age_days_max, uint64_t age_seed, cudaStream_t st);
@@ -165,5 +181,7 @@ cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out,
 // trials leave the simulations' course unchanged (k_trial_reset); the coming
 // step's constants must be current (PUB_REFRESH) before the call.
 cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, double* best_ms);
+
+#endif  // __CUDACC_RTC__
 
 }  // namespace sampo

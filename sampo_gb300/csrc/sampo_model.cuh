@@ -2,7 +2,8 @@
 //
 // One hourly step of one agent: killAgents (kernel/killAgents.cl:24-148)
 // followed by updateAgents (kernel/updateAgents.cl:39-270) with the species
-// functions of include/properties.h and the generator of include/gpuRand.h.
+// functions of sampo_species.cuh (include/properties.h, or a user's header
+// compiled in at run time) and the generator of include/gpuRand.h.
 // Float expressions are written in the reference's operation order and the
 // file is compiled with --fmad=false, so every product and sum rounds exactly
 // as the reference's C semantics say; the two places where the reference
@@ -71,6 +72,8 @@ struct alignas(16) StepCtx {
   float eggIncubation;         // eggsIncubation(T)
   float larvaDev;              // larvaDevelopment(T)
   float pupaDelay, immatureDelay, bmdDelay;
+  float mateDelay, bmsDelay;   // mateSeekingDelay(T), bloodMealSeekingDelay(T)
+  uint32_t tt;                 // transition-time bits of the hour (TT_*, sampo_species.cuh)
   double sporoInc;             // 1/((111/(T-16))*14) in double, used when T > 16 and bitten
   float sporoH, sporoM, sporoL;  // sporoInc = sporoH + sporoM + sporoL exactly
   uint32_t sporoOn;            // T > 16
@@ -119,32 +122,31 @@ __device__ __forceinline__ float trunc_sat_fast(float x) {
   return r > x ? __fadd_rn(r, -1.0f) : r;
 }
 
-__device__ __forceinline__ float rng(const StepCtx& c, int slot, uint32_t gid) {
-  uint32_t v = c.rng_c13[slot] ^ taus_step(c.rng_z2[slot] + gid, 2, 25, 4, 4294967288u) ^
-               (1664525u * (c.rng_z4[slot] * gid) + 1013904223u);
+// HybridTaus of one seed slot whose z1 and z3 parts are folded into c13.
+__device__ __forceinline__ float rng_folded(uint32_t c13, uint32_t z2, uint32_t z4, uint32_t gid) {
+  uint32_t v = c13 ^ taus_step(z2 + gid, 2, 25, 4, 4294967288u) ^ (1664525u * (z4 * gid) + 1013904223u);
   return 2.3283064365387e-10f * u32_to_f32_rn(v);  // (float)v * 2^-32
 }
+__device__ __forceinline__ float rng(const StepCtx& c, int slot, uint32_t gid) {
+  return rng_folded(c.rng_c13[slot], c.rng_z2[slot], c.rng_z4[slot], gid);
+}
 
-// BoxMuller(seeds+1, ...) (include/gpuRand.h:56-63): u0 from slot 1, u1 from slot 2.
-__device__ __forceinline__ float box_muller(const StepCtx& c, uint32_t gid, float mean, float sd) {
-  float u0 = rng(c, 1, gid), u1 = rng(c, 2, gid);
+// BoxMuller (include/gpuRand.h:56-63) of two uniform draws.
+__device__ __forceinline__ float box_muller_u(float u0, float u1, float mean, float sd) {
   float r = __fsqrt_rn(-2.0f * sampo_logf_bm(u0));
   float theta = (2.0f * 3.14159274101257f) * u1;
   return (r * sampo_sinf_bm(theta)) * sd + mean;
 }
-
-// eggsHatching (include/properties.h:39-60)
-__device__ __forceinline__ float eggs_hatching(float p) {
-  float m, b;
-  if (p < 0.5f) { m = 48.0f; b = 0.0f; }
-  else if (p < 0.85f) { m = 68.5714f; b = -10.2857f; }
-  else if (p < 0.90f) { m = 480.0f; b = -360.0f; }
-  else if (p < 0.94f) { m = 600.00f; b = -468.0f; }
-  else { m = 2400.0f; b = -2160.0f; }
-  return trunc_sat_fast(m * p + b + 0.5f);
+// BoxMuller(seeds+1, ...): u0 from slot 1, u1 from slot 2.
+__device__ __forceinline__ float box_muller(const StepCtx& c, uint32_t gid, float mean, float sd) {
+  return box_muller_u(rng(c, 1, gid), rng(c, 2, gid), mean, sd);
 }
 
-__host__ __device__ __forceinline__ bool night(uint32_t wt) { return wt <= 6u || wt >= 18u; }
+}  // namespace sampo
+
+#include "sampo_species.cuh"
+
+namespace sampo {
 
 __device__ __forceinline__ uint32_t age_days(float age) {
   return f32_to_u32_small(sampo_fminf(age / 24.0f, 99.0f));  // kernel/killAgents.cl:55
@@ -179,10 +181,14 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& m
     a.sporo = sampo_sporo_add(a.sporo, c.sporoH, c.sporoM, c.sporoL, c.sporoInc);
   switch (rg) {
     case EGG:
-      if (a.his >= a.delay) {
+      if (a.his >= a.delay && (c.tt & TT_EGG)) {
         if (FULL) {
           a.age = 24.0f; a.his = 0.0f;
+#ifdef SAMPO_USER_SPECIES
+          a.delay = species_larva_delay(c, gid);
+#else
           a.bm = BM_LARVA_DELAY;  // delay = larvaDelay (include/properties.h:87-91), owed
+#endif
         }
         return LARVA;
       }
@@ -193,59 +199,65 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& m
       }
       float cld = __uint_as_float(a.uni) + c.larvaDev;
       if (FULL) a.uni = __float_as_uint(cld);
-      if (cld >= a.delay && night(c.wt)) {
+      if (cld >= a.delay && (c.tt & TT_LARVA)) {
         if (FULL) { a.his = 0.0f; a.delay = c.pupaDelay; }
         return PUPA;
       }
       return LARVA;
     }
     case PUPA:
-      if (a.his >= a.delay && night(c.wt)) {
+      if (a.his >= a.delay && (c.tt & TT_PUPA)) {
         if (FULL) { a.age = 0.0f; a.his = 0.0f; a.delay = c.immatureDelay; }
         return IMMATURE;
       }
       return PUPA;
     case IMMATURE:
-      if (a.his >= a.delay) {
-        if (FULL) { a.delay = 1.0f; a.his = 0.0f; }  // mateSeekingDelay
+      if (a.his >= a.delay && (c.tt & TT_IMMATURE)) {
+        if (FULL) { a.delay = c.mateDelay; a.his = 0.0f; }
         return MATESEEKING;
       }
       return IMMATURE;
     case MATESEEKING:
-      if (a.his >= a.delay && a.female && c.wt == 18u) {
-        if (FULL) { a.his = 0.0f; a.delay = 0.0f; }   // bloodMealSeekingDelay
+      if (a.his >= a.delay && a.female && (c.tt & TT_MATESEEKING)) {
+        if (FULL) { a.his = 0.0f; a.delay = c.bmsDelay; }
         return BMS;
       }
       return MATESEEKING;
     case BMS:
       if (FULL) a.cycle += 1u;
-      if (a.his >= a.delay && night(c.wt)) {
+      if (a.his >= a.delay && (c.tt & TT_BMS)) {
         if (rng(c, 1, gid) <= c.env.bloodmealSuccess) {
-          if (c.env.ITNValue * 1.0f * 1.0f > 0.0f) {
-            if (rng(c, 2, gid) <= c.env.ITNValue * 1.0f * 1.0f) return -1;
+          if (c.env.ITNValue * SAMPO_BITE_HUMAN * SAMPO_BITE_INDOOR > 0.0f) {
+            if (rng(c, 2, gid) <= c.env.ITNValue * SAMPO_BITE_HUMAN * SAMPO_BITE_INDOOR) return -1;
           }
           if (FULL) {
-            a.hbc += 1u;
+            // bitesAhuman (kernel/updateAgents.cl:175)
+            const uint32_t bites = SAMPO_BITE_HUMAN < 1.0f ? (rng(c, 3, gid) <= SAMPO_BITE_HUMAN ? 1u : 0u) : 1u;
+            a.hbc += bites;
             acc.bites += 1u;
             a.his = 0.0f; a.delay = c.bmdDelay;
-            if (a.sporo >= 1.0f) acc.infectBites += 1u;
+            if (a.sporo >= 1.0f && bites) acc.infectBites += 1u;
           }
           return BMD;
         }
       }
       return BMS;
     case BMD:
-      if (c.env.IRSValue * 1.0f > 0.0f) {
-        if (rng(c, 2, gid) <= c.env.IRSValue * 1.0f) return -1;
+      if (c.env.IRSValue * SAMPO_REST_INDOOR > 0.0f) {
+        if (rng(c, 2, gid) <= c.env.IRSValue * SAMPO_REST_INDOOR) return -1;
       }
       if (FULL) a.cycle += 1u;
-      if (a.his >= a.delay) {
+      if (a.his >= a.delay && (c.tt & TT_BMD)) {
         if (FULL) {
           if (a.avail <= 0u && a.female) {
+#ifdef SAMPO_USER_SPECIES
+            a.avail = species_generate_eggs(c, gid, a.batches);
+#else
             // generateEggs (include/properties.h:257-266): the batch size is
             // owed; numEggBatches is incremented now, the draw uses the old value
             a.batches += 1u;
             a.bm = BM_EGG_BATCH;
+#endif
           }
           a.his = 0.0f; a.uni = 0u;
         }
@@ -254,7 +266,7 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& m
       return BMD;
     default: {  // GRAVID
       if (FULL) a.cycle += 1u;
-      if (night(c.wt)) {
+      if (c.tt & TT_LAY) {
         if (rng(c, 1, gid) < 0.25f) {
           uint32_t avail = a.avail;
           bool trapped = false;
@@ -262,18 +274,24 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& m
             if (rng(c, 2, gid) <= c.env.oviTrapValue) { trapped = true; avail = 0u; }
           }
           if (!trapped) {
+#ifdef SAMPO_USER_SPECIES
+            uint32_t pe = 0;
+            avail = species_lay_eggs(c, gid, a, avail, pe);
+            if (!FULL) acc.newEggs += pe;
+#else
             // layEggs (include/properties.h:296-307)
             float nbm = u32_to_f32_rn(c.totalBiomass) / ((u32_to_f32_rn(a.uni) + 1.0f) * c.env.carryingCapacity);
             float pbm = sampo_fmaxf(0.0f, 1.0f - nbm);
             uint32_t pe = f2u_sat_fast(ceilf(u32_to_f32_rn(avail) * pbm));
             if (!FULL) acc.newEggs += pe;
             avail = avail - pe;
+#endif
           }
           if (FULL) { a.uni += 1u; a.avail = avail; }
           if (avail == 0u) {
             if (FULL) {
               acc.cycles += 1u; acc.sumCycles += a.cycle;
-              a.cycle = 0u; a.his = 0.0f; a.delay = 0.0f;
+              a.cycle = 0u; a.his = 0.0f; a.delay = c.bmsDelay;
             }
             if (trapped) return -1;
             return BMS;
@@ -303,7 +321,7 @@ __device__ __forceinline__ void new_egg(const StepCtx& c, uint32_t id, Rec& a) {
   a.female = rng(c, 3, id) <= 0.5f ? 1u : 0u;
   a.sporo = 0.0f;
   a.hbc = 0u; a.avail = 0u; a.cycle = 0u; a.uni = 0u;
-  a.delay = c.eggIncubation + eggs_hatching(rng(c, 2, id));
+  a.delay = c.eggIncubation + species_eggs_hatching(rng(c, 2, id));
   a.batches = 0u;
 }
 

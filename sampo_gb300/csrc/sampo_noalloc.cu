@@ -132,6 +132,7 @@ static int run_step(const sampo_device_pool* in, uint32_t in_capacity, const sam
   p.nrep = 1;
   p.bat = &sc->bat;
   p.mc = &sc->mc;
+  p.ks = nullptr;  // the built-in species
   if (launch_publish_start(p, st) != cudaSuccess) return SAMPO_ERR_CUDA;
   if (launch_count(p, grid_blocks_count(1), st) != cudaSuccess) return SAMPO_ERR_CUDA;
   if (launch_scatter(p, grid_blocks_scatter(1), st) != cudaSuccess) return SAMPO_ERR_CUDA;

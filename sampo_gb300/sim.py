@@ -195,6 +195,12 @@ class Simulation:
         self._check(self.lib.sampo_autotune(self.h, C.byref(c), C.byref(s)))
         return c.value, s.value
 
+    def set_species(self, species):
+        """Use a species header compiled at run time (sampo_gb300.species.Species),
+        or the built-in species (None). Set it before init_population."""
+        self._check(self.lib.sampo_set_species(self.h, species.h if species is not None else None))
+        self._species = species  # the compiled kernels must outlive their use
+
     def set_grids(self, count_ctas_per_sm: int, scatter_ctas_per_sm: int):
         """Fix the grid sizes (CTAs per SM of the two passes) without tuning."""
         self._check(self.lib.sampo_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))

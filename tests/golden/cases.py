@@ -30,9 +30,21 @@ CASES = {
                     weather=("seasonal", 40, 3, 29.0, 2.0, 0.5), interventions="alternating"),
 }
 
+# Cases run with another species header (tests/golden/species/) in place of
+# the shipped properties.h: the reference's kernels compiled against it
+# (oracle/ref_build, target species) give the fixtures.
+SPECIES_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "species")
+SPECIES_CASES = {
+    # every species hook differs; interventions on and off so that the
+    # *_PROBABILITY factors matter too
+    "hot_species": dict(seed=99, initial=2000, cc=10000.0, steps=1440, age_days=3, age_seed=5,
+                        weather=("seasonal", 60, 8, 26.0, 4.0, 0.5), interventions="alternating",
+                        species="hot_species.h"),
+}
+
 
 def make_case_inputs(name: str, directory: str):
-    c = CASES[name]
+    c = CASES[name] if name in CASES else SPECIES_CASES[name]
     w = c["weather"]
     if w[0] == "seasonal":
         _, days, wseed, mean, amp, sd = w

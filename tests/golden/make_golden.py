@@ -25,18 +25,24 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-from tests.golden.cases import CASES, make_case_inputs  # noqa: E402
+from sampo_gb300 import inputs  # noqa: E402
+from tests.golden.cases import CASES, SPECIES_CASES, SPECIES_DIR, make_case_inputs  # noqa: E402
 
 REF = os.environ.get("SAMPO_REFERENCE", "/root/reference")
 
 
-def build_ref() -> str:
-    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref_build"), f"REF={REF}"], check=True)
-    return os.path.join(REPO, "oracle", "_ref", "sampo_ref")
+def build_ref(species: str | None = None) -> str:
+    """ref-as-C; with a species header, the build that compiles it in place of properties.h."""
+    cmd = ["make", "-s", "-C", os.path.join(REPO, "oracle", "ref_build"), f"REF={REF}"]
+    if species is None:
+        subprocess.run(cmd, check=True)
+        return os.path.join(REPO, "oracle", "_ref", "sampo_ref")
+    subprocess.run(cmd + ["species", f"SPECIES_HDR={os.path.join(SPECIES_DIR, species)}"], check=True)
+    return os.path.join(REPO, "oracle", "_ref", "species_" + os.path.splitext(species)[0], "sampo_ref")
 
 
 def run_case(exe: str, name: str) -> dict:
-    c = CASES[name]
+    c = CASES[name] if name in CASES else SPECIES_CASES[name]
     with tempfile.TemporaryDirectory() as td:
         tp, ep, meta = make_case_inputs(name, td)
         hf = os.path.join(td, "hash.txt")
@@ -45,6 +51,9 @@ def run_case(exe: str, name: str) -> dict:
         if c.get("age_days", -1) >= 0:
             cmd += ["--age-days", str(c["age_days"]), "--age-seed", str(c["age_seed"])]
         cmd += [tp, ep]
+        if c.get("species"):
+            cmd.append(c["species"])
+            meta["species_sha256"] = inputs.file_sha256(os.path.join(SPECIES_DIR, c["species"]))
         out = subprocess.run(cmd, cwd=td, check=True, capture_output=True).stdout.decode()
         lines = out.split("\n")
         trace = [ln for ln in lines if ln.endswith("\r") and ln.count(",") == 18]
@@ -59,10 +68,10 @@ def run_case(exe: str, name: str) -> dict:
 
 
 def main(argv):
-    names = argv or list(CASES)
-    exe = build_ref()
+    names = argv or list(CASES) + list(SPECIES_CASES)
     for name in names:
-        data = run_case(exe, name)
+        c = CASES[name] if name in CASES else SPECIES_CASES[name]
+        data = run_case(build_ref(c.get("species")), name)
         path = os.path.join(HERE, f"{name}.json.gz")
         with gzip.open(path, "wt") as f:
             json.dump(data, f, separators=(",", ":"))

@@ -27,7 +27,7 @@ def test_cli_arguments_without_gpu(cli, tmp_path):
                                            "Species:\tproperties.h",
                                            f"Cannot open {tmp_path / 'missing.txt'}. Check temperature file path"]
     out = subprocess.run([cli, "t.txt", "e.txt", "otherSpecies.h"], capture_output=True, text=True, cwd=tmp_path)
-    assert out.returncode == 2 and "built-in species" in out.stderr
+    assert out.stdout.splitlines()[3] == "Cannot open t.txt. Check temperature file path"
 
 
 @pytest.mark.gpu
