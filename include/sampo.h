@@ -169,6 +169,10 @@ int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_
  * on the same workload: 1 .. the occupancy limit of each pass. */
 int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
 int sampo_checkpoint_load(sampo_sim* s, const char* path);
+/* Header of a checkpoint file (no device needed): the step it resumes at,
+ * the population then, and the population at the previous step's start
+ * (*has_prev = 0 for step 0 or a version-1 file). Any pointer may be NULL. */
+int sampo_checkpoint_info(const char* path, uint32_t* step, sampo_population* pop, sampo_population* prev, int* has_prev);
 /* ---- species headers compiled at run time ----
  * The reference compiles its kernels at start-up with the species header
  * named by argv[3] (src/abms.c:565-568; default properties.h, which is built
@@ -341,6 +345,13 @@ int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm, uint32_t s
 /* The species of every replicate of the batch (NULL: built in); as
  * sampo_set_species. */
 int sampo_batch_set_species(sampo_batch* b, const sampo_species* sp);
+/* Checkpoints of one slot in the format of sampo_checkpoint_save: a file
+ * written by either loads into either (same carrying capacity, enough
+ * capacity). A slot's device seed stream travels with it. Load into a slot
+ * taken with sampo_batch_add (it replaces init_population); the slot resumes
+ * at the file's step and needs inputs from there. */
+int sampo_batch_checkpoint_save(sampo_batch* b, uint32_t slot, const char* path);
+int sampo_batch_checkpoint_load(sampo_batch* b, uint32_t slot, const char* path);
 /* Device time of the last sampo_batch_run, in milliseconds (after sync). */
 int sampo_batch_last_run_ms(sampo_batch* b, double* ms);
 

@@ -151,6 +151,10 @@ SIGNATURES = {
     "sampo_batch_set_seeds": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32]),
     "sampo_batch_init_population": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_int, C.c_uint64]),
     "sampo_batch_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "sampo_batch_checkpoint_save": (C.c_int, [_P, C.c_uint32, C.c_char_p]),
+    "sampo_batch_checkpoint_load": (C.c_int, [_P, C.c_uint32, C.c_char_p]),
+    "sampo_checkpoint_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(Population), C.POINTER(Population),
+                                        C.POINTER(C.c_int)]),
     "sampo_batch_seed_stream": (C.c_int, [_P, C.c_uint32, C.POINTER(RandState)]),
     "sampo_batch_seed_state": (C.c_int, [_P, C.c_uint32, C.POINTER(RandState), C.POINTER(C.c_uint32)]),
     "sampo_batch_run": (C.c_int, [_P, C.c_uint32, C.c_int]),

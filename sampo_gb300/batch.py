@@ -81,6 +81,15 @@ class Batch:
         init_seeds = np.ascontiguousarray(init_seeds, dtype=np.uint32).reshape(4, 4)
         self._check(self.lib.sampo_batch_init_population(self.h, slot, n, ptr(init_seeds), age_days_max, age_seed))
 
+    def checkpoint(self, slot: int, path: str):
+        """sampo_batch_checkpoint_save: the slot at its step boundary (the file
+        format of Simulation.checkpoint)."""
+        self._check(self.lib.sampo_batch_checkpoint_save(self.h, slot, path.encode()))
+
+    def resume(self, slot: int, path: str):
+        """sampo_batch_checkpoint_load into a slot taken with add()."""
+        self._check(self.lib.sampo_batch_checkpoint_load(self.h, slot, path.encode()))
+
     def seed_stream(self, slot: int, st: RandState):
         """sampo_batch_seed_stream: the slot draws each coming step's seeds
         from its own copy of the rand() stream `st` on the device."""

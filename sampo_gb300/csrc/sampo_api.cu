@@ -13,6 +13,7 @@
 #include <vector>
 #include "sampo_model.cuh"
 #include "sampo_kernels.cuh"
+#include "sampo_checkpoint.cuh"
 
 using namespace sampo;
 
@@ -560,77 +561,59 @@ extern "C" int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_v
 // ---- checkpoints: "SAMPOCK1", u32 version, u32 step, f32 cc, population,
 //      bites/cycles, u32 n, u32 0, then nine columns of n 4-byte values and
 //      the n flag bytes (state | isFemale << 3) ----
-namespace {
-const char kCkMagic[8] = {'S', 'A', 'M', 'P', 'O', 'C', 'K', '1'};
-struct CkHeader {
-  char magic[8];
-  uint32_t version, step;
-  float cc;
-  sampo_population pop;
-  sampo_bites_cycles bnc;
-  uint32_t n, reserved;
-};
-}  // namespace
-
 extern "C" int sampo_checkpoint_save(sampo_sim* s, const char* path) {
   if (!s || !path) return SAMPO_ERR_ARG;
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
   cudaSetDevice(s->device);
   SimDev h;
   CK(cudaMemcpyAsync(&h, s->sim_dev, sizeof(SimDev), cudaMemcpyDeviceToHost, s->stream), "state");
-  CK(cudaStreamSynchronize(s->stream), "state");
   CkHeader hd;
   memset(&hd, 0, sizeof(hd));
   memcpy(hd.magic, kCkMagic, 8);
-  hd.version = 1;
+  hd.version = 2;
   hd.step = h.step;
   hd.cc = s->cc;
   hd.pop = h.pop;
   hd.bnc = h.bnc;
   hd.n = h.pop.r[7].end;
-  const size_t n = hd.n;
-  std::vector<uint8_t> buf(n * 4);
-  FILE* f = fopen(path, "wb");
-  if (!f) return fail(s, SAMPO_ERR_IO, std::string("cannot write ") + path);
-  bool ok = fwrite(&hd, sizeof(hd), 1, f) == 1;
-  const DevPool& P = s->pool[h.cur & 1u];
-  void* cols[9] = {P.age, P.his, P.delay, P.sporo, P.uni, P.avail, P.cycle, P.hbc, P.batches};
-  for (int c = 0; c < 9 && ok; c++) {
-    if (n && cudaMemcpy(buf.data(), cols[c], n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
-    if (ok && n) ok = fwrite(buf.data(), 4, n, f) == n;
+  if (h.step > 0) {  // the previous step's row is still in the ring
+    sampo_stats_row prev;
+    CK(cudaMemcpyAsync(&prev, s->rows_dev + (h.step - 1) % s->ring, sizeof(prev), cudaMemcpyDeviceToHost, s->stream), "rows");
+    CK(cudaStreamSynchronize(s->stream), "rows");
+    hd.prev = prev.pop;
+    hd.flags |= CK_PREV;
   }
-  if (ok && n && cudaMemcpy(buf.data(), P.flags, n, cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
-  if (ok && n) ok = fwrite(buf.data(), 1, n, f) == n;
-  ok = (fclose(f) == 0) && ok;
-  if (!ok) return fail(s, SAMPO_ERR_IO, std::string("checkpoint write failed: ") + path);
+  CK(cudaStreamSynchronize(s->stream), "state");
+  const std::string err = ck_write(path, hd, s->pool[h.cur & 1u]);
+  if (!err.empty()) return fail(s, SAMPO_ERR_IO, err);
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_checkpoint_info(const char* path, uint32_t* step, sampo_population* pop, sampo_population* prev,
+                                     int* has_prev) {
+  if (!path) return SAMPO_ERR_ARG;
+  CkHeader hd;
+  FILE* f = nullptr;
+  if (!ck_open(path, hd, &f).empty()) return SAMPO_ERR_IO;
+  fclose(f);
+  if (step) *step = hd.step;
+  if (pop) *pop = hd.pop;
+  if (prev) *prev = hd.prev;
+  if (has_prev) *has_prev = (hd.flags & CK_PREV) ? 1 : 0;
   return SAMPO_OK;
 }
 
 extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
   if (!s || !path) return SAMPO_ERR_ARG;
-  FILE* f = fopen(path, "rb");
-  if (!f) return fail(s, SAMPO_ERR_IO, std::string("cannot read ") + path);
   CkHeader hd;
-  if (fread(&hd, sizeof(hd), 1, f) != 1 || memcmp(hd.magic, kCkMagic, 8) != 0 || hd.version != 1) {
-    fclose(f);
-    return fail(s, SAMPO_ERR_IO, std::string("not a checkpoint: ") + path);
-  }
+  FILE* f = nullptr;
+  const std::string err = ck_open(path, hd, &f);
+  if (!err.empty()) return fail(s, SAMPO_ERR_IO, err);
   if (hd.cc != s->cc) { fclose(f); return fail(s, SAMPO_ERR_ARG, "checkpoint carrying capacity differs from the handle's"); }
-  if ((uint64_t)hd.n > s->capacity || hd.pop.r[7].end != hd.n) { fclose(f); return fail(s, SAMPO_ERR_CAPACITY, "checkpoint pool exceeds the capacity"); }
+  if ((uint64_t)hd.n > s->capacity) { fclose(f); return fail(s, SAMPO_ERR_CAPACITY, "checkpoint pool exceeds the capacity"); }
   cudaSetDevice(s->device);
-  const size_t n = hd.n;
-  std::vector<uint8_t> buf(n * 4);
-  const DevPool& P = s->pool[0];
-  void* cols[9] = {P.age, P.his, P.delay, P.sporo, P.uni, P.avail, P.cycle, P.hbc, P.batches};
-  bool ok = true;
-  for (int c = 0; c < 9 && ok; c++) {
-    ok = fread(buf.data(), 4, n, f) == n;
-    if (ok && n) ok = cudaMemcpy(cols[c], buf.data(), n * 4, cudaMemcpyHostToDevice) == cudaSuccess;
-  }
-  if (ok) ok = fread(buf.data(), 1, n, f) == n;
-  if (ok && n) ok = cudaMemcpy(P.flags, buf.data(), n, cudaMemcpyHostToDevice) == cudaSuccess;
-  fclose(f);
-  if (!ok) return fail(s, SAMPO_ERR_IO, std::string("checkpoint read failed: ") + path);
+  const std::string rerr = ck_read_pool(f, hd, s->pool[0]);
+  if (!rerr.empty()) return fail(s, SAMPO_ERR_IO, rerr + ": " + path);
   // the state as a step boundary left it: step, ranges, the counters the next
   // row reports; the statistics and step constants are recomputed
   SimDev h = s->host_state;

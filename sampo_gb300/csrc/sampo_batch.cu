@@ -16,6 +16,7 @@
 #include <vector>
 #include "sampo_model.cuh"
 #include "sampo_kernels.cuh"
+#include "sampo_checkpoint.cuh"
 
 using namespace sampo;
 
@@ -384,6 +385,86 @@ extern "C" int sampo_batch_seed_stream(sampo_batch* b, uint32_t slot, const samp
   BCK(cudaMemcpyAsync(&b->sims_dev[slot].rnd, &h, sizeof(h), cudaMemcpyHostToDevice, b->stream), "seed stream");
   BCK(cudaStreamSynchronize(b->stream), "seed stream");
   r->dev_seeds = true;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_checkpoint_save(sampo_batch* b, uint32_t slot, const char* path) {
+  Replicate* r = get_slot(b, slot);
+  if (!r || !path) return SAMPO_ERR_ARG;
+  if (!r->have_pop) return bfail(b, SAMPO_ERR_STATE, "no population");
+  cudaSetDevice(b->device);
+  BCK(cudaStreamSynchronize(b->stream), "checkpoint");  // the slot is at a step boundary
+  SimDev h;
+  BCK(cudaMemcpy(&h, b->sims_dev + slot, sizeof(SimDev), cudaMemcpyDeviceToHost), "state");
+  CkHeader hd;
+  memset(&hd, 0, sizeof(hd));
+  memcpy(hd.magic, kCkMagic, 8);
+  hd.version = 2;
+  hd.step = h.step;
+  hd.cc = r->cc;
+  hd.pop = h.pop;
+  hd.bnc = h.bnc;
+  hd.n = h.pop.r[7].end;
+  if (h.step > 0) {
+    sampo_stats_row prev;
+    BCK(cudaMemcpy(&prev, r->rp.rows + (h.step - 1) % b->ring, sizeof(prev), cudaMemcpyDeviceToHost), "rows");
+    hd.prev = prev.pop;
+    hd.flags |= CK_PREV;
+  }
+  if (r->dev_seeds) {
+    hd.rnd = h.rnd;
+    hd.flags |= CK_SEED_STREAM;
+    if (h.rnd.next == h.step + 1) {  // the coming step's seeds are already drawn
+      BCK(cudaMemcpy(hd.coming, r->rp.seeds + (size_t)(h.step % b->ring) * 4, sizeof(hd.coming), cudaMemcpyDeviceToHost),
+          "seeds");
+      hd.flags |= CK_COMING_SEEDS;
+    }
+  }
+  const std::string err = ck_write(path, hd, r->rp.pool[h.cur & 1u]);
+  if (!err.empty()) return bfail(b, SAMPO_ERR_IO, err);
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_checkpoint_load(sampo_batch* b, uint32_t slot, const char* path) {
+  Replicate* r = get_slot(b, slot);
+  if (!r || !path) return SAMPO_ERR_ARG;
+  CkHeader hd;
+  FILE* f = nullptr;
+  const std::string err = ck_open(path, hd, &f);
+  if (!err.empty()) return bfail(b, SAMPO_ERR_IO, err);
+  if (hd.cc != r->cc) { fclose(f); return bfail(b, SAMPO_ERR_ARG, "checkpoint carrying capacity differs from the slot's"); }
+  if ((uint64_t)hd.n > r->capacity) { fclose(f); return bfail(b, SAMPO_ERR_CAPACITY, "checkpoint pool exceeds the slot's capacity"); }
+  cudaSetDevice(b->device);
+  BCK(cudaStreamSynchronize(b->stream), "checkpoint");
+  const std::string rerr = ck_read_pool(f, hd, r->rp.pool[0]);
+  if (!rerr.empty()) return bfail(b, SAMPO_ERR_IO, rerr + ": " + path);
+  SimDev h = initial_sim_state((uint32_t)r->capacity, r->cc);
+  h.pop = hd.pop;
+  h.pop.numLarvae1DayEquiv = h.pop.numFemale = h.pop.numPotentiallyInfective = 0;
+  h.bnc = hd.bnc;
+  h.step = hd.step;
+  h.stop_step = r->stop_step;
+  h.active = hd.step < r->stop_step;
+  r->dev_seeds = (hd.flags & CK_SEED_STREAM) != 0;
+  if (r->dev_seeds) {
+    h.rnd = hd.rnd;
+    if (hd.flags & CK_COMING_SEEDS)
+      BCK(cudaMemcpyAsync((sampo_seeds*)r->rp.seeds + (size_t)(hd.step % b->ring) * 4, hd.coming, sizeof(hd.coming),
+                          cudaMemcpyHostToDevice, b->stream), "seeds");
+  }
+  const int st = upload_slot(b, slot, h);
+  if (st) return st;
+  BCK(cudaMemsetAsync(r->rp.tilePre, 0, (size_t)r->rp.maxTiles * kTileArrayWords * 4, b->stream), "tile arrays");
+  BCK(launch_publish_start(slot_params(b, slot), b->stream), "checkpoint statistics");
+  SimDev back;
+  BCK(cudaMemcpyAsync(&back, b->sims_dev + slot, sizeof(SimDev), cudaMemcpyDeviceToHost, b->stream), "state");
+  BCK(cudaStreamSynchronize(b->stream), "state");
+  if (back.pop.numLarvae1DayEquiv != hd.pop.numLarvae1DayEquiv || back.pop.numFemale != hd.pop.numFemale ||
+      back.pop.numPotentiallyInfective != hd.pop.numPotentiallyInfective)
+    return bfail(b, SAMPO_ERR_INTERNAL, "checkpoint statistics do not match its pool");
+  r->have_pop = true;
+  r->step = hd.step;
+  r->active = h.active != 0;
   return SAMPO_OK;
 }
 

@@ -26,6 +26,10 @@
  *                   formats chunk k from one pinned row buffer while the GPU
  *                   runs chunk k + 1 into the other
  *   --device D      CUDA device
+ *   --checkpoint K F  write a checkpoint of the state after K steps to F
+ *   --resume F      continue from checkpoint F (same --seed, --cc and
+ *                   inputs): prints the stats lines from its step on, which
+ *                   equal those of the uninterrupted run
  * The species header (third argument, default properties.h): properties.h
  * is the built-in species; any other header file is compiled into the step
  * kernels at start-up (sampo_species_compile), as the reference compiles its
@@ -178,6 +182,9 @@ int main(int argc, char** argv) {
   uint64_t capacity = 6000000ull, age_seed = 0;
   float cc = 160000.0f;
   int age_days = -1, per_step = 0, device = 0;
+  uint32_t ck_step = 0xffffffffu;
+  const char* ck_path = NULL;
+  const char* resume_path = NULL;
   const char* pos[3] = {"temp.txt", "environment.txt", "properties.h"};
   int np = 0;
   for (int i = 1; i < argc; i++) {
@@ -193,6 +200,10 @@ int main(int argc, char** argv) {
     else if (!strcmp(argv[i], "--age-seed") && i + 1 < argc) age_seed = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--per-step")) per_step = 1;
     else if (!strcmp(argv[i], "--device") && i + 1 < argc) device = atoi(argv[++i]);
+    else if (!strcmp(argv[i], "--checkpoint") && i + 2 < argc) {
+      ck_step = (uint32_t)strtoul(argv[++i], 0, 10);
+      ck_path = argv[++i];
+    } else if (!strcmp(argv[i], "--resume") && i + 1 < argc) resume_path = argv[++i];
     else if (np < 3 && argv[i][0] != '-') pos[np++] = argv[i];
     else {
       fprintf(stderr, "sampo: unexpected argument %s\n", argv[i]);
@@ -245,12 +256,25 @@ int main(int argc, char** argv) {
   if (!seeds) return 1;
   for (uint32_t i = 0; i < steps; i++) draw_seeds(seeds + 4 * (size_t)i);
   if ((rc = sampo_set_seeds(s, 0, seeds, steps)) != SAMPO_OK) fail(s, "seeds", rc);
-  if ((rc = sampo_init_population(s, initial, init, age_days, age_seed)) != SAMPO_OK) fail(s, "initial population", rc);
+  uint32_t first = 0;
   sampo_population prev;
-  if ((rc = sampo_read_pool(s, &prev, NULL)) != SAMPO_OK) fail(s, "population", rc);
+  if (resume_path) {
+    int has_prev = 0;
+    if (sampo_checkpoint_info(resume_path, &first, NULL, &prev, &has_prev) != SAMPO_OK) {
+      fprintf(stderr, "sampo: cannot read checkpoint %s\n", resume_path);
+      return 2;
+    }
+    if (first > steps) first = steps;
+    if ((rc = sampo_checkpoint_load(s, resume_path)) != SAMPO_OK) fail(s, "checkpoint", rc);
+    if (!has_prev && (rc = sampo_read_pool(s, &prev, NULL)) != SAMPO_OK) fail(s, "population", rc);
+  } else {
+    if ((rc = sampo_init_population(s, initial, init, age_days, age_seed)) != SAMPO_OK) fail(s, "initial population", rc);
+    if ((rc = sampo_read_pool(s, &prev, NULL)) != SAMPO_OK) fail(s, "population", rc);
+  }
 
   if (per_step) {
-    for (uint32_t i = 0; i < steps; i++) {
+    for (uint32_t i = first; i < steps; i++) {
+      if (i == ck_step && (rc = sampo_checkpoint_save(s, ck_path)) != SAMPO_OK) fail(s, "checkpoint", rc);
       sampo_stats_row row;
       /* the row of step i is the state the step starts from: print and
        * check it first, as the reference does before its update */
@@ -274,16 +298,18 @@ int main(int argc, char** argv) {
     pr.prev = prev;
     pthread_t th;
     if (pthread_create(&th, NULL, printer_main, &pr) != 0) return 1;
-    uint32_t k = 0;
-    for (uint32_t first = 0; first < steps; first += chunk, k ^= 1u) {
-      const uint32_t n = steps - first < chunk ? steps - first : chunk;
+    uint32_t k = 0, n = 0;
+    for (uint32_t at = first; at < steps; at += n, k ^= 1u) {
+      if (at == ck_step && (rc = sampo_checkpoint_save(s, ck_path)) != SAMPO_OK) fail(s, "checkpoint", rc);
+      n = steps - at < chunk ? steps - at : chunk;
+      if (at < ck_step && ck_step - at < n) n = ck_step - at;  /* a chunk ends at the checkpoint */
       rc = sampo_run(s, n, rows[k]);  /* meanwhile the printer formats the other buffer */
       printer_idle(&pr);
       if (rc != SAMPO_OK) {
-        print_rows(&pr, rows[k], first, n - 1);  /* the rows before the failed step */
+        print_rows(&pr, rows[k], at, n - 1);  /* the rows before the failed step */
         fail(s, "run", rc);
       }
-      printer_submit(&pr, rows[k], first, n);
+      printer_submit(&pr, rows[k], at, n);
     }
     printer_idle(&pr);
     pthread_mutex_lock(&pr.mu);
@@ -295,6 +321,7 @@ int main(int argc, char** argv) {
     sampo_host_free(rows[1]);
   }
 
+  if (ck_path && ck_step == steps && (rc = sampo_checkpoint_save(s, ck_path)) != SAMPO_OK) fail(s, "checkpoint", rc);
   sampo_population final;
   if ((rc = sampo_read_pool(s, &final, NULL)) != SAMPO_OK) fail(s, "population", rc);
   print_population(&final);
