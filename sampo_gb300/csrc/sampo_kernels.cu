@@ -102,15 +102,16 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < 3 && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
   // each kernel's time is taken on its own (the best count grid does not
-  // depend on the scatter grid), minimum over every trial that ran it; one
-  // untimed trial first
+  // depend on the scatter grid), minimum over every trial that ran it (eight
+  // per pair: small pools run the kernels in tens of microseconds, where
+  // single timings differ by more than the grids do); one untimed trial first
   double tc[9], ts[9];
   for (int i = 0; i < 9; i++) tc[i] = ts[i] = 1e30;
   max_c = max_c > 8 ? 8 : max_c;
   max_s = max_s > 8 ? 8 : max_s;
   for (int c = 1; c <= max_c && e == cudaSuccess; c++) {
     for (int s = 1; s <= max_s && e == cudaSuccess; s++) {
-      for (int rep = (c == 1 && s == 1) ? -1 : 0; rep < 3 && e == cudaSuccess; rep++) {
+      for (int rep = (c == 1 && s == 1) ? -1 : 0; rep < 8 && e == cudaSuccess; rep++) {
         if ((e = launch_trial_reset(p, st)) != cudaSuccess) break;
         if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) break;
         if ((e = launch_count(p, c * sms, st)) != cudaSuccess) break;
@@ -132,6 +133,30 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
     if (tc[c] < tc[bc]) bc = c;
   for (int s = 1; s <= max_s; s++)
     if (ts[s] < ts[bs]) bs = s;
+  // the kernels run back to back in a step, where a small pool's times are
+  // mostly start-up and tail: keep the pick only if it also beats the
+  // largest grids run that way
+  if (e == cudaSuccess && (bc != max_c || bs != max_s)) {
+    double tj[2] = {1e30, 1e30};
+    const int gc[2] = {bc, max_c}, gs[2] = {bs, max_s};
+    for (int rep = 0; rep < 8 && e == cudaSuccess; rep++) {
+      for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+        if ((e = launch_trial_reset(p, st)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) break;
+        if ((e = launch_count(p, gc[v] * sms, st)) != cudaSuccess) break;
+        if ((e = launch_scatter(p, gs[v] * sms, st)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) break;
+        if ((e = cudaEventSynchronize(ev[2])) != cudaSuccess) break;
+        float m = 0;
+        cudaEventElapsedTime(&m, ev[0], ev[2]);
+        if (m < tj[v]) tj[v] = m;
+      }
+    }
+    if (tj[1] <= tj[0]) {
+      bc = max_c;
+      bs = max_s;
+    }
+  }
   if (e == cudaSuccess) e = launch_trial_reset(p, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   for (int i = 0; i < 3; i++)
