@@ -191,6 +191,8 @@ int sampo_species_compile(const char* header_path, int device, char* log, size_t
 int sampo_species_compile_text(const char* name, const char* text, int device, char* log, size_t log_size,
                                sampo_species** out);
 void sampo_species_free(sampo_species* sp);
+/* The device a species was compiled and loaded for (-1 for NULL). */
+int sampo_species_device(const sampo_species* sp);
 /* Compiles without loading, for sm_<sm>a (e.g. 103): a syntax check that
  * needs no GPU. */
 int sampo_species_check_text(const char* name, const char* text, int sm, char* log, size_t log_size);

@@ -137,6 +137,7 @@ SIGNATURES = {
     "sampo_species_compile_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(_P)]),
     "sampo_species_check_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_size_t]),
     "sampo_species_free": (None, [_P]),
+    "sampo_species_device": (C.c_int, [_P]),
     "sampo_set_species": (C.c_int, [_P, _P]),
     "sampo_batch_set_species": (C.c_int, [_P, _P]),
     "sampo_batch_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),

@@ -667,6 +667,7 @@ extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_
 
 extern "C" int sampo_set_species(sampo_sim* s, const sampo_species* sp) {
   if (!s) return SAMPO_ERR_ARG;
+  if (sp && sampo_species_device(sp) != s->device) return fail(s, SAMPO_ERR_ARG, "species compiled for another device");
   cudaSetDevice(s->device);
   if (s->species == sp) return SAMPO_OK;
   s->species = sp;

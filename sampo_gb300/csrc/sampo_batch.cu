@@ -578,6 +578,7 @@ extern "C" int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm,
 
 extern "C" int sampo_batch_set_species(sampo_batch* b, const sampo_species* sp) {
   if (!b) return SAMPO_ERR_ARG;
+  if (sp && sampo_species_device(sp) != b->device) return bfail(b, SAMPO_ERR_ARG, "species compiled for another device");
   cudaSetDevice(b->device);
   if (b->species == sp) return SAMPO_OK;
   b->species = sp;

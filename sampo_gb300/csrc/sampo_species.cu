@@ -16,6 +16,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -45,11 +46,16 @@ struct Nvrtc {
   decltype(&nvrtcDestroyProgram) destroy = nullptr;
 };
 
+void open_nvrtc(Nvrtc& n);
+
 const Nvrtc& nvrtc() {
   static Nvrtc n;
-  static bool tried = false;
-  if (tried) return n;
-  tried = true;
+  static std::once_flag once;
+  std::call_once(once, [] { open_nvrtc(n); });
+  return n;
+}
+
+void open_nvrtc(Nvrtc& n) {
   const char* names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
                          "/usr/local/cuda/lib64/libnvrtc.so"};
   void* h = nullptr;
@@ -57,7 +63,7 @@ const Nvrtc& nvrtc() {
     if ((h = dlopen(nm, RTLD_NOW | RTLD_LOCAL)) != nullptr) break;
   if (!h) {
     n.why = "NVRTC (libnvrtc.so) not found";
-    return n;
+    return;
   }
 #define SAMPO_SYM(field, sym) n.field = reinterpret_cast<decltype(n.field)>(dlsym(h, #sym))
   SAMPO_SYM(create, nvrtcCreateProgram);
@@ -72,10 +78,12 @@ const Nvrtc& nvrtc() {
 #undef SAMPO_SYM
   n.ok = n.create && n.compile && n.add_name && n.lowered && n.cubin_size && n.cubin && n.log_size && n.log && n.destroy;
   if (!n.ok) n.why = "NVRTC lacks an entry point this library needs";
-  return n;
+  return;
 }
 
 // ---- driver API entry points, from the runtime ----
+struct Driver;
+void open_driver(Driver& d);
 struct Driver {
   bool ok = false;
   CUresult (*module_load)(CUmodule*, const void*) = nullptr;
@@ -89,9 +97,12 @@ struct Driver {
 
 const Driver& driver() {
   static Driver d;
-  static bool tried = false;
-  if (tried) return d;
-  tried = true;
+  static std::once_flag once;
+  std::call_once(once, [] { open_driver(d); });
+  return d;
+}
+
+void open_driver(Driver& d) {
   auto get = [](const char* sym, void** fp) {
     cudaDriverEntryPointQueryResult q;
     return cudaGetDriverEntryPointByVersion(sym, fp, 12000, cudaEnableDefault, &q) == cudaSuccess &&
@@ -101,7 +112,6 @@ const Driver& driver() {
          get("cuModuleGetFunction", (void**)&d.get_function) && get("cuLaunchKernel", (void**)&d.launch) &&
          get("cuFuncSetAttribute", (void**)&d.set_attr) &&
          get("cuOccupancyMaxActiveBlocksPerMultiprocessor", (void**)&d.occupancy);
-  return d;
 }
 
 // the kernels of one compiled species, in KID_* order
@@ -278,6 +288,8 @@ extern "C" int sampo_species_compile(const char* header_path, int device, char* 
   fclose(f);
   return sampo_species_compile_text(header_path, text.c_str(), device, log, log_size, out);
 }
+
+extern "C" int sampo_species_device(const sampo_species* sp) { return sp ? sp->device : -1; }
 
 extern "C" void sampo_species_free(sampo_species* sp) {
   if (!sp) return;
