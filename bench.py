@@ -242,6 +242,8 @@ def gpu_arm(args, wl, rank, world, device):
     count_bytes = (live2 * COUNT_BYTES).sum(axis=1)
     n_launch = len(tot)
     scatter_ms, count_ms = times[1] / n_launch, times[0] / n_launch
+    # the step in timing mode minus the two passes: k_publish and the gaps between the launches
+    publish_ms = (times[2] - times[0] - times[1]) / n_launch
     peak, peak_kind = peaks()
     achieved = scatter_bytes.mean() / (scatter_ms * 1e-3) / 1e9
     prof = traffic_from_profile()
@@ -277,7 +279,7 @@ def gpu_arm(args, wl, rank, world, device):
         h.free()
     sim.close()
     return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(),
-                gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, achieved=achieved, peak=peak,
+                gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, publish_ms=publish_ms, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
                 count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned)
 
@@ -567,6 +569,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
                      "frac": r["achieved"] / r["peak"], "traffic": r["traffic"], "kernel": "k_scatter (update + stable scatter)",
                      "peak_kind": r["peak_kind"], "scatter_ms_per_launch": r["scatter_ms"], "count_ms_per_launch": r["count_ms"],
+                     "publish_and_gaps_ms_per_step": r["publish_ms"],
                      "count_pass_gbs": r["count_gbs"],
                      "algorithmic_bytes": "k_scatter: 37 B read per live agent + 37 B written per agent of the next pool"},
         "e2e": {"value": e2e_days / e2e_max, "unit": "agent-days/s", "h2d_bytes_per_step": 24 * (4 + 24 + 4 + 64),
