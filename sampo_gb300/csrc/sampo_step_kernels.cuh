@@ -3,7 +3,6 @@
 // the library by nvcc (sampo_kernels.cu) and, for a user species header, at
 // run time by NVRTC (sampo_species.cu).
 //
-//
 // A step of a batch of simulations is two persistent-CTA kernels over every
 // active replicate's current pool buffer, whose 1024-slot tiles they take
 // from one ticket counter, and a small one with a CTA per replicate:
@@ -11,12 +10,14 @@
 //  k_count   reads the ~12 bytes per agent that decide survival, the next
 //            state and the eggs laid (killAgents + the decision part of
 //            updateAgents), and publishes per tile the number of survivors
-//            per next state plus the replicate's newEggs total.
+//            per next state, the tile's prefix table over its (round, warp)
+//            chunks, and the replicate's newEggs total.
 //  k_scatter recomputes the same decisions with the complete record,
 //            obtains each survivor's stable rank within its next state
-//            (warp match/popc + a block scan + a decoupled look-back over
-//            the tile counts that k_count already published, within the
-//            replicate, so no CTA ever waits on another), writes the updated
+//            (warp match/popc, the tile's prefix table, and a decoupled
+//            look-back over the tile counts that k_count already published,
+//            within the replicate, so no CTA ever waits on another and the
+//            consumer warps share no barrier), writes the updated
 //            record to its slot in the other buffer (the reference's
 //            oldToNewAgents layout, kernel/oldToNewAgents.cl:57-95,126-226),
 //            writes the new eggs at [0, newEggs) (initAgents,
