@@ -136,9 +136,22 @@ int sampo_step(sampo_sim* s, const sampo_environment* env, float temperature, ui
  * Days are replayed as CUDA graphs of 24 steps. rows (may be NULL)
  * receives nsteps stats rows. */
 int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows);
+/* sampo_run without waiting (the stats rows of src/abms.c:502-529 streamed
+ * to the host while the caller formats earlier ones): the steps and the
+ * copies of their rows are queued on the simulation's stream and the call
+ * returns. rows must stay valid until sampo_sync; page-locked rows
+ * (sampo_host_alloc) keep the copies asynchronous. Further sampo_run_async
+ * calls queue behind; any other call on the handle first waits for the queue
+ * and returns its error, if any. Device errors of queued steps (capacity,
+ * temperature) are reported by sampo_sync. With timing on it waits like
+ * sampo_run. */
+int sampo_run_async(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows);
+/* Waits for the steps sampo_run_async queued; their status, and the device
+ * time from the first queued step to the last for sampo_last_run_ms. */
+int sampo_sync(sampo_sim* s);
 /* Stats at the start of the current (next) step. */
 int sampo_current_row(sampo_sim* s, sampo_stats_row* row);
-/* Index of the next step. */
+/* Index of the next step (after the steps sampo_run_async queued). */
 int sampo_get_step(sampo_sim* s, uint32_t* step);
 
 /* storeHistogram (src/abms.c:160-183, kernel/ageHistogram.cl:13-35):

@@ -109,6 +109,8 @@ SIGNATURES = {
     "sampo_load_pool": (C.c_int, [_P, C.POINTER(Population), C.POINTER(PoolView)]),
     "sampo_step": (C.c_int, [_P, C.POINTER(Environment), C.c_float, C.c_uint32, _P, C.POINTER(StatsRow)]),
     "sampo_run": (C.c_int, [_P, C.c_uint32, _P]),
+    "sampo_run_async": (C.c_int, [_P, C.c_uint32, _P]),
+    "sampo_sync": (C.c_int, [_P]),
     "sampo_current_row": (C.c_int, [_P, C.POINTER(StatsRow)]),
     "sampo_get_step": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "sampo_histogram": (C.c_int, [_P, _P]),

@@ -52,6 +52,7 @@ struct sampo_sim {
   uint32_t step = 0;                   // host mirror of the device step index
   uint32_t epoch = 1;                  // host mirror of the device epoch
   bool have_pop = false;
+  bool pending = false;                // steps queued by sampo_run_async, not yet synced
   int grid_count = 0, grid_scatter = 0;
   cudaGraphExec_t day_graph = nullptr;
   bool timing = false;
@@ -72,6 +73,17 @@ static int cuda_fail(sampo_sim* s, cudaError_t e, const char* what) {
   do {                                                   \
     cudaError_t e_ = (call);                             \
     if (e_ != cudaSuccess) return cuda_fail(s, e_, what); \
+  } while (0)
+
+extern "C" int sampo_sync(sampo_sim* s);
+// Every call that reads or changes the simulation first waits for the steps
+// sampo_run_async queued, and returns their error if they failed.
+#define SETTLE(s)                          \
+  do {                                     \
+    if ((s)->pending) {                    \
+      int rc_ = sampo_sync(s);             \
+      if (rc_ != SAMPO_OK) return rc_;     \
+    }                                      \
   } while (0)
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -207,6 +219,7 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
 extern "C" int sampo_set_inputs(sampo_sim* s, uint32_t first, const float* temperature, const sampo_environment* env,
                                 uint32_t nsteps) {
   if (!s || !temperature || !env) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (nsteps == 0 || nsteps > s->ring) return fail(s, SAMPO_ERR_ARG, "nsteps exceeds the input ring (config.max_steps)");
   for (uint32_t i = 0; i < nsteps; i++)
     if (env[i].carryingCapacity != s->cc)
@@ -234,6 +247,7 @@ extern "C" int sampo_set_inputs(sampo_sim* s, uint32_t first, const float* tempe
 
 extern "C" int sampo_set_seeds(sampo_sim* s, uint32_t first, const sampo_seeds* seeds, uint32_t nsteps) {
   if (!s || !seeds) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (nsteps == 0 || nsteps > s->ring) return fail(s, SAMPO_ERR_ARG, "nsteps exceeds the seed ring (config.max_steps)");
   cudaSetDevice(s->device);
   uint32_t done = 0;
@@ -276,6 +290,7 @@ static int publish_initial(sampo_sim* s) {
 
 extern "C" int sampo_init_population(sampo_sim* s, uint32_t n, const sampo_seeds init_seeds[4], int age_days_max, uint64_t age_seed) {
   if (!s || !init_seeds) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_inputs[0] || s->input_step[0] != 0)
     return fail(s, SAMPO_ERR_STATE, "set the inputs first: the initial eggs use temperature[0] (src/abms.c:198)");
   cudaSetDevice(s->device);
@@ -302,6 +317,7 @@ extern "C" int sampo_init_population(sampo_sim* s, uint32_t n, const sampo_seeds
 
 extern "C" int sampo_load_pool(sampo_sim* s, const sampo_population* pop, const sampo_pool_view* v) {
   if (!s || !pop || !v) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (pop->r[0].start != 0) return fail(s, SAMPO_ERR_ARG, "the egg range must start at slot 0");
   for (int k = 0; k < 8; k++) {
     if (pop->r[k].end < pop->r[k].start) return fail(s, SAMPO_ERR_ARG, "range end before start");
@@ -351,6 +367,7 @@ static cudaError_t launch_step(sampo_sim* s, const KParams& p) {
 extern "C" int sampo_step(sampo_sim* s, const sampo_environment* env, float temperature, uint32_t world_time,
                           const sampo_seeds seeds[4], sampo_stats_row* row) {
   if (!s || !env || !seeds) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population: call sampo_init_population or sampo_load_pool");
   if (env->carryingCapacity != s->cc) return fail(s, SAMPO_ERR_ARG, "environment carryingCapacity differs from the configured carrying capacity");
   cudaSetDevice(s->device);
@@ -390,14 +407,19 @@ static int build_day_graph(sampo_sim* s) {
 
 extern "C" int sampo_set_timing(sampo_sim* s, int on) {
   if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
   s->timing = on != 0;
   s->t_count = s->t_scatter = s->t_total = 0;
   s->launches = 0;
   return SAMPO_OK;
 }
 
-extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
-  if (!s) return SAMPO_ERR_ARG;
+// Queues nsteps steps and the copies of their rows on the simulation's
+// stream. With wait, the device status is checked after every chunk of
+// ring - 1 steps (a synchronisation) and the device time is summed per chunk;
+// without, the run is left pending for sampo_sync, which checks the status
+// once and times the whole queue.
+static int queue_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows, bool wait) {
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population: call sampo_init_population or sampo_load_pool");
   if (nsteps == 0) return SAMPO_OK;
   cudaSetDevice(s->device);
@@ -412,9 +434,13 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
   uint32_t done = 0;
   // rows of steps [s->step, s->step + n) are read back in chunks no longer than the ring allows
   const uint32_t chunk_max = s->ring - 1;
-  s->last_run_ms = 0;
-  while (done < nsteps) {
+  if (wait || !s->pending) {
+    s->last_run_ms = 0;
     CK(cudaEventRecord(s->ev[3], s->stream), "event");
+  }
+  s->pending = !wait;
+  while (done < nsteps) {
+    if (wait && done) CK(cudaEventRecord(s->ev[3], s->stream), "event");
     const uint32_t n = std::min(nsteps - done, chunk_max);
     const uint32_t first = s->step;
     if (s->timing) {
@@ -462,6 +488,7 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
     }
     s->step += n;
     done += n;
+    if (!wait) continue;
     int rc = check_device(s);
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev[3], s->ev[2]);
@@ -471,8 +498,35 @@ extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
   return SAMPO_OK;
 }
 
+extern "C" int sampo_sync(sampo_sim* s) {
+  if (!s) return SAMPO_ERR_ARG;
+  if (!s->pending) return SAMPO_OK;
+  s->pending = false;
+  cudaSetDevice(s->device);
+  int rc = check_device(s);  // waits for the queued steps and row copies
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, s->ev[3], s->ev[2]) == cudaSuccess) s->last_run_ms = ms;
+  return rc;
+}
+
+extern "C" int sampo_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
+  if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
+  return queue_run(s, nsteps, rows, true);
+}
+
+extern "C" int sampo_run_async(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows) {
+  if (!s) return SAMPO_ERR_ARG;
+  if (s->timing) {  // per-kernel timing waits for every step
+    SETTLE(s);
+    return queue_run(s, nsteps, rows, true);
+  }
+  return queue_run(s, nsteps, rows, false);
+}
+
 extern "C" int sampo_last_run_ms(sampo_sim* s, double* ms) {
   if (!s || !ms) return SAMPO_ERR_ARG;
+  SETTLE(s);
   *ms = s->last_run_ms;
   return SAMPO_OK;
 }
@@ -489,6 +543,7 @@ extern "C" void sampo_host_free(void* p) {
 
 extern "C" int sampo_flush_l2(sampo_sim* s) {
   if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
   cudaSetDevice(s->device);
   if (!s->flush_buf) {
     int l2 = 0;
@@ -502,6 +557,7 @@ extern "C" int sampo_flush_l2(sampo_sim* s) {
 
 extern "C" int sampo_current_row(sampo_sim* s, sampo_stats_row* row) {
   if (!s || !row) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
   cudaSetDevice(s->device);
   CK(cudaMemcpyAsync(row, s->rows_dev + s->step % s->ring, sizeof(sampo_stats_row), cudaMemcpyDeviceToHost, s->stream), "row");
@@ -517,6 +573,7 @@ extern "C" int sampo_get_step(sampo_sim* s, uint32_t* step) {
 
 extern "C" int sampo_histogram(sampo_sim* s, uint32_t out[100]) {
   if (!s || !out) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
   cudaSetDevice(s->device);
   CK(cudaMemsetAsync(s->hist_dev, 0, 100 * sizeof(uint32_t), s->stream), "histogram");
@@ -529,6 +586,7 @@ extern "C" int sampo_histogram(sampo_sim* s, uint32_t out[100]) {
 
 extern "C" int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_view* v) {
   if (!s || !pop) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
   cudaSetDevice(s->device);
   SimDev h;
@@ -563,6 +621,7 @@ extern "C" int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_v
 //      the n flag bytes (state | isFemale << 3) ----
 extern "C" int sampo_checkpoint_save(sampo_sim* s, const char* path) {
   if (!s || !path) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
   cudaSetDevice(s->device);
   SimDev h;
@@ -605,6 +664,7 @@ extern "C" int sampo_checkpoint_info(const char* path, uint32_t* step, sampo_pop
 
 extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
   if (!s || !path) return SAMPO_ERR_ARG;
+  SETTLE(s);
   CkHeader hd;
   FILE* f = nullptr;
   const std::string err = ck_open(path, hd, &f);
@@ -640,6 +700,7 @@ extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
 
 extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm) {
   if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (!s->have_pop) return fail(s, SAMPO_ERR_STATE, "no population");
   const uint32_t slot = s->step % s->ring;
   if (!s->have_inputs[slot] || s->input_step[slot] != s->step || s->seed_step[slot] != s->step)
@@ -667,6 +728,7 @@ extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_
 
 extern "C" int sampo_set_species(sampo_sim* s, const sampo_species* sp) {
   if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
   if (sp && sampo_species_device(sp) != s->device) return fail(s, SAMPO_ERR_ARG, "species compiled for another device");
   cudaSetDevice(s->device);
   if (s->species == sp) return SAMPO_OK;
@@ -682,6 +744,7 @@ extern "C" int sampo_set_species(sampo_sim* s, const sampo_species* sp) {
 
 extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm) {
   if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
   cudaSetDevice(s->device);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
@@ -705,6 +768,7 @@ extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_
 
 extern "C" int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear) {
   if (!s || !bits) return SAMPO_ERR_ARG;
+  if (s->pending) (void)sampo_sync(s);  // the bits below include the queued steps
   cudaSetDevice(s->device);
   uint32_t st[2];
   CK(cudaMemcpyAsync(st, &s->sim_dev->error, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream), "status");
@@ -720,6 +784,7 @@ extern "C" int sampo_device_status(sampo_sim* s, uint32_t* bits, int clear) {
 
 extern "C" int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launches) {
   if (!s || !out) return SAMPO_ERR_ARG;
+  SETTLE(s);
   out[0] = s->t_count; out[1] = s->t_scatter; out[2] = s->t_total;
   if (launches) *launches = s->launches;
   return SAMPO_OK;

@@ -222,6 +222,16 @@ class Simulation:
         """sampo_run writing rows into caller memory (e.g. page-locked)."""
         self._check(self.lib.sampo_run(self.h, nsteps, rows_ptr))
 
+    def run_async(self, nsteps: int, rows_ptr: int | None = None):
+        """sampo_run_async: queues nsteps steps whose rows land in caller
+        memory (page-locked for a copy that does not block); the memory must
+        stay alive until sync()."""
+        self._check(self.lib.sampo_run_async(self.h, nsteps, rows_ptr))
+
+    def sync(self):
+        """sampo_sync: waits for the queued steps and reports their status."""
+        self._check(self.lib.sampo_sync(self.h))
+
 
 class PinnedArray:
     """numpy array over page-locked host memory (sampo_host_alloc)."""
