@@ -65,7 +65,7 @@ cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
 cudaError_t launch_publish(const KParams& p, int mode, cudaStream_t st) {
   KParams q = p;
   void* args[] = {&q, &mode};
-  return launch(p, KID_PUBLISH, (const void*)k_publish, p.nrep, mode == PUB_REFRESH ? 32 : 128, 0, st, args);
+  return launch(p, KID_PUBLISH, (const void*)k_publish, p.nrep, mode == PUB_REFRESH ? 32 : kPublishThreads, 0, st, args);
 }
 cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev, int age_days_max,
                              uint64_t age_seed, cudaStream_t st) {
@@ -80,7 +80,7 @@ cudaError_t launch_publish_start(const KParams& p, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   int mode = PUB_INITIAL;
   void* args2[] = {&q, &mode};
-  return launch(p, KID_PUBLISH, (const void*)k_publish, 1, 128, 0, st, args2);
+  return launch(p, KID_PUBLISH, (const void*)k_publish, 1, kPublishThreads, 0, st, args2);
 }
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st) {
   KParams q = p;

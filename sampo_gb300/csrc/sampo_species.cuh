@@ -3,7 +3,7 @@
 // the two normal draws and egg laying), behind one interface the model uses.
 //
 // Built in: the reference's shipped properties.h, restated in this file's
-// own code; the per-step functions are evaluated once per step (compute_ctx)
+// own code; the per-step functions are evaluated once per step (make_ctx)
 // and the normal draws are deferred to dense warps (finish_box_muller).
 //
 // SAMPO_USER_SPECIES: the step kernels are compiled at run time by NVRTC

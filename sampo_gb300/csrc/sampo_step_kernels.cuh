@@ -125,25 +125,40 @@ __device__ __forceinline__ bool layout_fits(const uint32_t cnt[8], uint32_t newE
   return tot <= 0xffffffffull && e <= (uint64_t)capacity;
 }
 
-// The constants of step `step` of one simulation starting from `pop`:
-// HybridTaus with z1 and z3 folded per seed slot (include/gpuRand.h:33-50),
-// the species functions of the step's temperature (include/properties.h) and
-// the biomass of the pool (kernel/killAgents.cl:42-43). The larval mortality
-// table is filled separately (k_publish).
-__device__ void compute_ctx(const RepParams& rp, const sampo_population& pop, uint32_t step, StepCtx& c) {
-  c.larvaHMR = rp.sim->larvaHMR;
+// The inputs of step `step` of one replicate (its ring slot).
+struct CtxInputs {
+  sampo_seeds sd[4];
+  sampo_environment env;
+  float T;
+  uint32_t wt;
+};
+__device__ __forceinline__ void load_ctx_inputs(const RepParams& rp, uint32_t step, CtxInputs& in) {
   const uint32_t i = step % rp.ring;
-  const sampo_seeds* sd = rp.seeds + (size_t)i * 4;
+#pragma unroll
+  for (int k = 0; k < 4; k++) in.sd[k] = rp.seeds[(size_t)i * 4 + k];
+  in.env = rp.env[i];
+  in.T = rp.T[i];
+  in.wt = rp.wt[i];
+}
+
+// The constants of a step of one simulation starting from `pop`, from the
+// step's inputs: HybridTaus with z1 and z3 folded per seed slot
+// (include/gpuRand.h:33-50), the species functions of the step's temperature
+// (include/properties.h) and the biomass of the pool
+// (kernel/killAgents.cl:42-43). The larval mortality table is filled
+// separately (k_publish).
+__device__ void make_ctx(const CtxInputs& in, const float* larvaHMR, const sampo_population& pop, StepCtx& c) {
+  c.larvaHMR = larvaHMR;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    c.rng_c13[k] = taus_step(sd[k].z1 + 128u, 13, 19, 12, 4294967294u) ^ taus_step(sd[k].z3 + 128u, 3, 11, 17, 4294967280u);
-    c.rng_z2[k] = sd[k].z2 + 128u;
-    c.rng_z4[k] = sd[k].z4;
+    c.rng_c13[k] = taus_step(in.sd[k].z1 + 128u, 13, 19, 12, 4294967294u) ^ taus_step(in.sd[k].z3 + 128u, 3, 11, 17, 4294967280u);
+    c.rng_z2[k] = in.sd[k].z2 + 128u;
+    c.rng_z4[k] = in.sd[k].z4;
   }
-  c.env = rp.env[i];
-  const float T = rp.T[i];
+  c.env = in.env;
+  const float T = in.T;
   c.T = T;
-  c.wt = rp.wt[i];
+  c.wt = in.wt;
   c.totalBiomass = pop.numLarvae1DayEquiv + pop.r[EGG].end + (pop.r[PUPA].end - pop.r[PUPA].start);
   species_step(T, c.wt, c);
   c.sporoOn = T > 16.0f;                                             // kernel/updateAgents.cl:69-70
@@ -519,7 +534,9 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
 // mode PUB_REFRESH only recomputes the input-dependent step constants (the
 // inputs of the coming step may have been written after its publish).
 // ------------------------------------------------------------------------
-__global__ void k_publish(KParams p, int mode) {
+// warp 0 publishes; warps 1-4 fill the 100 entries of the larval table at once
+constexpr int kPublishThreads = 160;
+__global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode) {
   __shared__ uint32_t s_go, s_l1, s_dmin, s_dmax;
   __shared__ float s_cc;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -535,74 +552,112 @@ __global__ void k_publish(KParams p, int mode) {
     __syncwarp();
   }
   if (mode == PUB_REFRESH) {
-    if (threadIdx.x == 0 && sim->active) compute_ctx(rp, sim->pop, sim->step, sim->ctx);
+    if (threadIdx.x == 0 && sim->active) {
+      CtxInputs in;
+      load_ctx_inputs(rp, sim->step, in);
+      StepCtx c;
+      make_ctx(in, sim->larvaHMR, sim->pop, c);
+      sim->ctx = c;
+    }
     return;
   }
   const bool after_step = mode == PUB_AFTER_STEP;
+  // Thread 0 reads all it needs before its first store (a store that may
+  // alias a later load would hold that load back until the store is issued,
+  // turning the reads into a chain), hands the larval table's inputs to the
+  // other warps and does its writes while they fill the table.
+  sampo_population np;
+  sampo_bites_cycles bnc;
+  CtxInputs in;
+  uint32_t step = 0, stop = 0, epoch = 0, cur = 0, warn = 0;
+  bool relayout = false, shared_end_warn = false;
   if (threadIdx.x == 0) {
-    s_go = sim->active;
-    if (s_go) {
-      sampo_population np = sim->pop;
-      if (after_step) {
-        uint32_t cnt[8];
-        for (int k = 0; k < 8; k++) cnt[k] = sim->cnt[k];
-        const uint32_t ne = sim->newEggs;
-        // the reference's shared empty initial ranges (src/abms.c:204-219) make
-        // oldToNewAgents read one prefix-sum entry for several range ends
-        bool shared_end = false;
-        uint32_t moved = 0;
-        for (int k = 1; k < 8; k++) {
-          shared_end |= np.r[k].end == np.r[k - 1].end;
-          moved += cnt[k];
-        }
-        if (shared_end && moved) sim->warn |= SAMPO_DEV_WARN_REF_LAYOUT;
-        if (layout_fits(cnt, ne, sim->capacity)) {  // else the scatter pass flagged the capacity error
-          uint32_t base[8];
-          next_layout(cnt, ne, np, base);
-          sim->cur ^= 1u;
-        }
-        sim->step += 1u;
-        sim->epoch += 1u;
-        for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
-        sim->newEggs = 0;
-        sim->bnc.numCyclesReported = sim->acc_bnc[0];
-        sim->bnc.sumCyclesReported = sim->acc_bnc[1];
-        sim->bnc.numBitesReported = sim->acc_bnc[2];
-        sim->bnc.numInfectBitesReported = sim->acc_bnc[3];
+    const uint32_t active = sim->active;
+    np = sim->pop;
+    bnc = sim->bnc;
+    uint32_t cnt[8], abnc[4];
+#pragma unroll
+    for (int k = 0; k < 8; k++) cnt[k] = sim->cnt[k];
+#pragma unroll
+    for (int q = 0; q < 4; q++) abnc[q] = sim->acc_bnc[q];
+    const uint32_t ne = sim->newEggs, capacity = sim->capacity;
+    const uint32_t aL1 = sim->acc_L1de, afem = sim->acc_fem, ainf = sim->acc_inf;
+    const uint32_t dmin = sim->acc_dmin, dmax = sim->acc_dmax;
+    const float cc = sim->cc;
+    step = sim->step;
+    stop = sim->stop_step;
+    epoch = sim->epoch;
+    cur = sim->cur;
+    warn = sim->warn;
+    if (after_step) {
+      // the reference's shared empty initial ranges (src/abms.c:204-219) make
+      // oldToNewAgents read one prefix-sum entry for several range ends
+      bool shared_end = false;
+      uint32_t moved = 0;
+      for (int k = 1; k < 8; k++) {
+        shared_end |= np.r[k].end == np.r[k - 1].end;
+        moved += cnt[k];
       }
-      np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? sim->acc_L1de : 0u;  // kernel/calcL1de.cl:259-280
-      np.numFemale = sim->acc_fem;
-      np.numPotentiallyInfective = sim->acc_inf;
-      sim->pop = np;
-      const uint32_t step = sim->step;
-      sampo_stats_row row;
-      row.pop = np;
-      row.bnc = sim->bnc;
-      rp.rows[step % rp.ring] = row;
-      s_l1 = np.numLarvae1DayEquiv;
-      s_dmin = sim->acc_dmin;
-      s_dmax = sim->acc_dmax;
-      s_cc = sim->cc;
-      sim->acc_L1de = 0; sim->acc_fem = 0; sim->acc_inf = 0;
-      sim->acc_dmin = 0xffffffffu; sim->acc_dmax = 0;
-      sim->acc_bnc[0] = sim->acc_bnc[1] = sim->acc_bnc[2] = sim->acc_bnc[3] = 0;
-      compute_ctx(rp, np, step, sim->ctx);
-      if (step >= sim->stop_step) sim->active = 0;
+      shared_end_warn = shared_end && moved;
+      if (layout_fits(cnt, ne, capacity)) {  // else the scatter pass flagged the capacity error
+        uint32_t base[8];
+        next_layout(cnt, ne, np, base);
+        relayout = true;
+      }
+      step += 1u;
+      bnc.numCyclesReported = abnc[0];
+      bnc.sumCyclesReported = abnc[1];
+      bnc.numBitesReported = abnc[2];
+      bnc.numInfectBitesReported = abnc[3];
     }
+    np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? aL1 : 0u;  // kernel/calcL1de.cl:259-280
+    np.numFemale = afem;
+    np.numPotentiallyInfective = ainf;
+    if (active) load_ctx_inputs(rp, step, in);
+    s_go = active;
+    s_l1 = np.numLarvae1DayEquiv;
+    s_dmin = dmin;
+    s_dmax = dmax;
+    s_cc = cc;
   }
   __syncthreads();
   if (!s_go) return;
-  for (int d = threadIdx.x; d < 100; d += blockDim.x) {
-    float hmr = SAMPO_NAN_F;
-    if ((uint32_t)d >= s_dmin && (uint32_t)d <= s_dmax) {
-      // kernel/killAgents.cl:117-125
-      float dmr = 0.1f * sampo_expf((float)s_l1 / ((float)(uint32_t)d * s_cc * 1.0f));
-      dmr = sampo_fminf(dmr, 0.8f);
-      float dsr = 1.0f - dmr;
-      float hsr = sampo_powf(dsr, 1.0f / 24.0f);
-      hmr = 1.0f - hsr;
+  if (threadIdx.x == 0) {
+    if (shared_end_warn) sim->warn = warn | SAMPO_DEV_WARN_REF_LAYOUT;
+    if (after_step) {
+      if (relayout) sim->cur = cur ^ 1u;
+      sim->step = step;
+      sim->epoch = epoch + 1u;
+#pragma unroll
+      for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
+      sim->newEggs = 0;
+      sim->bnc = bnc;
     }
-    sim->larvaHMR[d] = hmr;
+    sim->pop = np;
+    sampo_stats_row row;
+    row.pop = np;
+    row.bnc = bnc;
+    rp.rows[step % rp.ring] = row;
+    sim->acc_L1de = 0; sim->acc_fem = 0; sim->acc_inf = 0;
+    sim->acc_dmin = 0xffffffffu; sim->acc_dmax = 0;
+    sim->acc_bnc[0] = sim->acc_bnc[1] = sim->acc_bnc[2] = sim->acc_bnc[3] = 0;
+    StepCtx c;
+    make_ctx(in, sim->larvaHMR, np, c);
+    sim->ctx = c;
+    if (step >= stop) sim->active = 0;
+  } else if (threadIdx.x >= 32) {
+    for (int d = threadIdx.x - 32; d < 100; d += blockDim.x - 32) {
+      float hmr = SAMPO_NAN_F;
+      if ((uint32_t)d >= s_dmin && (uint32_t)d <= s_dmax) {
+        // kernel/killAgents.cl:117-125
+        float dmr = 0.1f * sampo_expf((float)s_l1 / ((float)(uint32_t)d * s_cc * 1.0f));
+        dmr = sampo_fminf(dmr, 0.8f);
+        float dsr = 1.0f - dmr;
+        float hsr = sampo_powf(dsr, 1.0f / 24.0f);
+        hmr = 1.0f - hsr;
+      }
+      sim->larvaHMR[d] = hmr;
+    }
   }
 }
 
