@@ -278,7 +278,19 @@ def gpu_arm(args, wl, rank, world, device):
     for h in (hT, hE, hS, hR):
         h.free()
     sim.close()
-    return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(),
+    # each pass against the peak, and the whole step as the day graphs run it
+    step_ms_graph = ms / (24 * args.steps)
+    step_bytes = float(count_bytes.mean() + scatter_bytes.mean())
+
+    def pass_line(nbytes, t_ms):
+        gbs = nbytes / (t_ms * 1e-3) / 1e9
+        return {"bytes_per_launch": nbytes, "ms_per_launch": t_ms, "gbs": gbs, "frac": gbs / peak}
+    passes = {
+        "k_count: decisions + in-tile scan (8-13 B read per live agent)": pass_line(float(count_bytes.mean()), count_ms),
+        "k_scatter: update + cross-tile scan + compaction (37 B read + 37 B written per agent)": pass_line(float(scatter_bytes.mean()), scatter_ms),
+        "hourly step in the day graphs (both passes + k_publish)": pass_line(step_bytes, step_ms_graph),
+    }
+    return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(), passes=passes,
                 gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, publish_ms=publish_ms, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
                 count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned)
@@ -571,7 +583,8 @@ def main():
                      "peak_kind": r["peak_kind"], "scatter_ms_per_launch": r["scatter_ms"], "count_ms_per_launch": r["count_ms"],
                      "publish_and_gaps_ms_per_step": r["publish_ms"],
                      "count_pass_gbs": r["count_gbs"],
-                     "algorithmic_bytes": "k_scatter: 37 B read per live agent + 37 B written per agent of the next pool"},
+                     "algorithmic_bytes": "k_scatter: 37 B read per live agent + 37 B written per agent of the next pool",
+                     "passes": r["passes"]},
         "e2e": {"value": e2e_days / e2e_max, "unit": "agent-days/s", "h2d_bytes_per_step": 24 * (4 + 24 + 4 + 64),
                 "d2h_bytes_per_step": 24 * 92},
         "gpu_launches": r["gpu_launches"] * world,
