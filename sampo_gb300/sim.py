@@ -252,12 +252,6 @@ class PinnedArray:
             self.lib.sampo_host_free(self.p)
             self.p = None
 
-    @property
-    def step_index(self) -> int:
-        s = C.c_uint32()
-        self._check(self.lib.sampo_get_step(self.h, C.byref(s)))
-        return s.value
-
 
 # ---------------------------------------------------------------------------
 # printStats (src/abms.c:67-81) and calcStats's derived numbers (:287-302)

@@ -5,7 +5,7 @@ admitted and whichever slot it holds."""
 import numpy as np
 import pytest
 
-from sampo_gb300.batch import NEVER, ReplicateSpec
+from sampo_gb300.batch import ReplicateSpec
 
 SPECS = [
     ReplicateSpec(initial=600, seed=11, mean_t=27.0, amplitude=3.0, rain_mean=4.0, days=3, capacity=40000),

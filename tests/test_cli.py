@@ -7,7 +7,7 @@ import subprocess
 
 import pytest
 
-from tests.conftest import REPO, load_golden
+from tests.conftest import load_golden
 from tests.golden.cases import CASES, make_case_inputs
 
 

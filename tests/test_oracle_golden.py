@@ -1,7 +1,6 @@
 """The CPU oracle against the golden traces made by the reference's own code
 (ref-as-C, tests/golden/make_golden.py): every stats line, the pool hash
 after every step, the final ranges and histogram.txt must be identical."""
-import os
 import subprocess
 
 import pytest

@@ -8,10 +8,9 @@ import os
 import shutil
 import subprocess
 
-import numpy as np
 import pytest
 
-from tests.conftest import REPO, load_golden
+from tests.conftest import load_golden
 from tests.golden.cases import SPECIES_CASES, SPECIES_DIR, make_case_inputs
 
 HOT = os.path.join(SPECIES_DIR, "hot_species.h")
