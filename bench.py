@@ -43,11 +43,11 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 WORKLOADS = {
-    # BASELINE config 1: the headline
+    # the headline workload: a large plain run
     "plain-large": dict(name="plain large run: 1e6 agents (egg/larva/pupa/adult 40/30/10/20), 2^27 slots, 730 days, seasonal weather seed 2",
                         counts=(400_000, 300_000, 100_000, 200_000), capacity=1 << 27, days=730, seed=2,
                         cc=5_000_000.0, weather=("seasonal", 2, 26.0, 4.0, 0.5)),
-    # BASELINE config 2: the bandwidth-roofline run
+    # the bandwidth-roofline run
     "roofline": dict(name="roofline run: 5e7 preloaded agents (uniform over 4 stages, 50/50 gender), 1e8 slots, 28 C constant, 90 days, seed 3",
                      counts=(12_500_000,) * 4, capacity=100_000_000, days=90, seed=3, cc=3_000_000.0,
                      weather=("constant", 28.0)),
@@ -55,7 +55,7 @@ WORKLOADS = {
     "roofline-5m": dict(name="roofline mix at 5e6 agents: preloaded uniform over 4 stages, 50/50 gender, 1e7 slots, 28 C constant, seed 3",
                         counts=(1_250_000,) * 4, capacity=10_000_000, days=90, seed=3, cc=300_000.0,
                         weather=("constant", 28.0)),
-    # BASELINE config 0 with its mixed-stage analogue off: the CPU-runnable case
+    # the CPU-runnable plain case: eggs only
     "plain-small": dict(name="plain single run: 10,000 eggs aged U{0..3} days, 2^20 slots, 365 days, seed 1",
                         eggs=10_000, capacity=1 << 20, days=365, seed=1, cc=50_000.0,
                         weather=("seasonal", 1, 26.0, 4.0, 0.5)),
@@ -367,7 +367,7 @@ def all_reduce(vals, op):
 
 
 def ensemble_arm(args):
-    """BASELINE config 3 over a window of days: batched vs one at a time."""
+    """The 512-replicate ensemble over a window of days: batched vs one at a time."""
     from sampo_gb300.batch import Batch, ensemble_specs
     from sampo_gb300.sim import Simulation, rand_state, seed_stream
     days = args.warmup + args.steps
@@ -459,7 +459,7 @@ def ensemble_arm(args):
 
 
 def served_arm(args):
-    """BASELINE config 4, a bounded number of requests per rate."""
+    """The served request stream, a bounded number of requests per rate."""
     from sampo_gb300.serve import Server, latency_summary, one_at_a_time, request_stream
     rates = [float(x) for x in args.rates.split(",")]
     out = {"metric": "sims/s", "unit": "sims/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
