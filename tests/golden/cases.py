@@ -14,8 +14,8 @@ from sampo_gb300 import inputs  # noqa: E402
 CASES = {
     # The CPU-runnable benchmark workload: 10,000 eggs aged U{0..3} days,
     # seasonal weather (26 +- 4 C, noise 0.5), 365 days, seed 1, cc = 5 x 10,000.
-    "config0": dict(seed=1, initial=10000, cc=50000.0, steps=8760, age_days=3, age_seed=1,
-                    weather=("seasonal", 365, 1, 26.0, 4.0, 0.5), interventions=None),
+    "eggs_1e4_year": dict(seed=1, initial=10000, cc=50000.0, steps=8760, age_days=3, age_seed=1,
+                          weather=("seasonal", 365, 1, 26.0, 4.0, 0.5), interventions=None),
     # All four interventions switched on and off every 10 days.
     "interventions": dict(seed=3, initial=2000, cc=10000.0, steps=1440, age_days=3, age_seed=3,
                           weather=("seasonal", 60, 5, 27.0, 3.0, 0.5), interventions="alternating"),

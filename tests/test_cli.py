@@ -31,7 +31,7 @@ def test_cli_arguments_without_gpu(cli, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name,per_step", [("config0", False), ("interventions", True), ("reference_default", False)])
+@pytest.mark.parametrize("name,per_step", [("eggs_1e4_year", False), ("interventions", True), ("reference_default", False)])
 def test_cli_output_matches_reference(gpu_ready, cli, tmp_path, name, per_step):
     c = CASES[name]
     g = load_golden(name)
