@@ -1142,7 +1142,9 @@ __global__ void k_init_eggs(KParams p, uint32_t n, float T0, const sampo_seeds* 
   }
   __syncthreads();
   const DevPool dst = p.reps[0].pool[0];
-  for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+  // 64-bit counters: a bound within one grid stride of 2^32 must not wrap
+  for (uint64_t i64 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i64 < n; i64 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t id = (uint32_t)i64;
     Rec a;
     new_egg(c, id, a);
     if (age_days_max >= 0) {
@@ -1184,7 +1186,8 @@ __global__ void k_pool_stats(KParams p) {
   const DevPool src = p.reps[0].pool[sim->cur];
   uint32_t l1 = 0, fem = 0, inf = 0, dmin = 0xffffffffu, dmax = 0;
   const uint32_t end = pop.r[GRAVID].end;
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < end; g += gridDim.x * blockDim.x) {
+  for (uint64_t g64 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g64 < end; g64 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t g = (uint32_t)g64;
     int rg = range_of(pop, g);
     if (rg == LARVA) {
       float age = src.age[g];
@@ -1219,9 +1222,9 @@ __global__ void k_histogram(KParams p, uint32_t* hist) {
   const DevPool src = p.reps[0].pool[sim->cur];
   const uint32_t lo = pop.r[IMMATURE].start, hi = pop.r[GRAVID].end;
   const uint32_t span = hi > lo ? hi - lo : 0u;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < span; base += stride) {
-    const uint32_t g = lo + base + threadIdx.x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < span; base += stride) {  // warp-uniform
+    const uint32_t g = lo + (uint32_t)base + threadIdx.x;
     int rg = (base + threadIdx.x < span) ? range_of(pop, g) : -1;
     uint32_t bin = 0xffffffffu;
     if (rg >= IMMATURE) {
@@ -1238,7 +1241,8 @@ __global__ void k_histogram(KParams p, uint32_t* hist) {
 
 // Diagnostic: the model's transcendental definitions evaluated on the device.
 __global__ void k_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (uint64_t i64 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i64 < n; i64 += (uint64_t)gridDim.x * blockDim.x) {
+    const size_t i = (size_t)i64;
     float v = 0.0f;
     switch (fn) {
       case 0: v = sampo_expf(x[i]); break;
