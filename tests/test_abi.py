@@ -35,6 +35,8 @@ def test_struct_layouts(sampo_lib):
 def test_errors_without_handle(sampo_lib):
     assert sampo_lib.sampo_create(None, None) == -1
     assert sampo_lib.sampo_run(None, 1, None) == -1
+    assert sampo_lib.sampo_run_async(None, 1, None) == -1
+    assert sampo_lib.sampo_sync(None) == -1
     assert sampo_lib.sampo_destroy(None) == 0
 
 
