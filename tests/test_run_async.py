@@ -72,3 +72,26 @@ def test_queued_capacity_error_surfaces_at_sync(gpu_ready, tmp_path):
         sim.sync()
     assert e.value.code == -3
     sim.close()
+
+
+def test_step_after_queue(gpu_ready, oracle_mod, tmp_path):
+    """sampo_step with explicit inputs straight after a queued run (no sync)
+    continues from the queued steps: its row and the pool equal sampo_run's
+    over the same steps."""
+    from sampo_gb300.sim import seed_stream
+    n, k = 200, 150
+    ref = _sim("small_b", tmp_path, n, n + 1)
+    rows_ref = ref.run(n)
+    pop_ref, pool_ref = ref.read_pool()
+    ref.close()
+    c, T, env = _inputs("small_b", tmp_path, n)
+    _, seeds = seed_stream(c["seed"], n)
+    sim = _sim("small_b", tmp_path, n, n + 1)
+    sim.run_async(k)
+    for i in range(k, n):
+        row = sim.step(env[i], T[i], i % 24, seeds[i])
+        assert row.tobytes() == rows_ref[i].tobytes(), f"step {i}"
+    assert sim.get_step() == n
+    pop, pool = sim.read_pool()
+    assert oracle_mod.pool_hash(pop["ranges"], pool) == oracle_mod.pool_hash(pop_ref["ranges"], pool_ref)
+    sim.close()
