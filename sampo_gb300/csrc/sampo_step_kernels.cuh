@@ -361,7 +361,11 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     t_next = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket1, 1u);
     s_tick[sidx] = t;
     if (t >= total) return;
-    const uint32_t r = find_rep(s_pre, p.nrep, t);
+    // tickets run from the last tile down: the scatter pass then starts on
+    // the tiles whose decision columns and prefix tables this pass touched
+    // last, while they are still in L2
+    const uint32_t tile = total - 1u - t;
+    const uint32_t r = find_rep(s_pre, p.nrep, tile);
     CountStage& cs = s_cs[sidx];
     if (cs.rep != r) {
       const RepParams& rp = p.reps[r];
@@ -374,7 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
       cs.tilePre = rp.tilePre;
       cs.larv = sim->ctx.env.larvacideValue > 0.0f;
     }
-    cs.lt = t - s_pre[r];
+    cs.lt = tile - s_pre[r];
     const uint32_t lo = cs.lt * kTile;
     fence_proxy_async();  // the stage was last read through the generic proxy
     issue_count_tile(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, min((uint32_t)kTile, cs.end - lo), cs.larv != 0);
