@@ -9,6 +9,8 @@ REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 if REPO not in sys.path:
     sys.path.insert(0, REPO)
 
+import numpy as np  # noqa: E402
+
 from sampo_gb300 import inputs  # noqa: E402
 
 CASES = {
@@ -23,6 +25,13 @@ CASES = {
     # no-intervention files (regenerated byte for byte), its initial layout.
     "reference_default": dict(seed=11, initial=32000, cc=160000.0, steps=1200, age_days=-1, age_seed=0,
                               weather=("constant30", 50), interventions=None),
+    # Constant-temperature segments across the species functions' edges, after
+    # a warm start that brings bitten adults: 16.0 C (sporogonic development
+    # off, the test is T > 16), 16.5 C, 8.0 C (below the devRates clamp at
+    # 12 C), exactly 12.0 C, 43.9 C (the last devRates entry), then 30 C.
+    "temperature_edges": dict(seed=21, initial=2000, cc=10000.0, steps=960, age_days=3, age_seed=6,
+                              weather=("segments", ((18, 28.0), (4, 16.0), (4, 16.5), (4, 8.0), (2, 12.0),
+                                                    (3, 43.9), (5, 30.0))), interventions=None),
     # Small, quick cases for the CPU suite.
     "small_a": dict(seed=7, initial=600, cc=3000.0, steps=720, age_days=3, age_seed=9,
                     weather=("seasonal", 30, 2, 25.0, 5.0, 0.5), interventions=None),
@@ -49,6 +58,12 @@ def make_case_inputs(name: str, directory: str):
     if w[0] == "seasonal":
         _, days, wseed, mean, amp, sd = w
         weather = inputs.seasonal_weather(days, wseed, mean, amp, sd)
+        tp, ep = inputs.write_inputs(directory, weather,
+                                     inputs.alternating_interventions() if c["interventions"] == "alternating" else None)
+    elif w[0] == "segments":
+        temps = [t for days, t in w[1] for _ in range(days)]
+        weather = inputs.DailyWeather(np.array(temps, dtype=np.float64), np.full(len(temps), 75.0),
+                                      np.full(len(temps), 4.0))
         tp, ep = inputs.write_inputs(directory, weather,
                                      inputs.alternating_interventions() if c["interventions"] == "alternating" else None)
     elif w[0] == "constant30":

@@ -107,7 +107,8 @@ def test_step_by_step_against_oracle(gpu_ready, oracle_mod, tmp_path, name, n):
     sim.close()
 
 
-@pytest.mark.parametrize("name", ["small_a", "small_b", "interventions", "reference_default", "eggs_1e4_year"])
+@pytest.mark.parametrize("name", ["small_a", "small_b", "interventions", "reference_default", "eggs_1e4_year",
+                                  "temperature_edges"])
 def test_run_matches_reference_golden(gpu_ready, oracle_mod, tmp_path, name):
     """sampo_run (CUDA-graph days) against the reference's own trace: every
     printStats line, the pool hash at day boundaries, ranges, histogram.txt."""

@@ -10,7 +10,7 @@ from tests.golden.cases import CASES, make_case_inputs
 
 # (case, steps): None = the whole case; a number = that prefix (CPU budget)
 RUNS = [("small_a", None), ("small_b", None), ("interventions", None), ("reference_default", 600),
-        ("eggs_1e4_year", 1000)]
+        ("eggs_1e4_year", 1000), ("temperature_edges", None)]
 
 
 @pytest.mark.parametrize("name,steps", RUNS)
