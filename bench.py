@@ -381,29 +381,43 @@ def ensemble_arm(args):
         prep.append((T, env, init, seeds))
     ring = days * 24 + 1
     # ---- batched (each replicate draws its seeds on the device) ----
-    t0 = time.perf_counter()
+    # e2e: the whole batched run through the public API, timed on the host:
+    # slots taken, every replicate's inputs for all its days up from
+    # page-locked buffers, initial populations, warm-up days, grid tuning, the
+    # timed days, and every replicate's stats rows back. value: the device time
+    # of the timed days alone (CUDA events)
+    from sampo_gb300._lib import ENV_DTYPE, ROW_DTYPE
+    from sampo_gb300.sim import PinnedArray
+    nsteps = 24 * days
+    hT, hE = PinnedArray((nsteps,), np.float32), PinnedArray((nsteps,), ENV_DTYPE)
+    hR = PinnedArray((nsteps + 1,), ROW_DTYPE)
+    t_all = time.perf_counter()
     b = Batch(n, ring)
     slots = []
     for s, (T, env, init, seeds) in zip(specs, prep):
         slot = b.add(s.capacity, s.cc, stop_step=s.steps)
-        b.set_inputs(slot, T, env)
+        hT.a[:] = T
+        hE.a[:] = env
+        b._check(b.lib.sampo_batch_set_inputs(b.h, slot, 0, hT.p, hE.p, nsteps))
         init, stream = rand_state(s.seed)
         b.init_population(slot, s.initial, init, age_days_max=s.age_days_max, age_seed=s.seed)
         b.seed_stream(slot, stream)
         slots.append(slot)
     b.sync()
-    setup_batch = time.perf_counter() - t0
+    setup_batch = time.perf_counter() - t_all
     b.run(24 * args.warmup)
     tuned = b.autotune()
     with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
         b.run(24 * args.steps)
-        wall_batch = time.perf_counter() - t0
     dev_batch = b.last_run_ms() / 1e3
     rows_b, bits_b = [], []
-    for slot, s in zip(slots, specs):
-        rows_b.append(b.rows(slot, 0, s.steps + 1))
+    for slot in slots:
+        b._check(b.lib.sampo_batch_rows(b.h, slot, 0, nsteps + 1, hR.p))
+        rows_b.append(hR.a.copy())
         bits_b.append(b.state(slot)[2])
+    wall_e2e = time.perf_counter() - t_all
+    for h in (hT, hE, hR):
+        h.free()
     b.close()
     # ---- one at a time through the plain path ----
     from sampo_gb300._lib import SampoError
@@ -443,7 +457,7 @@ def ensemble_arm(args):
                    "ctas_per_sm": {"count": tuned[0], "scatter": tuned[1], "picked_by": "sampo_batch_autotune"},
                    "l2": "pools far larger than L2"},
         "batched": {"replicate_days_per_s": value, "sims_per_s_365d_equiv": value / 365.0,
-                    "agent_days_per_s": live_sum / 24.0 / dev_batch, "wall_s": wall_batch, "device_s": dev_batch,
+                    "agent_days_per_s": live_sum / 24.0 / dev_batch, "device_s": dev_batch,
                     "setup_s": setup_batch},
         "one_at_a_time": {"replicate_days_per_s": n * args.steps / plain_run_s, "run_s": plain_run_s,
                           "with_setup_s": plain_total_s},
@@ -451,8 +465,9 @@ def ensemble_arm(args):
         "speedup_incl_setup": plain_total_s / (dev_batch + setup_batch),
         "bit_exact_replicates": f"{exact}/{n}",
         "replicates_out_of_capacity": overflow,
-        "e2e": {"value": n * args.steps / wall_batch, "unit": "replicate-days/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
+        "e2e": {"value": n * days / wall_e2e, "unit": "replicate-days/s",
+                "h2d_bytes_per_step": n * 24 * (4 + 24 + 4), "d2h_bytes_per_step": n * 24 * 92,
+                "window": f"the whole batched run: setup, days 0..{days}, grid tuning, rows read back"},
         "gpu_launches": 1 + 73 * args.steps,
         "clocks": clk.summary(),
     }
@@ -495,13 +510,20 @@ def served_arm(args):
             "bit_exact": f"{exact}/{len(res)}", "peak_resident": srv.peak_resident,
             "peak_hbm_gb": srv.peak_bytes / 1e9, "days_stepped": srv.days_run, "wall_s": time.perf_counter() - t0}
     first = per_rate[str(rates[0])]
+    # host traffic per request (the line's step): its inputs up at admission
+    # (temperature, environment row, world time per hourly step) and its stats
+    # rows and histogram down at completion
+    hours = np.array([r.spec.steps for r in request_stream(args.requests, rates[0], seed=7,
+                                                          days_range=(args.min_days, args.max_days))], dtype=np.float64)
     out.update({"value": first["sims_per_s"], "ms_per_step": None,
                 "config": {"workload": f"served stream: {args.requests} requests per rate, Poisson arrivals, initial eggs "
                                        f"log-uniform in [1e2, 5e6], horizons U{{{args.min_days}..{args.max_days}}} days, "
                                        f"own seed and weather each, {args.budget_gb:g} GB HBM budget, capacity 96 x initial + 65536",
                            "rates_per_s": rates},
                 "per_rate": per_rate,
-                "e2e": {"value": first["sims_per_s"], "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+                "e2e": {"value": first["sims_per_s"], "unit": "sims/s", "h2d_bytes_per_step": float(hours.mean() * (4 + 24 + 4)),
+                        "d2h_bytes_per_step": float((hours.mean() + 1) * 92 + 400),
+                        "note": "value is already end to end: wall clock through sampo_gb300.serve.Server"}})
     return out
 
 
