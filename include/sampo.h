@@ -264,12 +264,15 @@ int sampo_read_environment_file(const char* path, sampo_environment* out, uint32
  * isFemale << 3. pop_in: ranges of `in` (stats are recomputed). Writes the
  * next pool into `out`; *row = stats at the start of the step (bnc zero),
  * *pop_out = ranges and stats of `out`, *bnc_out = this step's counters.
- * Capacities above SAMPO_NOALLOC_MAX_SLOTS return SAMPO_ERR_ARG.
+ * Capacities above SAMPO_NOALLOC_MAX_SLOTS, and `in` and `out` columns that
+ * overlap, return SAMPO_ERR_ARG.
  * The first call on a device resolves the scratch array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress) with that device current.
  * All calls share the one array and it keeps the last call's contents:
  * calls that overlap on the GPU (other threads, other streams) race. The
- * call is synchronous on `stream` (NULL = the default stream). */
+ * call is synchronous: it copies the step's inputs from host memory and
+ * waits on `stream` (NULL = the default stream) for the results, so it
+ * must not be made on a stream that is capturing a graph (SAMPO_ERR_STATE). */
 #define SAMPO_NOALLOC_MAX_SLOTS (1u << 24)
 typedef struct {
   float* ageInHours; float* hoursInState; float* delay; float* cumulativeSporogonicDevelopment;

@@ -3,8 +3,9 @@
   oracle/_build/liboracle.so   the C restatement, for ctypes (tests, bench)
   oracle/_build/sampo_oracle   its command-line driver (abms.c's I/O)
   oracle/_ref/sampo_ref        ref-as-C, only where the reference checkout
-                               exists ($SAMPO_REFERENCE, default
-                               /root/reference); built by ref_build/Makefile
+                               exists ($SAMPO_REFERENCE, else a checkout
+                               named "reference" beside this repository);
+                               built by ref_build/Makefile
 """
 from __future__ import annotations
 
@@ -36,8 +37,14 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+def reference_dir() -> str:
+    """The reference checkout: $SAMPO_REFERENCE, else a directory named
+    "reference" beside this repository."""
+    return os.environ.get("SAMPO_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
 def build_ref() -> str | None:
-    ref = os.environ.get("SAMPO_REFERENCE", "/root/reference")
+    ref = reference_dir()
     if not os.path.isdir(os.path.join(ref, "kernel")):
         return None
     subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref_build"), f"REF={ref}"], check=True)

@@ -318,11 +318,7 @@ extern "C" int sampo_init_population(sampo_sim* s, uint32_t n, const sampo_seeds
 extern "C" int sampo_load_pool(sampo_sim* s, const sampo_population* pop, const sampo_pool_view* v) {
   if (!s || !pop || !v) return SAMPO_ERR_ARG;
   SETTLE(s);
-  if (pop->r[0].start != 0) return fail(s, SAMPO_ERR_ARG, "the egg range must start at slot 0");
-  for (int k = 0; k < 8; k++) {
-    if (pop->r[k].end < pop->r[k].start) return fail(s, SAMPO_ERR_ARG, "range end before start");
-    if (k > 0 && pop->r[k].start <= pop->r[k - 1].end) return fail(s, SAMPO_ERR_ARG, "ranges must be ordered with a gap");
-  }
+  if (const char* why = ranges_error(*pop, UINT64_MAX)) return fail(s, SAMPO_ERR_ARG, why);
   const uint32_t n = pop->r[7].end;
   if ((uint64_t)n > s->capacity) return fail(s, SAMPO_ERR_CAPACITY, "pool exceeds the capacity");
   cudaSetDevice(s->device);
@@ -671,7 +667,18 @@ extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
   if (!err.empty()) return fail(s, SAMPO_ERR_IO, err);
   if (hd.cc != s->cc) { fclose(f); return fail(s, SAMPO_ERR_ARG, "checkpoint carrying capacity differs from the handle's"); }
   if ((uint64_t)hd.n > s->capacity) { fclose(f); return fail(s, SAMPO_ERR_CAPACITY, "checkpoint pool exceeds the capacity"); }
+  if (const char* why = ranges_error(hd.pop, s->capacity)) {
+    fclose(f);
+    return fail(s, SAMPO_ERR_IO, std::string("inconsistent checkpoint (") + why + "): " + path);
+  }
   cudaSetDevice(s->device);
+  // the columns are copied on the legacy stream: nothing of this handle may
+  // still run on its own stream
+  const cudaError_t se = cudaStreamSynchronize(s->stream);
+  if (se != cudaSuccess) {
+    fclose(f);
+    return cuda_fail(s, se, "checkpoint");
+  }
   const std::string rerr = ck_read_pool(f, hd, s->pool[0]);
   if (!rerr.empty()) return fail(s, SAMPO_ERR_IO, rerr + ": " + path);
   // the state as a step boundary left it: step, ranges, the counters the next

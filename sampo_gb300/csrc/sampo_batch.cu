@@ -434,6 +434,10 @@ extern "C" int sampo_batch_checkpoint_load(sampo_batch* b, uint32_t slot, const 
   if (!err.empty()) return bfail(b, SAMPO_ERR_IO, err);
   if (hd.cc != r->cc) { fclose(f); return bfail(b, SAMPO_ERR_ARG, "checkpoint carrying capacity differs from the slot's"); }
   if ((uint64_t)hd.n > r->capacity) { fclose(f); return bfail(b, SAMPO_ERR_CAPACITY, "checkpoint pool exceeds the slot's capacity"); }
+  if (const char* why = ranges_error(hd.pop, r->capacity)) {
+    fclose(f);
+    return bfail(b, SAMPO_ERR_IO, std::string("inconsistent checkpoint (") + why + "): " + path);
+  }
   cudaSetDevice(b->device);
   BCK(cudaStreamSynchronize(b->stream), "checkpoint");
   const std::string rerr = ck_read_pool(f, hd, r->rp.pool[0]);

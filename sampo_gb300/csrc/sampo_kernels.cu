@@ -1,28 +1,48 @@
 // sampo_kernels.cu - host side of the step kernels: grid sizes, launchers
 // and the grid autotuner. The device code is in sampo_step_kernels.cuh.
 #include <cuda_runtime.h>
+#include <mutex>
 #include "sampo_step_kernels.cuh"
 
 namespace sampo {
 
 // ------------------------------------------------------------------------
-static int sm_count() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  return sms;
-}
-static void set_smem_attrs() {
-  static bool done = false;
-  if (done) return;
+// Per-device set-up, once per device under a once_flag: the SM count and the
+// dynamic shared memory limit of the two persistent kernels (a function
+// attribute applies to the device that is current when it is set, so every
+// device the library runs on gets its own). Devices beyond kMaxDevices are
+// set up on every call under a mutex.
+namespace {
+constexpr int kMaxDevices = 64;
+struct DeviceSetup {
+  std::once_flag once;
+  int sms = 1;
+};
+DeviceSetup g_setup[kMaxDevices];
+std::mutex g_setup_mu;
+
+int setup_current_device(int dev) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kCountSmem + plan_bytes(kMaxRep)));
   cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kScatterSmem + plan_bytes(kMaxRep)));
-  done = true;
+  return sms > 0 ? sms : 1;
 }
+}  // namespace
+
+// The SM count of the current device, after its one-time set-up.
+static int sm_count() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevices) {
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    return setup_current_device(dev);
+  }
+  DeviceSetup& d = g_setup[dev];
+  std::call_once(d.once, [&] { d.sms = setup_current_device(dev); });
+  return d.sms;
+}
+static void set_smem_attrs() { (void)sm_count(); }
 size_t count_smem_max() { return kCountSmem + plan_bytes(kMaxRep); }
 size_t scatter_smem_max() { return kScatterSmem + plan_bytes(kMaxRep); }
 

@@ -140,6 +140,22 @@ inline void set_tile_arrays(RepParams& r, uint32_t* base, uint32_t max_tiles) {
   r.maxTiles = max_tiles;
 }
 
+// Why a pool's ranges cannot be stepped, or null when they can: the egg
+// range starts at slot 0, no range ends before it starts, the ranges are
+// ordered with a gap between them (every layout kernel/oldToNewAgents.cl:57-95
+// and createInitialPopulation, src/abms.c:185-228, produce), and the pool's
+// end fits `capacity`. Shared by every entry point that takes ranges from
+// its caller or from a file.
+inline const char* ranges_error(const sampo_population& pop, uint64_t capacity) {
+  if (pop.r[0].start != 0) return "the egg range must start at slot 0";
+  for (int k = 0; k < 8; k++) {
+    if (pop.r[k].end < pop.r[k].start) return "range end before start";
+    if (k > 0 && pop.r[k].start <= pop.r[k - 1].end) return "ranges must be ordered with a gap";
+  }
+  if ((uint64_t)pop.r[7].end > capacity) return "pool exceeds the capacity";
+  return nullptr;
+}
+
 inline SimDev initial_sim_state(uint32_t capacity, float cc) {
   SimDev h;
   memset(&h, 0, sizeof(h));

@@ -72,6 +72,26 @@ static bool pool_ok(const sampo_device_pool* d) {
          aligned16(d->numEggBatches) && aligned16(d->flags) && d->ageInHours && d->flags;
 }
 
+// Whether any column of buffer a (a_cap slots) overlaps any column of buffer
+// b (b_cap slots): the step reads `in` while it writes `out`, so the two
+// must be disjoint.
+static bool pools_overlap(const sampo_device_pool* a, uint32_t a_cap, const sampo_device_pool* b, uint32_t b_cap) {
+  const void* ca[10] = {a->ageInHours, a->hoursInState, a->delay, a->cumulativeSporogonicDevelopment,
+                        a->larvalDelayOrOviAttempts, a->availableEggs, a->cycleLength, a->humanBloodmealCount,
+                        a->numEggBatches, a->flags};
+  const void* cb[10] = {b->ageInHours, b->hoursInState, b->delay, b->cumulativeSporogonicDevelopment,
+                        b->larvalDelayOrOviAttempts, b->availableEggs, b->cycleLength, b->humanBloodmealCount,
+                        b->numEggBatches, b->flags};
+  for (int i = 0; i < 10; i++) {
+    const uintptr_t a0 = (uintptr_t)ca[i], a1 = a0 + (uintptr_t)a_cap * (i == 9 ? 1u : 4u) + 16u;
+    for (int j = 0; j < 10; j++) {
+      const uintptr_t b0 = (uintptr_t)cb[j], b1 = b0 + (uintptr_t)b_cap * (j == 9 ? 1u : 4u) + 16u;
+      if (a0 < b1 && b0 < a1) return true;
+    }
+  }
+  return false;
+}
+
 static DevPool to_dev(const sampo_device_pool* d) {
   DevPool p;
   p.age = d->ageInHours; p.his = d->hoursInState; p.delay = d->delay; p.sporo = d->cumulativeSporogonicDevelopment;
@@ -160,15 +180,19 @@ extern "C" int sampo_step_noalloc(const sampo_device_pool* in, uint32_t in_capac
   if (in_capacity > SAMPO_NOALLOC_MAX_SLOTS || out_capacity > SAMPO_NOALLOC_MAX_SLOTS || out_capacity < 128)
     return SAMPO_ERR_ARG;  // the fixed scratch covers pools of up to SAMPO_NOALLOC_MAX_SLOTS slots
   if (!(carrying_capacity > 0.0f) || env->carryingCapacity != carrying_capacity) return SAMPO_ERR_ARG;
-  if (pop_in->r[0].start != 0 || pop_in->r[7].end > in_capacity) return SAMPO_ERR_ARG;
-  for (int k = 0; k < 8; k++) {
-    if (pop_in->r[k].end < pop_in->r[k].start) return SAMPO_ERR_ARG;
-    if (k > 0 && pop_in->r[k].start <= pop_in->r[k - 1].end) return SAMPO_ERR_ARG;
-  }
+  if (ranges_error(*pop_in, in_capacity)) return SAMPO_ERR_ARG;
   if (!pool_ok(in) || !pool_ok(out)) return SAMPO_ERR_ARG;
+  if (pools_overlap(in, in_capacity, out, out_capacity)) return SAMPO_ERR_ARG;
   int prev = -1;
   if (cudaGetDevice(&prev) != cudaSuccess) return SAMPO_ERR_CUDA;
   if (cudaSetDevice(device) != cudaSuccess) return SAMPO_ERR_CUDA;
+  // the call copies from host memory and waits for the step: it cannot be
+  // recorded into a graph
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing((cudaStream_t)stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaSetDevice(prev);
+    return SAMPO_ERR_STATE;
+  }
   const int rc = run_step(in, in_capacity, out, out_capacity, pop_in, env, temperature, world_time, seeds,
                           carrying_capacity, row, pop_out, bnc_out, device, (cudaStream_t)stream);
   cudaSetDevice(prev);

@@ -7,7 +7,8 @@ the per-step stats lines exactly as the reference prints them
 (src/abms.c:67-81), a position-dependent hash of the pool after every step,
 the final ranges and histogram.txt (src/abms.c:176-180).
 
-Needs the reference checkout (default /root/reference, or $SAMPO_REFERENCE)
+Needs the reference checkout ($SAMPO_REFERENCE, else a checkout named
+"reference" beside this repository)
 and only runs where that exists; the fixtures it writes are committed.
 
     python tests/golden/make_golden.py [case ...]
@@ -28,7 +29,9 @@ sys.path.insert(0, REPO)
 from sampo_gb300 import inputs  # noqa: E402
 from tests.golden.cases import CASES, SPECIES_CASES, SPECIES_DIR, make_case_inputs  # noqa: E402
 
-REF = os.environ.get("SAMPO_REFERENCE", "/root/reference")
+from oracle.build import reference_dir  # noqa: E402
+
+REF = reference_dir()
 
 
 def build_ref(species: str | None = None) -> str:

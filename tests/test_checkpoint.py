@@ -180,3 +180,39 @@ def test_checkpoints_move_between_batches_and_simulations(gpu_ready, tmp_path):
         b3.resume(s, ck_plain)
         b3.run(n - k)
         assert b3.rows(s, k, n - k + 1).tobytes() == want[k:].tobytes()
+
+
+@pytest.mark.gpu
+def test_checkpoint_with_broken_ranges_is_refused(gpu_ready, tmp_path):
+    """A checkpoint whose ranges no step could have produced (here the egg
+    range moved off slot 0, with the pool size left consistent) is refused
+    before any column reaches the device."""
+    import struct
+    from sampo_gb300._lib import SampoError
+    from sampo_gb300.sim import Simulation, seed_stream
+    init, seeds = seed_stream(5, 48)
+    T = np.full(48, 27.0, np.float32)
+    from sampo_gb300 import inputs
+    env = np.zeros(48, dtype=inputs.ENV_DTYPE)
+    env["bloodmealSuccess"] = 0.25
+    env["carryingCapacity"] = 5000.0
+    sim = Simulation(capacity=1 << 16, carrying_capacity=5000.0, max_steps=49)
+    sim.set_inputs(T, env)
+    sim.set_seeds(0, seeds)
+    sim.init_population(1000, init, 3, 5)
+    sim.run(24)
+    ck = str(tmp_path / "sim.ck")
+    sim.checkpoint(ck)
+    sim.close()
+    raw = bytearray(open(ck, "rb").read())
+    struct.pack_into("<I", raw, 20, 1)   # pop.r[0].start (after magic, version, step, cc)
+    bad = str(tmp_path / "bad.ck")
+    open(bad, "wb").write(bytes(raw))
+    sim = Simulation(capacity=1 << 16, carrying_capacity=5000.0, max_steps=49)
+    sim.set_inputs(T, env)
+    sim.set_seeds(0, seeds)
+    with pytest.raises(SampoError):
+        sim.resume(bad)
+    sim.resume(ck)             # the intact file still loads into the same handle
+    assert sim.get_step() == 24
+    sim.close()

@@ -129,3 +129,30 @@ def test_step_noalloc_rejects_oversized_pools(gpu_ready):
                                   s.ctypes.data, 100.0, C.byref(row), C.byref(po), C.byref(b), 0, None) == -1
     assert lib.sampo_step_noalloc(C.byref(d), 1024, C.byref(d), big, C.byref(pop), C.byref(e), 25.0, 0,
                                   s.ctypes.data, 100.0, C.byref(row), C.byref(po), C.byref(b), 0, None) == -1
+
+
+def test_step_noalloc_rejects_overlapping_buffers(gpu_ready):
+    """The step reads `in` while it writes `out`: the same buffers, or a
+    column of one inside the other, are refused before anything runs."""
+    torch = pytest.importorskip("torch")
+    from sampo_gb300 import _lib
+    lib = _lib.load()
+    cap = 4096
+    ta, da = _device_pool(torch, cap)
+    tb, db = _device_pool(torch, cap)
+    pop = _lib.Population()
+    for k in range(8):
+        pop.r[k].start = pop.r[k].end = 64 * (k + 1) if k else 0
+    pop.r[0].end = 10
+    e = _lib.Environment(0.25, 0, 0, 100.0, 0, 0)
+    s = np.zeros(16, np.uint32)
+    row, po, b = _lib.StatsRow(), _lib.Population(), _lib.BitesCycles()
+
+    def call(din, dout):
+        return lib.sampo_step_noalloc(C.byref(din), cap, C.byref(dout), cap, C.byref(pop), C.byref(e), 25.0, 0,
+                                      s.ctypes.data, 100.0, C.byref(row), C.byref(po), C.byref(b), 0, None)
+    assert call(da, da) == -1
+    mixed = _lib.DevicePool(**{f: getattr(db, f) for f, _ in _lib.DevicePool._fields_})
+    mixed.flags = da.flags
+    assert call(da, mixed) == -1
+    torch.cuda.synchronize()
