@@ -3,14 +3,14 @@
 
 A bench step is one simulated day: 24 hourly steps of the hot path (count
 pass + update/scatter pass each), replayed as one CUDA graph. The default
-workload is the large plain run: 1e6 initial agents in the egg / larva /
-pupa / adult ratio 40/30/10/20, a 2^27-slot pool, seasonal weather
-(26 + 4 sin(2 pi d/365) + N(0, 0.5^2) C, seed 2) for 730 days, carrying
-capacity 5 x 1e6. agent-days = sum over hourly steps of the live agents at
-the step's start / 24.
+workload is the bandwidth-roofline run: 5e7 preloaded agents uniform over
+the egg / larva / pupa / adult stages (50/50 gender), a 1e8-slot pool, a
+constant 28 C for 90 days, seed 3; W warm-up days, then K timed days.
+agent-days = sum over hourly steps of the live agents at the step's start
+/ 24.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload plain-large|roofline|plain-small|ensemble|served]
+                  [--workload roofline|plain-large|plain-small|ensemble|served]
 
 --workload ensemble: 512 replicates (sizes log-uniform in [1e3, 1e6] eggs, each
 with its own seed and weather) stepped as one batch for W + K days against
@@ -22,7 +22,8 @@ p50/p95/p99 latency and sims/s per rate.
 
 --impl reference times the reference's own per-step algorithm on the host
 cores (the CPU restatement in oracle/, pinned to the reference's code by the
-golden traces) over a bounded sample of the same workload.
+golden traces) over the same simulated days: W untimed warm-up days, then
+K timed days, with the same `config`.
 Under torchrun (N > 1) every rank runs its own replicate (replicas only:
 a simulation does not shard), rank 0 prints one JSON line.
 """
@@ -43,11 +44,11 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 WORKLOADS = {
-    # the headline workload: a large plain run
+    # the large plain run
     "plain-large": dict(name="plain large run: 1e6 agents (egg/larva/pupa/adult 40/30/10/20), 2^27 slots, 730 days, seasonal weather seed 2",
                         counts=(400_000, 300_000, 100_000, 200_000), capacity=1 << 27, days=730, seed=2,
                         cc=5_000_000.0, weather=("seasonal", 2, 26.0, 4.0, 0.5)),
-    # the bandwidth-roofline run
+    # the bandwidth-roofline run (the default)
     "roofline": dict(name="roofline run: 5e7 preloaded agents (uniform over 4 stages, 50/50 gender), 1e8 slots, 28 C constant, 90 days, seed 3",
                      counts=(12_500_000,) * 4, capacity=100_000_000, days=90, seed=3, cc=3_000_000.0,
                      weather=("constant", 28.0)),
@@ -213,6 +214,7 @@ def gpu_arm(args, wl, rank, world, device):
     fresh()
     sim.flush_l2()
     rows, ms = [], 0.0
+    launches0 = sim.kernel_times()[1]
     sync_barrier(world)
     t0 = time.perf_counter()
     with ClockSampler(device) as clk:
@@ -225,7 +227,9 @@ def gpu_arm(args, wl, rank, world, device):
     rows = np.concatenate(rows)
     live = live_counts(rows)
     agent_days = float(live.sum()) / 24.0
-    gpu_launches = 73 * args.steps  # per day: one constants refresh + 24 x (count, scatter, publish)
+    # kernels the library launched in the timed region (its own count: the
+    # kernel nodes of each replayed day graph plus the launches outside graphs)
+    gpu_launches = sim.kernel_times()[1] - launches0
 
     # ---- roofline: the same days again, each kernel between CUDA events ----
     fresh()
@@ -530,10 +534,10 @@ def served_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=727)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain-large", choices=list(WORKLOADS) + ["ensemble", "served"])
+    ap.add_argument("--workload", default="roofline", choices=list(WORKLOADS) + ["ensemble", "served"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ctas-per-sm", default="",
                     help="COUNT,SCATTER: fixed grid sizes of the plain-path workloads instead of the autotuner")
@@ -561,21 +565,25 @@ def main():
     wl = WORKLOADS[args.workload]
     rank, world, local = dist_env()
     dist_init(world)
+    # both arms print this same config: the workload and the simulated days they time
     cfg = {"workload": wl["name"], "step": "one simulated day = 24 hourly steps",
-           "capacity_slots": wl["capacity"], "carrying_capacity": wl["cc"]}
+           "days_warmup": args.warmup, "days_timed": args.steps, "window": f"days {args.warmup}..{args.warmup + args.steps}",
+           "capacity_slots": wl["capacity"], "carrying_capacity": wl["cc"],
+           "l2": "GPU arm: flushed between timed days (write of a buffer > 2x L2)"}
 
     if args.impl == "reference":
         if rank != 0:
             return
-        # each bench step = one simulated hour of the same workload on the host cores
-        ref = cpu_reference(wl, 0, first_steps=args.steps, warmup=args.warmup)
+        # the reference's per-step algorithm on the host cores over the same
+        # days: warm-up days untimed, then the timed days
+        ref = cpu_reference(wl, 0, first_steps=24 * args.steps, warmup=24 * args.warmup)
         line = {"impl": "reference", "metric": "agent-days/s", "value": ref["value"], "unit": "agent-days/s",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": ref["seconds"] * 1e3 / max(ref["steps"], 1), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
-                "config": dict(cfg, step="one simulated hour (bounded sample of the same workload)"),
+                "ms_per_step": ref["seconds"] * 1e3 / max(args.steps, 1), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic", "config": cfg,
                 "cpu_baseline": {"value": ref["value"], "unit": "agent-days/s", "cores": ref["threads"], "kind": "port",
-                                 "sample": f"first {ref['steps']} hourly steps of the workload, all host threads (OpenMP)"},
+                                 "sample": f"hourly steps {24 * args.warmup}..{24 * (args.warmup + args.steps)} of the workload "
+                                           f"(the timed days; {ref['seconds']:.1f} s), all host threads (OpenMP)"},
                 "e2e": {"value": ref["value"], "unit": "agent-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -590,18 +598,19 @@ def main():
     cpu = cpu_reference(wl, args.cpu_seconds) if world == 1 else None
     live_tot = r["live"].sum(axis=1)
     pool_bytes = live_tot * RECORD_BYTES
-    cfg.update({"days_timed": args.steps, "live_agents_min": int(live_tot.min()), "live_agents_max": int(live_tot.max()),
-                "l2": "flushed between timed days (write of a buffer > 2x L2); pool bytes %.2e..%.2e" % (pool_bytes.min(), pool_bytes.max()),
-                "parallelism": f"replicas x{world}",
-                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1],
-                                "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"}})
+    details = {"live_agents_min": int(live_tot.min()), "live_agents_max": int(live_tot.max()),
+               "pool_bytes": [float(pool_bytes.min()), float(pool_bytes.max())], "parallelism": f"replicas x{world}",
+               "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1],
+                               "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"}}
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32 (f64 where the reference promotes)",
-        "data": "synthetic", "config": cfg,
+        "data": "synthetic", "config": cfg, "details": details,
         "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
                      "frac": r["achieved"] / r["peak"], "traffic": r["traffic"], "kernel": "k_scatter (update + stable scatter)",
+                     "traffic_from": "scaled: DRAM bytes per live agent of one ncu capture of k_scatter on the 5e6-agent "
+                                     "roofline mix (profiles/k_scatter_dram.json) x this run's mean live pool",
                      "peak_kind": r["peak_kind"], "scatter_ms_per_launch": r["scatter_ms"], "count_ms_per_launch": r["count_ms"],
                      "publish_and_gaps_ms_per_step": r["publish_ms"],
                      "count_pass_gbs": r["count_gbs"],

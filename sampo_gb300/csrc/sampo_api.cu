@@ -55,6 +55,7 @@ struct sampo_sim {
   bool pending = false;                // steps queued by sampo_run_async, not yet synced
   int grid_count = 0, grid_scatter = 0;
   cudaGraphExec_t day_graph = nullptr;
+  uint32_t day_graph_kernels = 0;      // kernel nodes of day_graph (counted at capture)
   bool timing = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   double t_count = 0, t_scatter = 0, t_total = 0;
@@ -395,6 +396,19 @@ static int build_day_graph(sampo_sim* s) {
   cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
   if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(s, e, "capture launch"); }
   if (e2 != cudaSuccess) return cuda_fail(s, e2, "end capture");
+  // the launches a replay makes: the kernel nodes the capture recorded
+  size_t nn = 0;
+  e = cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (e == cudaSuccess && nn) e = cudaGraphGetNodes(g, nodes.data(), &nn);
+  uint32_t kernels = 0;
+  for (size_t i = 0; i < nn && e == cudaSuccess; i++) {
+    cudaGraphNodeType t;
+    e = cudaGraphNodeGetType(nodes[i], &t);
+    kernels += t == cudaGraphNodeTypeKernel ? 1u : 0u;
+  }
+  if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(s, e, "graph nodes"); }
+  s->day_graph_kernels = kernels;
   e = cudaGraphInstantiate(&s->day_graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) { s->day_graph = nullptr; return cuda_fail(s, e, "graph instantiate"); }
@@ -463,7 +477,7 @@ static int queue_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows, bool 
         if (rc) return rc;
         for (; i + 24 <= n; i += 24) {
           CK(cudaGraphLaunch(s->day_graph, s->stream), "day graph");
-          s->launches += 72;
+          s->launches += s->day_graph_kernels;
         }
       }
       for (; i < n; i++) {
