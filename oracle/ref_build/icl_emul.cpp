@@ -18,8 +18,19 @@
  *
  * Hooks for pinning (not part of the reference): the seed given to srand is
  * replaced (link with -Wl,--wrap=srand), optional initial ages are applied
- * right after the first initAgents launch, and a position-dependent hash of
+ * right after the first initAgents launch, an optional mixed-stage pool file
+ * replaces the initial population (below), and a position-dependent hash of
  * the pool written by each oldToNewAgents launch is appended to a file.
+ *
+ * Pool file (little-endian): the 8 bytes "SAMPOPL1", the eight ranges as
+ * uint32 start/end pairs, uint32 n (= the last range's end), then the n
+ * slots as the reference's device records: n struct Agent, n struct
+ * AgentAge, n struct AgentState (include/agent.h:66-102). Its layout must be
+ * one a compaction produces (kernel/oldToNewAgents.cl:57-95): eggs from slot
+ * 0, each next range at ((previous end + 64) / 64) * 64. The slots replace
+ * what the first initAgents launch wrote, and the ranges replace the host
+ * Population that src/abms.c:477 writes to the device (abms.c keeps using
+ * the same struct, so its host view agrees).
  */
 #include <cstdarg>
 #include <cstdint>
@@ -60,7 +71,11 @@ unsigned sampo_ref_seed = 1;
 int sampo_ref_age_days = -1;
 unsigned long long sampo_ref_age_seed = 0;
 const char* sampo_ref_hash_file = nullptr;
+const char* sampo_ref_pool_file = nullptr;
 }
+
+static EPop g_pool_pop;
+static bool g_pool_ready = false;
 
 extern "C" void __wrap_srand(unsigned) { __real_srand(sampo_ref_seed); }
 
@@ -135,7 +150,11 @@ void icl_write_buffer_offset(icl_buffer* buf, cl_bool, size_t off, size_t size, 
    * pop[1]. With aged initial eggs (an extension) the host copy is switched
    * to the padded layout first (the same one the CPU port and the CUDA path
    * use); the pointer is abms.c's own non-const struct. */
-  if (sampo_ref_age_days >= 0 && size == sizeof(EPop) && off == sizeof(EPop) && g_pop_writes++ == 0) {
+  if (g_pool_ready && size == sizeof(EPop) && off == sizeof(EPop) && g_pop_writes == 0) {
+    g_pop_writes++;
+    EPop* p = (EPop*)const_cast<void*>(ptr);
+    for (int k = 0; k < 8; k++) p->r[k] = g_pool_pop.r[k];
+  } else if (sampo_ref_age_days >= 0 && size == sizeof(EPop) && off == sizeof(EPop) && g_pop_writes++ == 0) {
     EPop* p = (EPop*)const_cast<void*>(ptr);
     for (int k = 1; k < 8; k++) {
       p->r[k].start = ((p->r[k - 1].end + 64u) / 64u) * 64u;
@@ -203,6 +222,26 @@ static void apply_initial_ages(EAgentAge* g, uint32_t n) {
   }
 }
 
+static void load_pool_file(icl_buffer* agents, icl_buffer* ages, icl_buffer* states) {
+  FILE* f = fopen(sampo_ref_pool_file, "rb");
+  char magic[8];
+  uint32_t rg[16], n = 0;
+  bool ok = f && fread(magic, 8, 1, f) == 1 && memcmp(magic, "SAMPOPL1", 8) == 0 && fread(rg, sizeof(rg), 1, f) == 1 &&
+            fread(&n, 4, 1, f) == 1 && n == rg[15] && rg[0] == 0;
+  for (int k = 1; k < 8 && ok; k++) ok = rg[2 * k] == ((rg[2 * k - 1] + 64u) / 64u) * 64u && rg[2 * k + 1] >= rg[2 * k];
+  ok = ok && (size_t)n * sizeof(EAgent) <= agents->size && (size_t)n * sizeof(EAgentAge) <= ages->size &&
+       (size_t)n * sizeof(EAgentState) <= states->size;
+  ok = ok && fread(agents->mem, sizeof(EAgent), n, f) == n && fread(ages->mem, sizeof(EAgentAge), n, f) == n &&
+       fread(states->mem, sizeof(EAgentState), n, f) == n;
+  if (f) fclose(f);
+  if (!ok) {
+    fprintf(stderr, "icl_emul: bad pool file %s\n", sampo_ref_pool_file);
+    exit(-1);
+  }
+  for (int k = 0; k < 8; k++) g_pool_pop.r[k] = ERange{rg[2 * k], rg[2 * k + 1]};
+  g_pool_ready = true;
+}
+
 void icl_run_kernel(const icl_kernel* kernel, cl_uint, const size_t* gws, const size_t*, icl_event*, icl_event*, cl_uint nargs, ...) {
   Args a;
   va_list ap;
@@ -217,8 +256,10 @@ void icl_run_kernel(const icl_kernel* kernel, cl_uint, const size_t* gws, const 
 
   if (nm == "initAgents") {
     refk_initAgents(G, a.buf(0), a.buf(1), a.buf(2), a.buf(3), a.f(4), a.buf(5));
-    if (g_init_launches++ == 0)
-      apply_initial_ages((EAgentAge*)a.buf(1), ((EEnb*)a.buf(3))->newEggs);
+    if (g_init_launches++ == 0) {
+      if (sampo_ref_pool_file) load_pool_file((icl_buffer*)a.val[0], (icl_buffer*)a.val[1], (icl_buffer*)a.val[2]);
+      else apply_initial_ages((EAgentAge*)a.buf(1), ((EEnb*)a.buf(3))->newEggs);
+    }
   } else if (nm == "killAgents") {
     refk_killAgents(G, a.buf(0), a.buf(1), a.buf(2), a.buf(3), a.buf(4), a.buf(5), a.f(6));
   } else if (nm == "updateAgents") {

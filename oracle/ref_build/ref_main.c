@@ -8,7 +8,11 @@
  * the emulator (icl_emul.cpp).
  *
  *   sampo_ref [--seed S] [--initial N] [--cc CC] [--steps K]
- *             [--age-days D --age-seed A] [--hash-file F] TEMP ENV [SPECIES]
+ *             [--age-days D --age-seed A | --pool FILE] [--hash-file F]
+ *             TEMP ENV [SPECIES]
+ *
+ * --pool FILE starts from a mixed-stage pool (format in icl_emul.cpp) in
+ * place of the initial eggs.
  *
  * SPECIES is passed on as abms.c's argv[3]; the kernels were compiled with
  * the species header at build time (ref_build/Makefile, target species).
@@ -24,6 +28,7 @@ extern unsigned sampo_ref_seed;
 extern int sampo_ref_age_days;
 extern unsigned long long sampo_ref_age_seed;
 extern const char* sampo_ref_hash_file;
+extern const char* sampo_ref_pool_file;
 int abms_main(int argc, char** argv);
 
 int main(int argc, char** argv) {
@@ -37,6 +42,7 @@ int main(int argc, char** argv) {
     else if (!strcmp(argv[i], "--age-days") && i + 1 < argc) sampo_ref_age_days = atoi(argv[++i]);
     else if (!strcmp(argv[i], "--age-seed") && i + 1 < argc) sampo_ref_age_seed = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--hash-file") && i + 1 < argc) sampo_ref_hash_file = argv[++i];
+    else if (!strcmp(argv[i], "--pool") && i + 1 < argc) sampo_ref_pool_file = argv[++i];
     else if (np < 4) pos[np++] = argv[i];
     else { fprintf(stderr, "sampo_ref: unexpected argument %s\n", argv[i]); return 2; }
   }

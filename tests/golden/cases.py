@@ -32,6 +32,12 @@ CASES = {
     "temperature_edges": dict(seed=21, initial=2000, cc=10000.0, steps=960, age_days=3, age_seed=6,
                               weather=("segments", ((18, 28.0), (4, 16.0), (4, 16.5), (4, 8.0), (2, 12.0),
                                                     (3, 43.9), (5, 30.0))), interventions=None),
+    # A mixed-stage start: every one of the eight states populated
+    # (sampo_gb300.population.make_pool at the first hour's temperature),
+    # loaded in place of the initial eggs; interventions on from day 10.
+    "mixed_pool": dict(seed=31, initial=0, cc=27500.0, steps=480, age_days=-1, age_seed=0,
+                       pool=dict(counts=(1500, 1200, 400, 2400), seed=17),
+                       weather=("seasonal", 20, 9, 27.0, 3.0, 0.5), interventions="alternating"),
     # Small, quick cases for the CPU suite.
     "small_a": dict(seed=7, initial=600, cc=3000.0, steps=720, age_days=3, age_seed=9,
                     weather=("seasonal", 30, 2, 25.0, 5.0, 0.5), interventions=None),
@@ -78,3 +84,40 @@ def make_case_inputs(name: str, directory: str):
         raise ValueError(w)
     meta = {"temp_sha256": inputs.file_sha256(tp), "env_sha256": inputs.file_sha256(ep)}
     return tp, ep, meta
+
+
+def case_pool(name: str, T0: float):
+    """The initial pool of a case with a "pool" entry: (ranges, arrays)."""
+    from sampo_gb300.population import make_pool
+    p = CASES[name]["pool"]
+    return make_pool(p["counts"], T0, seed=p["seed"])
+
+
+def write_ref_pool(path: str, ranges, arrays) -> None:
+    """A pool in the file format of ref-as-C's --pool option: "SAMPOPL1", the
+    ranges, n, then the slots as the reference's device records (struct Agent,
+    struct AgentAge, struct AgentState, include/agent.h:66-102)."""
+    r = np.asarray(ranges, dtype=np.uint32).reshape(8, 2)
+    n = int(r[7][1])
+    agent = np.zeros(n, dtype=[("availableEggs", "<u4"), ("cycleLength", "<u4"), ("hbc", "<u4"), ("delay", "<f4"),
+                               ("numEggBatches", "<u4"), ("uni", "<u4")])
+    age = np.zeros(n, dtype=[("age", "<f4"), ("his", "<f4"), ("isFemale", "<i4"), ("sporo", "<f4")])
+    st = np.zeros(n, dtype=[("dead", "<i4"), ("state", "<i4")])
+    agent["availableEggs"] = arrays["availableEggs"][:n]
+    agent["cycleLength"] = arrays["cycleLength"][:n]
+    agent["hbc"] = arrays["humanBloodmealCount"][:n]
+    agent["delay"] = arrays["delay"][:n]
+    agent["numEggBatches"] = arrays["numEggBatches"][:n]
+    agent["uni"] = arrays["larvalDelayOrOviAttempts"][:n]
+    age["age"] = arrays["ageInHours"][:n]
+    age["his"] = arrays["hoursInState"][:n]
+    age["isFemale"] = arrays["isFemale"][:n].astype(np.int32)
+    age["sporo"] = arrays["cumulativeSporogonicDevelopment"][:n]
+    st["state"] = (1 << arrays["state"][:n].astype(np.int64)).astype(np.int32)
+    with open(path, "wb") as f:
+        f.write(b"SAMPOPL1")
+        f.write(r.astype("<u4").tobytes())
+        f.write(np.uint32(n).astype("<u4").tobytes())
+        f.write(agent.tobytes())
+        f.write(age.tobytes())
+        f.write(st.tobytes())

@@ -27,7 +27,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
 from sampo_gb300 import inputs  # noqa: E402
-from tests.golden.cases import CASES, SPECIES_CASES, SPECIES_DIR, make_case_inputs  # noqa: E402
+from tests.golden.cases import CASES, SPECIES_CASES, SPECIES_DIR, case_pool, make_case_inputs, write_ref_pool  # noqa: E402
 
 from oracle.build import reference_dir  # noqa: E402
 
@@ -53,6 +53,12 @@ def run_case(exe: str, name: str) -> dict:
                "--steps", str(c["steps"]), "--hash-file", hf]
         if c.get("age_days", -1) >= 0:
             cmd += ["--age-days", str(c["age_days"]), "--age-seed", str(c["age_seed"])]
+        if c.get("pool"):
+            ranges, arrays = case_pool(name, inputs.read_temperature(tp, 1)[0])
+            pf = os.path.join(td, "pool.bin")
+            write_ref_pool(pf, ranges, arrays)
+            cmd += ["--pool", pf]
+            meta["pool_slots"] = int(ranges[7][1])
         cmd += [tp, ep]
         if c.get("species"):
             cmd.append(c["species"])

@@ -137,6 +137,40 @@ def test_run_matches_reference_golden(gpu_ready, oracle_mod, tmp_path, name):
     sim.close()
 
 
+def test_mixed_stage_pool_matches_reference_golden(gpu_ready, oracle_mod, tmp_path):
+    """The mixed-stage start of the reference's own code (ref-as-C from the
+    same pool file): every printStats line, the pool hash after every day,
+    the final ranges and histogram.txt, through sampo_run's day graphs."""
+    from sampo_gb300.sim import Simulation, histogram_text, population_lines, seed_stream, stats_lines
+    from tests.golden.cases import case_pool
+    name = "mixed_pool"
+    g = load_golden(name)
+    n = CASES[name]["steps"]
+    c, T, env = _inputs(name, tmp_path, n)
+    ranges, arrays = case_pool(name, T[0])
+    _, seeds = seed_stream(c["seed"], n)
+    sim = Simulation(capacity=1 << 18, carrying_capacity=c["cc"], max_steps=n + 1)
+    sim.set_inputs(T, env)
+    sim.set_seeds(0, seeds)
+    sim.load_pool(ranges, arrays)
+    lines, done, prev = [], 0, None
+    while done < n:
+        rows = sim.run(24)
+        lines += stats_lines(rows, T, ranges, first_step=done, prev_ranges=prev)
+        prev = rows[-1]["ranges"]
+        done += 24
+        pop, pool = sim.read_pool()
+        assert format(oracle_mod.pool_hash(pop["ranges"], pool), "016x") == g["pool_hash"][done - 1], f"pool after step {done - 1}"
+    for i, (a, b) in enumerate(zip(lines, g["trace"])):
+        assert a == b, f"step {i}: cuda {a!r} != reference {b!r}"
+    assert len(lines) == len(g["trace"])
+    pop, _ = sim.read_pool(ranges_only=True)
+    assert population_lines(pop["ranges"]) == g["final_ranges"]
+    assert histogram_text(sim.histogram()) == g["histogram_txt"]
+    assert sim.device_status() == 0
+    sim.close()
+
+
 def test_mixed_stage_pool_against_oracle(gpu_ready, oracle_mod):
     """A loaded mixed-stage pool (all eight states populated) stepped on both."""
     from oracle import OracleSim

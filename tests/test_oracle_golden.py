@@ -3,6 +3,8 @@
 after every step, the final ranges and histogram.txt must be identical."""
 import subprocess
 
+import numpy as np
+
 import pytest
 
 from tests.conftest import load_golden
@@ -59,3 +61,34 @@ def test_golden_fixtures_are_complete():
         assert len(g["trace"]) == c["steps"] == len(g["pool_hash"])
         assert g["histogram_txt"].count(",") == 100
         assert len(g["final_ranges"]) == 8
+
+
+def test_oracle_matches_reference_from_mixed_stage_pool(oracle_mod, tmp_path):
+    """A mixed-stage start (all eight states populated) loaded into the
+    oracle against the reference's own code started from the same pool
+    (ref-as-C's --pool): every stats line and the pool hash after every step."""
+    from oracle import OracleSim
+    from sampo_gb300 import inputs
+    from sampo_gb300.sim import seed_stream, stats_lines
+    from tests.golden.cases import case_pool
+    name = "mixed_pool"
+    g = load_golden(name)
+    c = CASES[name]
+    n = c["steps"]
+    tp, ep, meta = make_case_inputs(name, str(tmp_path))
+    T = inputs.read_temperature(tp, n)
+    env = inputs.read_environment(ep, n, c["cc"])
+    ranges, arrays = case_pool(name, T[0])
+    assert {k: v for k, v in g["inputs"].items() if k != "pool_slots"} == meta
+    assert g["inputs"]["pool_slots"] == int(ranges[7][1])
+    _, seeds = seed_stream(c["seed"], n)
+    o = OracleSim(1 << 18)
+    o.load_pool(ranges, arrays)
+    rows = []
+    for i in range(n):
+        rows.append(o.step(env[i], T[i], i % 24, seeds[i]))
+        assert format(o.pool_hash(), "016x") == g["pool_hash"][i], f"pool after step {i}"
+    lines = stats_lines(np.array(rows), T, ranges)
+    for i, (a, b) in enumerate(zip(lines, g["trace"])):
+        assert a == b, f"step {i}: oracle {a!r} != reference {b!r}"
+    o.close()
