@@ -71,6 +71,12 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 __device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
+__device__ __forceinline__ void mbar_init_count(uint64_t* bar, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // 1-D bulk copy global -> shared, completion counted on bar (both addresses
 // 16-byte aligned, bytes a multiple of 16).
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
@@ -309,8 +315,8 @@ __device__ void issue_count_tile(const DevPool& src, uint8_t* st, uint64_t* bar,
   if (m & CA_FLAGS) bulk_load(st + 5 * kColBytes, src.flags + lo, b1, bar);
 }
 
-// One tile in flight or in work in a count stage. Everything but lt is the
-// replicate's and stays valid while the stage keeps serving that replicate.
+// One tile in flight or in work in a count stage. The replicate's part
+// (c .. larv) is reloaded only when the stage moves on to another replicate.
 struct alignas(16) CountStage {
   StepCtx c;
   sampo_population pop;
@@ -318,7 +324,11 @@ struct alignas(16) CountStage {
   uint32_t* tileAgg;
   uint32_t* tilePre;
   uint32_t rep, lt, end, larv;    // replicate, its tile index, its pool end, larvicide on
-  uint32_t loaded;                // replicate whose c is loaded
+  uint32_t tick;                  // the tile's ticket; >= the ticket total: no more tiles
+  int urg;                        // the range that holds every slot of the tile, or -1
+  uint32_t left;                  // warps that have not finished the tile
+  uint32_t crep;                  // replicate whose survivor counts `cnt` holds
+  uint32_t cnt[8];                // survivors by next state of the stage's tiles of crep, not yet added to its totals
 };
 
 // Dynamic shared memory of the persistent kernels: the two stages, then the
@@ -327,16 +337,78 @@ struct alignas(16) CountStage {
 constexpr size_t kCountSmem = 2 * kCountStage;
 constexpr size_t kScatterSmem = 2 * kScatterStage;
 __host__ __device__ constexpr size_t plan_bytes(uint32_t nrep) { return ((size_t)(nrep + 1) * 4 + 15) & ~(size_t)15; }
+constexpr uint32_t kNoRep = 0xffffffffu;
 
-__global__ void __launch_bounds__(kBlock) k_count(KParams p) {
+// One warp's items of a count-pass tile in stage memory st: the decision
+// part of the update for each of its slots, and per (round, warp) chunk the
+// survivors by next state into ent (8-bit fields, states 0-3 | 4-7).
+// RG >= 0: every slot of the tile lies in range RG, so only that state's
+// code is compiled in; RG = -1: a tile that spans ranges.
+template <int RG>
+__device__ __forceinline__ void count_items(const CountStage& cs, const uint8_t* st, const KillConst& mc, uint32_t lo,
+                                            uint32_t end, int tid, uint2* ent, Acc& acc, uint32_t& devoob) {
+  const int lane = tid & 31, warp = tid >> 5;
+  const StepCtx& c = cs.c;
+  const bool larvicide = c.env.larvacideValue > 0.0f;
+  const float* s_age = (const float*)(st + 0 * kColBytes);
+  const float* s_his = (const float*)(st + 1 * kColBytes);
+  const float* s_delay = (const float*)(st + 2 * kColBytes);
+  const uint32_t* s_uni = (const uint32_t*)(st + 3 * kColBytes);
+  const uint32_t* s_avail = (const uint32_t*)(st + 4 * kColBytes);
+  const uint8_t* s_flags = st + 5 * kColBytes;
+#pragma unroll
+  for (int k = 0; k < kItems; k++) {
+    const uint32_t i = k * kBlock + tid;
+    const uint32_t g = lo + i;
+    int rg;
+    bool valid;
+    if (RG >= 0) {
+      rg = RG;
+      valid = g < end;
+    } else {
+      rg = g < end ? range_of(cs.pop, g) : -1;
+      valid = rg >= 0;
+    }
+    uint32_t pk0 = 0, pk1 = 0;  // this slot's next state as an 8-bit counter: states 0-3, 4-7
+    if (valid) {
+      Rec a;
+      a.age = (rg == LARVA || rg >= IMMATURE) ? s_age[i] : 0.0f;
+      a.his = (rg != GRAVID && (rg != LARVA || larvicide)) ? s_his[i] : 0.0f;
+      a.delay = rg != GRAVID ? s_delay[i] : 0.0f;
+      a.uni = (rg == LARVA || rg == GRAVID) ? s_uni[i] : 0u;
+      a.avail = rg == GRAVID ? s_avail[i] : 0u;
+      a.female = rg == MATESEEKING ? (s_flags[i] >> 3) & 1u : 0u;
+      a.sporo = 0.0f; a.cycle = 0u; a.hbc = 0u; a.batches = 0u;
+      devoob |= (rg == LARVA) & c.devOOB;
+      const int ns = update_agent<false>(c, mc, rg, g, a, acc);
+      if (ns >= 0) {
+        if (ns < 4) pk0 = 1u << (8 * ns);
+        else pk1 = 1u << (8 * (ns - 4));
+      }
+    }
+    pk0 = __reduce_add_sync(0xffffffffu, pk0);
+    pk1 = __reduce_add_sync(0xffffffffu, pk1);
+    if (lane == 0) ent[k * kWarps + warp] = make_uint2(pk0, pk1);
+  }
+}
+
+// The count pass. Its warps share no barrier once the tiles flow: each warp
+// takes the stages' tiles in turn (stage it & 1 for its it-th tile, behind
+// the stage's mbarrier), and the LAST warp to finish a tile does the tile's
+// bookkeeping while the others go on with the tile in the other stage: it
+// builds the tile's prefix table from the warps' chunk counts, adds the
+// tile's totals to the stage's counts, claims the next ticket and starts
+// that tile's copies into the stage it has just emptied. A warp's stall is
+// then the wait for a tile's data, never the wait for the slowest warp.
+__global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ CountStage s_cs[2];
   __shared__ KillConst s_mc;
   __shared__ uint32_t s_w[33];
   uint32_t* s_pre = reinterpret_cast<uint32_t*>(dsm + kCountSmem);
   __shared__ __align__(8) uint64_t bars[2];
-  __shared__ uint32_t s_tick[2];
-  __shared__ uint2 s_ent[kChunks];  // per (round, warp): survivors by state, 8-bit fields (states 0-3 | 4-7)
+  __shared__ uint32_t s_tnext;                // the next ticket, drawn one claim ahead
+  __shared__ uint2 s_ent[2][kChunks];         // per stage, per (round, warp): survivors by state, 8-bit fields (states 0-3 | 4-7)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   load_model_const(&p.mc->kill, s_mc);
   plan_tickets(p.nrep, s_pre, s_w, [&](uint32_t r) -> uint32_t {
@@ -344,134 +416,144 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
     return sim->active ? (sim->pop.r[GRAVID].end + kTile - 1) / kTile : 0u;
   });
   const uint32_t total = s_pre[p.nrep];
-  Acc acc = {0, 0, 0, 0, 0, 0};
-  uint32_t cta_cnt = 0;  // thread b < 8: this CTA's survivors of next state b in the current replicate
-  uint32_t devoob = 0, phase = 0, pend = 0;  // pend (thread 0): stages with a copy in flight
-  uint32_t fail_rep = 0;
-  bool failed = false;
-
-  // thread 0: take the next ticket into stage sidx and start its copies. The
-  // ticket was drawn one claim earlier, so the atomic's round trip overlaps
-  // a tile's work. A step with no more tiles than CTAs gives CTA b tile b
-  // (no CTA queues a second tile while others have none).
+  // a step with no more tiles than CTAs gives CTA b tile b (no CTA queues a
+  // second tile while others have none)
   const bool one_each = total <= gridDim.x;
-  uint32_t t_next = 0;
+
+  // the whole warp: add the stage's counts to their replicate's totals
+  auto flush_stage = [&](CountStage& cs) {
+    if (cs.crep != kNoRep && lane < 8 && cs.cnt[lane]) atomicAdd(&p.reps[cs.crep].sim->cnt[lane], cs.cnt[lane]);
+    __syncwarp();
+    if (lane < 8) cs.cnt[lane] = 0;
+    if (lane == 0) cs.crep = kNoRep;
+    __syncwarp();
+  };
+  // the whole warp: take the next ticket into stage sidx (emptied by every
+  // warp), describe its tile and start its copies. The description is
+  // written before the arrival on bars[sidx] that the waiting warps acquire.
+  // Tickets run from the last tile down: the scatter pass then starts on the
+  // tiles whose decision columns and prefix tables this pass touched last,
+  // while they are still in L2.
   auto claim = [&](uint32_t sidx) {
-    const uint32_t t = t_next;
-    t_next = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket1, 1u);
-    s_tick[sidx] = t;
-    if (t >= total) return;
-    // tickets run from the last tile down: the scatter pass then starts on
-    // the tiles whose decision columns and prefix tables this pass touched
-    // last, while they are still in L2
-    const uint32_t tile = total - 1u - t;
-    const uint32_t r = find_rep(s_pre, p.nrep, tile);
     CountStage& cs = s_cs[sidx];
-    if (cs.rep != r) {
-      const RepParams& rp = p.reps[r];
-      const SimDev* sim = rp.sim;
-      cs.rep = r;
-      cs.pop = sim->pop;
-      cs.end = cs.pop.r[GRAVID].end;
-      cs.src = rp.pool[sim->cur];
-      cs.tileAgg = rp.tileAgg;
-      cs.tilePre = rp.tilePre;
-      cs.larv = sim->ctx.env.larvacideValue > 0.0f;
+    uint32_t t = 0;
+    if (lane == 0) {
+      t = s_tnext;
+      s_tnext = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket1, 1u);
     }
-    cs.lt = tile - s_pre[r];
-    const uint32_t lo = cs.lt * kTile;
-    fence_proxy_async();  // the stage was last read through the generic proxy
-    issue_count_tile(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, min((uint32_t)kTile, cs.end - lo), cs.larv != 0);
-    pend |= 1u << sidx;
-  };
-  // all threads: the stage's step constants when its replicate changed (a
-  // uniform test); then synchronised
-  auto stage_ctx = [&](CountStage& cs) {
-    const uint32_t r = cs.rep;
-    if (cs.loaded == r) return;
-    copy16(&cs.c, &p.reps[r].sim->ctx, (int)sizeof(StepCtx), tid, kBlock);
-    __syncthreads();
-    if (tid == 0) cs.loaded = r;
-  };
-  // all threads: add this CTA's counts of replicate r to its totals
-  auto flush = [&](uint32_t r) {
-    SimDev* sim = p.reps[r].sim;
-    if (tid < 8 && cta_cnt) atomicAdd(&sim->cnt[tid], cta_cnt);
-    cta_cnt = 0;
-    const uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
-    if (lane == 0 && ne) atomicAdd(&sim->newEggs, ne);
-    const uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
-    if (lane == 0 && bad) atomicOr(&sim->error, bad);
-    acc.newEggs = 0; acc.bad = 0; devoob = 0;
+    t = __shfl_sync(0xffffffffu, t, 0);
+    const uint32_t tile = total - 1u - t;
+    const uint32_t r = t < total ? find_rep(s_pre, p.nrep, tile) : kNoRep;
+    const uint32_t cur = cs.rep;
+    __syncwarp();
+    if (cur != r) {  // uniform: the stage moves on to another replicate
+      flush_stage(cs);
+      if (r != kNoRep) {
+        const RepParams& rp = p.reps[r];
+        const SimDev* sim = rp.sim;
+        copy16(&cs.c, &sim->ctx, (int)sizeof(StepCtx), lane, 32);
+        if (lane == 0) {
+          cs.pop = sim->pop;
+          cs.end = cs.pop.r[GRAVID].end;
+          cs.src = rp.pool[sim->cur];
+          cs.tileAgg = rp.tileAgg;
+          cs.tilePre = rp.tilePre;
+          cs.larv = sim->ctx.env.larvacideValue > 0.0f;
+          cs.crep = r;
+        }
+      }
+      if (lane == 0) cs.rep = r;
+      __syncwarp();
+    }
+    if (lane == 0) {
+      cs.tick = t;
+      cs.left = kWarps;
+      if (t >= total) {
+        mbar_arrive(&bars[sidx]);  // no copy: the waiting warps see the end
+      } else {
+        cs.lt = tile - s_pre[r];
+        const uint32_t lo = cs.lt * kTile, n = min((uint32_t)kTile, cs.end - lo);
+        const int u = range_of(cs.pop, lo);
+        cs.urg = (u >= 0 && lo + n <= cs.pop.r[u].end) ? u : -1;
+        fence_proxy_async();  // the stage was last read through the generic proxy
+        issue_count_tile(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, n, cs.larv != 0);
+      }
+    }
   };
 
   if (tid == 0) {
     mbar_init(&bars[0]);
     mbar_init(&bars[1]);
     fence_mbar_init();
-    s_cs[0].loaded = s_cs[1].loaded = 0xffffffffu;
-    s_cs[0].rep = s_cs[1].rep = 0xffffffffu;
-    t_next = one_each ? blockIdx.x : atomicAdd(&p.bat->ticket1, 1u);
+    s_tnext = one_each ? blockIdx.x : atomicAdd(&p.bat->ticket1, 1u);
+  }
+  if (tid < 2) {
+    s_cs[tid].rep = kNoRep;
+    s_cs[tid].crep = kNoRep;
+  }
+  if (tid < 16) s_cs[tid >> 3].cnt[tid & 7] = 0;
+  __syncthreads();
+  if (warp == 0) {
     claim(0);
+    claim(1);
   }
   __syncthreads();
-  if (s_tick[0] < total) stage_ctx(s_cs[0]);
-  __syncthreads();
 
-  for (uint32_t it = 0;; it++) {
+  Acc acc = {0, 0, 0, 0, 0, 0};
+  uint32_t devoob = 0, w_rep = kNoRep;
+  // the warp's own accumulators into replicate r's totals
+  auto flush_warp = [&](uint32_t r) {
+    const uint32_t ne = __reduce_add_sync(0xffffffffu, acc.newEggs);
+    if (lane == 0 && ne) atomicAdd(&p.reps[r].sim->newEggs, ne);
+    const uint32_t bad = __reduce_or_sync(0xffffffffu, (acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (devoob ? SAMPO_DEV_ERR_DEVRATES : 0u));
+    if (lane == 0 && bad) atomicOr(&p.reps[r].sim->error, bad);
+    acc.newEggs = 0; acc.bad = 0; devoob = 0;
+  };
+
+  uint32_t it = 0;
+  bool failed = false;
+  for (;; it++) {
     const uint32_t sidx = it & 1u;
-    const uint32_t t = s_tick[sidx];
+    CountStage& cs = s_cs[sidx];
+    if (!__all_sync(0xffffffffu, mbar_wait(&bars[sidx], (it >> 1) & 1u))) {  // bounded; acquires the description
+      failed = true;
+      break;
+    }
+    const uint32_t t = cs.tick;
     if (t >= total) break;
-    const CountStage& cs = s_cs[sidx];
-    uint8_t* st = dsm + sidx * kCountStage;
-    if (tid == 0) claim(sidx ^ 1u);  // prefetch the next tile into the other stage
-    const bool ok = mbar_wait(&bars[sidx], (phase >> sidx) & 1u);
-    if (ok) {
-      phase ^= 1u << sidx;
-      pend &= ~(1u << sidx);
-    }
-    const StepCtx& c = cs.c;
-    const uint32_t end = cs.end, lo = cs.lt * kTile;
-    const bool larvicide = c.env.larvacideValue > 0.0f;
-    const float* s_age = (const float*)(st + 0 * kColBytes);
-    const float* s_his = (const float*)(st + 1 * kColBytes);
-    const float* s_delay = (const float*)(st + 2 * kColBytes);
-    const uint32_t* s_uni = (const uint32_t*)(st + 3 * kColBytes);
-    const uint32_t* s_avail = (const uint32_t*)(st + 4 * kColBytes);
-    const uint8_t* s_flags = st + 5 * kColBytes;
-#pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      const uint32_t i = k * kBlock + tid;
-      const uint32_t g = lo + i;
-      const int rg = (ok && g < end) ? range_of(cs.pop, g) : -1;
-      uint32_t pk0 = 0, pk1 = 0;  // this slot's next state as an 8-bit counter: states 0-3, 4-7
-      if (rg >= 0) {
-        Rec a;
-        a.age = (rg == LARVA || rg >= IMMATURE) ? s_age[i] : 0.0f;
-        a.his = (rg != GRAVID && (rg != LARVA || larvicide)) ? s_his[i] : 0.0f;
-        a.delay = rg != GRAVID ? s_delay[i] : 0.0f;
-        a.uni = (rg == LARVA || rg == GRAVID) ? s_uni[i] : 0u;
-        a.avail = rg == GRAVID ? s_avail[i] : 0u;
-        a.female = rg == MATESEEKING ? (s_flags[i] >> 3) & 1u : 0u;
-        a.sporo = 0.0f; a.cycle = 0u; a.hbc = 0u; a.batches = 0u;
-        devoob |= (rg == LARVA) & c.devOOB;
-        const int ns = update_agent<false>(c, s_mc, rg, g, a, acc);
-        if (ns >= 0) {
-          if (ns < 4) pk0 = 1u << (8 * ns);
-          else pk1 = 1u << (8 * (ns - 4));
-        }
-      }
-      pk0 = __reduce_add_sync(0xffffffffu, pk0);
-      pk1 = __reduce_add_sync(0xffffffffu, pk1);
-      if (lane == 0) s_ent[k * kWarps + warp] = make_uint2(pk0, pk1);
-    }
-    __syncthreads();
     const uint32_t rep = cs.rep;
-    if (warp == 0) {
+    if (rep != w_rep) {
+      if (w_rep != kNoRep) flush_warp(w_rep);
+      w_rep = rep;
+    }
+    const uint8_t* st = dsm + sidx * kCountStage;
+    const uint32_t end = cs.end, lo = cs.lt * kTile;
+    uint2* ent = s_ent[sidx];
+    switch (cs.urg) {  // CTA-uniform: a tile inside one range runs that state's code only
+      case EGG: count_items<EGG>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case LARVA: count_items<LARVA>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case PUPA: count_items<PUPA>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case IMMATURE: count_items<IMMATURE>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case MATESEEKING: count_items<MATESEEKING>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case BMS: count_items<BMS>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case BMD: count_items<BMD>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case GRAVID: count_items<GRAVID>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      default: count_items<-1>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+    }
+    // this warp is done with the stage: the last warp out does the tile's bookkeeping
+    uint32_t last = 0;
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();  // this warp's entries and its reads of the stage come first
+      last = atomicSub(&cs.left, 1u) == 1u;
+      __threadfence_block();  // and the other warps' before the last warp's work
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
+    {
       // the tile's prefix table: exclusive prefix of the 32 (round, warp)
       // chunks, 16-bit packed, and the tile's totals (the update/scatter pass
       // reads both; the totals also feed the look-back)
-      const uint2 e = lane < kChunks ? s_ent[lane] : make_uint2(0u, 0u);
+      const uint2 e = lane < kChunks ? s_ent[sidx][lane] : make_uint2(0u, 0u);
       uint32_t w[5], x[5];
       w[0] = (e.x & 0xffu) | ((e.x & 0xff00u) << 8);
       w[1] = ((e.x >> 16) & 0xffu) | ((e.x >> 8) & 0xff0000u);
@@ -500,30 +582,26 @@ __global__ void __launch_bounds__(kBlock) k_count(KParams p) {
       uint32_t tw = 0;  // lanes 0..7: the tile's survivors of next state `lane`
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        const uint32_t t = __shfl_sync(0xffffffffu, x[q], kChunks - 1);
-        if ((lane >> 1) == q) tw = (t >> (16 * (lane & 1))) & 0xffffu;
+        const uint32_t tq = __shfl_sync(0xffffffffu, x[q], kChunks - 1);
+        if ((lane >> 1) == q) tw = (tq >> (16 * (lane & 1))) & 0xffffu;
       }
       if (lane < 8) {
         cs.tileAgg[(size_t)cs.lt * 8 + lane] = tw;
-        cta_cnt += tw;
+        cs.cnt[lane] += tw;
       }
+      __syncwarp();
     }
-    if (!ok) fail_rep = rep;
-    // the next tile was claimed above and is visible after the barrier
-    const bool more = s_tick[sidx ^ 1u] < total;
-    const bool sw = !more || s_cs[sidx ^ 1u].rep != rep;
-    if (sw) flush(rep);
-    if (more) stage_ctx(s_cs[sidx ^ 1u]);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      if (!sw) flush(rep);
-      break;
-    }
+    claim(sidx);  // the next tile into the stage this tile emptied
   }
-  if (failed && tid == 0) {
-    atomicOr(&p.reps[fail_rep].sim->error, SAMPO_DEV_ERR_TMA);
-    for (int s = 0; s < 2; s++)  // let copies still in flight land before the CTA exits
-      if ((pend >> s) & 1u) (void)mbar_wait(&bars[s], (phase >> s) & 1u);
+  // (each stage's counts were added to their totals by the claim that found
+  // no more tickets for it: the claims alternate stages in iteration order)
+  if (w_rep != kNoRep) flush_warp(w_rep);
+  if (failed && lane == 0) {
+    const uint32_t r = s_cs[it & 1u].rep;
+    atomicOr(&p.reps[r != kNoRep ? r : 0u].sim->error, SAMPO_DEV_ERR_TMA);
+    // let copies still in flight land before the warp exits (bounded waits)
+    (void)mbar_wait(&bars[it & 1u], (it >> 1) & 1u);
+    (void)mbar_wait(&bars[(it + 1) & 1u], ((it + 1) >> 1) & 1u);
   }
 }
 
@@ -749,12 +827,6 @@ __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epo
   }
 }
 
-__device__ __forceinline__ void mbar_init_count(uint64_t* bar, uint32_t n) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(n) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
 
 constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one producer warp
 static_assert(kChunks <= 32, "one (round, warp) chunk per lane");
