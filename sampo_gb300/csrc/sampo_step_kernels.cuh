@@ -844,6 +844,7 @@ struct alignas(16) ScatterStage {
   uint32_t rep, end, newEggs, nold, epoch;  // replicate, pool end, eggs laid, old tiles, look-back epoch
   uint32_t base[8];          // first slot of each next-state range
   uint32_t kind, lo;         // TK_*, first slot (old tile) or first egg id (egg tile)
+  int urg;                   // old tile: the range that holds every slot of the tile, or -1
   uint32_t d0[8], cnt[8];    // per next state: the tile's first slot in it, survivors
 };
 constexpr int kAhead = 3;                 // the producer describes tiles this far ahead of the consumers
@@ -856,6 +857,76 @@ static_assert(kAhead >= 2 && kDescSlots <= 16, "issue() needs tile seq + 2 descr
 // next buffer, its slot in the current one (the generator's gid), its
 // numEggBatches after the step, BM_*.
 struct BmEntry { uint32_t d, gid, batches, kind; };
+
+// Phase A of the update/scatter pass for one warp's items of an old tile in
+// stage memory st: the full update of each slot, and each survivor's slot in
+// the next buffer (dk; 0xffffffff for none): the tile's first slot of its
+// next state + the survivors of that state in earlier (round, warp) chunks
+// (the count pass's prefix table) + its rank within its chunk. nb gets the
+// next state (8: none) | female << 4 | owed draw << 5. RG >= 0: every slot
+// of the tile lies in range RG, so only that state's code is compiled in;
+// RG = -1: a tile that spans ranges.
+template <int RG>
+__device__ __forceinline__ void scatter_phase_a(const ScatterStage& si, const uint8_t* st, const KillConst& kc, int tid,
+                                                Rec (&a)[kItems], uint32_t (&nb)[kItems], uint32_t (&dk)[kItems], Acc& acc,
+                                                uint32_t& tilebad) {
+  const int warp = tid >> 5;
+  const float* c_age = (const float*)(st + 0 * kColBytes);
+  const float* c_his = (const float*)(st + 1 * kColBytes);
+  const float* c_delay = (const float*)(st + 2 * kColBytes);
+  const float* c_sporo = (const float*)(st + 3 * kColBytes);
+  const uint32_t* c_uni = (const uint32_t*)(st + 4 * kColBytes);
+  const uint32_t* c_avail = (const uint32_t*)(st + 5 * kColBytes);
+  const uint32_t* c_cycle = (const uint32_t*)(st + 6 * kColBytes);
+  const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
+  const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
+  const uint8_t* c_flags = st + 9 * kColBytes;
+  const uint32_t* c_pre = (const uint32_t*)(st + kPreOff);
+  const StepCtx& c = si.c;
+  const uint32_t lo = si.lo, end = si.end;
+#pragma unroll
+  for (int k = 0; k < kItems; k++) {
+    const uint32_t i = k * kBlock + tid;
+    const uint32_t g = lo + i;
+    int rg;
+    bool valid;
+    if (RG >= 0) {
+      rg = RG;
+      valid = g < end;
+    } else {
+      rg = g < end ? range_of(si.pop, g) : -1;
+      valid = rg >= 0;
+    }
+    nb[k] = 8;
+    a[k].bm = BM_NONE;
+    a[k].female = 0u;
+    if (valid) {
+      a[k].age = c_age[i]; a[k].his = c_his[i]; a[k].delay = c_delay[i]; a[k].sporo = c_sporo[i];
+      a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
+      a[k].batches = c_batches[i];
+      a[k].female = (c_flags[i] >> 3) & 1u;
+      const int ns = update_agent<true>(c, kc, rg, g, a[k], acc);
+      if (ns >= 0) nb[k] = ns;
+    }
+    const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
+    const uint32_t rk = __popc(peers & lanemask_lt());
+    const uint32_t* e0 = c_pre + (k * kWarps + warp) * kPreEntryWords;  // this chunk's entry
+    const uint32_t* e1 = e0 + kPreEntryWords;                         // the next one
+    const int b = nb[k];
+    dk[k] = 0xffffffffu;
+    if (b < 8) {
+      const uint32_t sh = 16 * (b & 1);
+      const uint32_t j = ((e0[b >> 1] >> sh) & 0xffffu) + rk;
+      // the two passes disagree when a survivor falls outside its chunk's run
+      if (j < ((e1[b >> 1] >> sh) & 0xffffu)) dk[k] = si.d0[b] + j;
+      else tilebad = 1;
+    }
+    // ... or when the chunk's survivors are not the count pass's
+    const uint32_t ns = __popc(__ballot_sync(0xffffffffu, b < 8));
+    if (ns != e1[4] - e0[4]) tilebad = 1;
+    nb[k] = (uint32_t)b | (a[k].female << 4) | (a[k].bm << 5);
+  }
+}
 
 // The producer warp describes tiles three ahead (ticket, replicate data,
 // look-back, layout) and hands each to the consumers in a free stage with
@@ -964,6 +1035,9 @@ __global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(
           }
           si.kind = TK_OLD;
           si.lo = j * kTile;
+          const uint32_t n = min((uint32_t)kTile, si.end - si.lo);
+          const int u = range_of(si.pop, si.lo);
+          si.urg = (u >= 0 && si.lo + n <= si.pop.r[u].end) ? u : -1;
         }
         __syncwarp();
         return TK_OLD;
@@ -1069,52 +1143,16 @@ __global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(
       uint32_t nb[kItems];  // after phase A: next state (8: none) | female << 4 | owed draw << 5
       uint32_t dk[kItems];
       if (kind == TK_OLD) {
-        const float* c_age = (const float*)(st + 0 * kColBytes);
-        const float* c_his = (const float*)(st + 1 * kColBytes);
-        const float* c_delay = (const float*)(st + 2 * kColBytes);
-        const float* c_sporo = (const float*)(st + 3 * kColBytes);
-        const uint32_t* c_uni = (const uint32_t*)(st + 4 * kColBytes);
-        const uint32_t* c_avail = (const uint32_t*)(st + 5 * kColBytes);
-        const uint32_t* c_cycle = (const uint32_t*)(st + 6 * kColBytes);
-        const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
-        const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
-        const uint8_t* c_flags = st + 9 * kColBytes;
-        const uint32_t* c_pre = (const uint32_t*)(st + kPreOff);
-        const StepCtx& c = si.c;
-        const uint32_t lo = si.lo, end = si.end;
-#pragma unroll
-        for (int k = 0; k < kItems; k++) {
-          const uint32_t i = k * kBlock + tid;
-          const uint32_t g = lo + i;
-          const int rg = g < end ? range_of(si.pop, g) : -1;
-          nb[k] = 8;
-          a[k].bm = BM_NONE;
-          a[k].female = 0u;
-          if (rg >= 0) {
-            a[k].age = c_age[i]; a[k].his = c_his[i]; a[k].delay = c_delay[i]; a[k].sporo = c_sporo[i];
-            a[k].uni = c_uni[i]; a[k].avail = c_avail[i]; a[k].cycle = c_cycle[i]; a[k].hbc = c_hbc[i];
-            a[k].batches = c_batches[i];
-            a[k].female = (c_flags[i] >> 3) & 1u;
-            const int ns = update_agent<true>(c, mc.kill, rg, g, a[k], acc);
-            if (ns >= 0) nb[k] = ns;
-          }
-          const uint32_t peers = __match_any_sync(0xffffffffu, nb[k]);
-          const uint32_t rk = __popc(peers & lanemask_lt());
-          const uint32_t* e0 = c_pre + (k * kWarps + warp) * kPreEntryWords;  // this chunk's entry
-          const uint32_t* e1 = e0 + kPreEntryWords;                         // the next one
-          const int b = nb[k];
-          dk[k] = 0xffffffffu;
-          if (b < 8) {
-            const uint32_t sh = 16 * (b & 1);
-            const uint32_t j = ((e0[b >> 1] >> sh) & 0xffffu) + rk;
-            // the two passes disagree when a survivor falls outside its chunk's run
-            if (j < ((e1[b >> 1] >> sh) & 0xffffu)) dk[k] = si.d0[b] + j;
-            else tilebad = 1;
-          }
-          // ... or when the chunk's survivors are not the count pass's
-          const uint32_t ns = __popc(__ballot_sync(0xffffffffu, b < 8));
-          if (ns != e1[4] - e0[4]) tilebad = 1;
-          nb[k] = (uint32_t)b | (a[k].female << 4) | (a[k].bm << 5);
+        switch (si.urg) {  // CTA-uniform: a tile inside one range runs that state's code only
+          case EGG: scatter_phase_a<EGG>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case LARVA: scatter_phase_a<LARVA>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case PUPA: scatter_phase_a<PUPA>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case IMMATURE: scatter_phase_a<IMMATURE>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case MATESEEKING: scatter_phase_a<MATESEEKING>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case BMS: scatter_phase_a<BMS>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case BMD: scatter_phase_a<BMD>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case GRAVID: scatter_phase_a<GRAVID>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          default: scatter_phase_a<-1>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
         }
       }
       if (kind != TK_END) mbar_arrive(&empty[s]);  // this thread is done with the stage's inputs
