@@ -166,6 +166,7 @@ def gpu_arm(args, wl, rank, world, device):
     # --ctas-per-sm fixes them instead (profiling runs, where timings under
     # the profiler would mislead the tuner)
     fresh()
+    sim.set_small_step(None if args.small_step == "auto" else 0 if args.small_step == "off" else int(args.small_step))
     if args.ctas_per_sm:
         tuned = tuple(int(x) for x in args.ctas_per_sm.split(","))
         sim.set_grids(*tuned)
@@ -189,8 +190,11 @@ def gpu_arm(args, wl, rank, world, device):
     live = live_counts(rows)
     agent_days = float(live.sum()) / 24.0
     # kernels the library launched in the timed region (its own count: the
-    # kernel nodes of each replayed day graph plus the launches outside graphs)
+    # launches outside graphs, the kernel nodes of each replayed three-kernel
+    # day graph, and the kernels counted on the device by day graphs that
+    # pick each hour's path there)
     gpu_launches = sim.kernel_times()[1] - launches0
+    small = sim.small_step_info()
 
     # ---- roofline: the same days again, each kernel between CUDA events ----
     fresh()
@@ -258,7 +262,7 @@ def gpu_arm(args, wl, rank, world, device):
     return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(), passes=passes,
                 gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, publish_ms=publish_ms, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
-                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned)
+                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned, small=small)
 
 
 def cpu_reference(wl, seconds: float, first_steps: int | None = None, warmup: int = 0):
@@ -502,6 +506,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ctas-per-sm", default="",
                     help="COUNT,SCATTER: fixed grid sizes of the plain-path workloads instead of the autotuner")
+    ap.add_argument("--small-step", default="auto",
+                    help="plain-path workloads: 'auto' (one-launch step for pools of up to one tile per CTA of its "
+                         "grid), 'off' (the three-kernel step every hour) or a largest pool in 1024-slot tiles")
     ap.add_argument("--replicates", type=int, default=512, help="ensemble: replicates")
     ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
     ap.add_argument("--rates", default="10,100,1000", help="served: arrival rates per second")
@@ -562,7 +569,10 @@ def main():
     details = {"live_agents_min": int(live_tot.min()), "live_agents_max": int(live_tot.max()),
                "pool_bytes": [float(pool_bytes.min()), float(pool_bytes.max())], "parallelism": f"replicas x{world}",
                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1],
-                               "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"}}
+                               "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"},
+               "small_step": {"grid_ctas": r["small"]["grid"], "max_tiles": r["small"]["max_tiles"],
+                              "day_graph": {0: "none", 1: "three-kernel steps", 2: "path picked on the device, cooperative one-launch step",
+                                            3: "path picked on the device, one-launch step as a plain launch"}[r["small"]["day_graph"]]}}
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,

@@ -41,6 +41,7 @@ extern "C" {
 #define SAMPO_DEV_ERR_TILECOUNT  0x4u
 #define SAMPO_DEV_ERR_LARVATABLE 0x8u
 #define SAMPO_DEV_ERR_TMA        0x10u  /* a tile's bulk copy did not land within the wait limit */
+#define SAMPO_DEV_ERR_BARRIER    0x20u  /* the one-launch step's grid barrier was not met within the wait limit */
 /* warning bit: the step ran on the reference's initial layout with shared
  * empty ranges and produced agents in the ranges whose ends coincide; the
  * reference's compaction would have read one prefix-sum entry for several
@@ -181,6 +182,23 @@ int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_
 /* Sets the grid sizes sampo_autotune would pick, e.g. a choice tuned earlier
  * on the same workload: 1 .. the occupancy limit of each pass. */
 int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
+/* One-launch step for small pools (for such pools it replaces the per-step
+ * launch sequence of src/abms.c:502-529 that the three-kernel step already
+ * shortens): the day graphs of sampo_run pick each hourly step's path on the
+ * device. A pool of at most max_tiles 1024-slot tiles takes one cooperative
+ * kernel (update, scan and compaction with one grid barrier, publish by its
+ * last CTA); a larger one the count, update/scatter and publish kernels. Both
+ * give the same results at any size. SAMPO_SMALL_STEP_DEFAULT: one tile per
+ * CTA of the one-launch grid (the default); 0: never. sampo_step and runs
+ * with timing on always take the three-kernel path; a run-time species
+ * (sampo_set_species) too. */
+#define SAMPO_SMALL_STEP_DEFAULT 0xffffffffu
+int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles);
+/* The one-launch step's grid (CTAs; 0 when it cannot run here), the current
+ * max_tiles, and how the last day graph was built: 0 none yet, 1 three-kernel
+ * steps only, 2 path picked on the device with a cooperative one-launch
+ * step, 3 the same with a plain launch of the same co-resident grid. */
+int sampo_small_step_info(sampo_sim* s, uint32_t* grid, uint32_t* max_tiles, int* day_graph_kind);
 int sampo_checkpoint_load(sampo_sim* s, const char* path);
 /* Header of a checkpoint file (no device needed): the step it resumes at,
  * the population then, and the population at the previous step's start

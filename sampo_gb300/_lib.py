@@ -19,6 +19,7 @@ ERR_NAMES = {-1: "SAMPO_ERR_ARG", -2: "SAMPO_ERR_CUDA", -3: "SAMPO_ERR_CAPACITY"
              -5: "SAMPO_ERR_STATE", -6: "SAMPO_ERR_INTERNAL", -7: "SAMPO_ERR_IO", -8: "SAMPO_ERR_SPECIES",
              -9: "SAMPO_ERR_UNSUPPORTED"}
 DEV_ERR_CAPACITY, DEV_ERR_DEVRATES, DEV_ERR_TILECOUNT, DEV_ERR_LARVATABLE = 0x1, 0x2, 0x4, 0x8
+DEV_ERR_TMA, DEV_ERR_BARRIER = 0x10, 0x20
 DEV_WARN_REF_LAYOUT = 0x100
 STATE_NAMES = ("EGG", "LARVA", "PUPA", "IMMATURE", "MATESEEKING", "BMS", "BMD", "GRAVID")
 
@@ -135,6 +136,8 @@ SIGNATURES = {
     "sampo_checkpoint_save": (C.c_int, [_P, C.c_char_p]),
     "sampo_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
+    "sampo_set_small_step": (C.c_int, [_P, C.c_uint32]),
+    "sampo_small_step_info": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int)]),
     "sampo_species_compile": (C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(_P)]),
     "sampo_species_compile_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(_P)]),
     "sampo_species_check_text": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_size_t]),

@@ -55,13 +55,22 @@ struct sampo_sim {
   bool pending = false;                // steps queued by sampo_run_async, not yet synced
   int grid_count = 0, grid_scatter = 0;
   cudaGraphExec_t day_graph = nullptr;
-  uint32_t day_graph_kernels = 0;      // kernel nodes of day_graph (counted at capture)
+  uint32_t day_graph_kernels = 0;      // kernel nodes of day_graph (counted at capture; 0 when the device counts them)
+  int small_grid = 0;                  // CTAs of the one-launch step (0: it cannot run on this device)
+  uint32_t small_tiles = 0;            // largest pool in tiles that takes the one-launch step (0: never)
+  int day_graph_kind = 0;              // DG_* of day_graph
   bool timing = false;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   double t_count = 0, t_scatter = 0, t_total = 0;
   uint64_t launches = 0;
   std::string err;
 };
+
+// How a day graph steps the simulation: the three-kernel step every hour, or
+// each hour's path picked on the device (conditional nodes) with the
+// one-launch step launched cooperatively or (where a graph cannot hold a
+// cooperative launch) as a plain launch of the same co-resident grid.
+enum : int { DG_PLAIN = 1, DG_SWITCH_COOP = 2, DG_SWITCH = 3 };
 
 static int fail(sampo_sim* s, int code, const std::string& msg) {
   if (s) s->err = msg;
@@ -205,6 +214,8 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     }
     s->grid_count = grid_blocks_count(1);
     s->grid_scatter = grid_blocks_scatter(1);
+    s->small_grid = grid_blocks_small();
+    s->small_tiles = s->small_grid > 0 ? (uint32_t)s->small_grid : 0u;  // one tile per CTA
     for (auto& ev : s->ev) cudaEventCreate(&ev);
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_fail(s, e, "create"); break; }
   } while (0);
@@ -276,6 +287,8 @@ static int reset_state(sampo_sim* s, const sampo_population& pop) {
   // run must go: clear the tile arrays before the first step.
   h.epoch = 1;
   CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream), "tile reset");
+  // the one-launch step's grid barrier and exit counters start from zero
+  CK(cudaMemsetAsync(&s->bat_dev->bar, 0, 2 * sizeof(uint32_t), s->stream), "barrier reset");
   CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state reset");
   s->step = 0;
   return SAMPO_OK;
@@ -386,10 +399,85 @@ extern "C" int sampo_step(sampo_sim* s, const sampo_environment* env, float temp
   return check_device(s);
 }
 
+// Captures what `launches` queues on the simulation's stream into `graph`.
+template <class F>
+static cudaError_t capture_into(sampo_sim* s, cudaGraph_t graph, F launches) {
+  cudaError_t e = cudaStreamBeginCaptureToGraph(s->stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  e = launches();
+  cudaGraph_t out = graph;
+  const cudaError_t e2 = cudaStreamEndCapture(s->stream, &out);
+  return e != cudaSuccess ? e : e2;
+}
+
+// A day of 24 hourly steps whose path is picked on the device: k_select sets
+// the first hour's conditional node from the current pool, and each hour's
+// last kernel sets the next hour's (one-launch step when the next pool has at
+// most small_tiles tiles, else count + scatter + publish). Both paths give
+// the same results at any size; the pick only decides which is faster.
+static cudaError_t build_switch_graph(sampo_sim* s, bool coop, cudaGraph_t* out) {
+  const KParams p = make_params(s);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h[24];
+  for (int i = 0; i < 24 && e == cudaSuccess; i++) e = cudaGraphConditionalHandleCreate(&h[i], g, 0, cudaGraphCondAssignDefault);
+  auto with = [&](uint32_t hour, bool next) {
+    KParams q = p;
+    q.dflags = DF_COUNT | (next ? DF_COND : 0u);
+    q.cond = next ? h[hour] : 0ull;
+    q.small_tiles = s->small_tiles;
+    return q;
+  };
+  if (e == cudaSuccess) e = capture_into(s, g, [&] { return launch_select(with(0, true), s->stream); });
+  cudaGraphNode_t prev = nullptr;
+  size_t nn = 1;
+  if (e == cudaSuccess) e = cudaGraphGetNodes(g, &prev, &nn);
+  if (e == cudaSuccess && nn != 1) e = cudaErrorUnknown;
+  for (int i = 0; i < 24 && e == cudaSuccess; i++) {
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h[i];
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 2;
+    cudaGraphNode_t node = nullptr;
+    if ((e = cudaGraphAddNode(&node, g, &prev, nullptr, 1, &cp)) != cudaSuccess) break;
+    const KParams q = with(i + 1, i + 1 < 24);
+    const cudaGraph_t small_body = cp.conditional.phGraph_out[0], large_body = cp.conditional.phGraph_out[1];
+    e = capture_into(s, small_body, [&] { return launch_small(q, s->small_grid, coop, s->stream); });
+    if (e == cudaSuccess) e = capture_into(s, large_body, [&] { return launch_step(s, q); });
+    prev = node;
+  }
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    return e;
+  }
+  *out = g;
+  return cudaSuccess;
+}
+
 static int build_day_graph(sampo_sim* s) {
   if (s->day_graph) return SAMPO_OK;
   KParams p = make_params(s);
   cudaGraph_t g = nullptr;
+  // the device-picked day where the one-launch step can run (built-in
+  // species, a grid that fits the device): cooperative first
+  if (!s->species && s->small_grid > 0 && s->small_tiles > 0) {
+    for (int kind : {DG_SWITCH_COOP, DG_SWITCH}) {
+      if (build_switch_graph(s, kind == DG_SWITCH_COOP, &g) != cudaSuccess) continue;
+      cudaError_t e = cudaGraphInstantiate(&s->day_graph, g, 0);
+      cudaGraphDestroy(g);
+      g = nullptr;
+      if (e == cudaSuccess) {
+        s->day_graph_kind = kind;
+        s->day_graph_kernels = 0;  // counted on the device (BatchDev::dev_launches)
+        return SAMPO_OK;
+      }
+      s->day_graph = nullptr;
+      (void)cudaGetLastError();
+    }
+  }
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture");
   cudaError_t e = cudaSuccess;
   for (int h = 0; h < 24 && e == cudaSuccess; h++) e = launch_step(s, p);
@@ -412,6 +500,34 @@ static int build_day_graph(sampo_sim* s) {
   e = cudaGraphInstantiate(&s->day_graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) { s->day_graph = nullptr; return cuda_fail(s, e, "graph instantiate"); }
+  s->day_graph_kind = DG_PLAIN;
+  return SAMPO_OK;
+}
+
+static void drop_day_graph(sampo_sim* s) {
+  if (s->day_graph) {
+    cudaGraphExecDestroy(s->day_graph);
+    s->day_graph = nullptr;
+  }
+  s->day_graph_kind = 0;
+}
+
+extern "C" int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles) {
+  if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
+  if (max_tiles == SAMPO_SMALL_STEP_DEFAULT) max_tiles = s->small_grid > 0 ? (uint32_t)s->small_grid : 0u;
+  if (max_tiles != s->small_tiles) {
+    s->small_tiles = max_tiles;
+    drop_day_graph(s);
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_small_step_info(sampo_sim* s, uint32_t* grid, uint32_t* max_tiles, int* day_graph_kind) {
+  if (!s) return SAMPO_ERR_ARG;
+  if (grid) *grid = (uint32_t)s->small_grid;
+  if (max_tiles) *max_tiles = s->small_tiles;
+  if (day_graph_kind) *day_graph_kind = s->day_graph_kind;
   return SAMPO_OK;
 }
 
@@ -421,6 +537,9 @@ extern "C" int sampo_set_timing(sampo_sim* s, int on) {
   s->timing = on != 0;
   s->t_count = s->t_scatter = s->t_total = 0;
   s->launches = 0;
+  cudaSetDevice(s->device);
+  CK(cudaMemsetAsync(&s->bat_dev->dev_launches, 0, sizeof(unsigned long long), s->stream), "launch count");
+  CK(cudaStreamSynchronize(s->stream), "launch count");
   return SAMPO_OK;
 }
 
@@ -737,10 +856,7 @@ extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_
   if (gc != s->grid_count || gs != s->grid_scatter) {
     s->grid_count = gc;
     s->grid_scatter = gs;
-    if (s->day_graph) {  // captured with the old grids
-      cudaGraphExecDestroy(s->day_graph);
-      s->day_graph = nullptr;
-    }
+    drop_day_graph(s);  // captured with the old grids
   }
   if (count_ctas_per_sm) *count_ctas_per_sm = (uint32_t)(gc / sms);
   if (scatter_ctas_per_sm) *scatter_ctas_per_sm = (uint32_t)(gs / sms);
@@ -756,10 +872,7 @@ extern "C" int sampo_set_species(sampo_sim* s, const sampo_species* sp) {
   s->species = sp;
   s->grid_count = grid_blocks_count(1, sp);
   s->grid_scatter = grid_blocks_scatter(1, sp);
-  if (s->day_graph) {  // captured with the other kernels
-    cudaGraphExecDestroy(s->day_graph);
-    s->day_graph = nullptr;
-  }
+  drop_day_graph(s);  // captured with the other kernels
   return SAMPO_OK;
 }
 
@@ -779,10 +892,7 @@ extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_
   if (gc != s->grid_count || gs != s->grid_scatter) {
     s->grid_count = gc;
     s->grid_scatter = gs;
-    if (s->day_graph) {  // captured with the old grids
-      cudaGraphExecDestroy(s->day_graph);
-      s->day_graph = nullptr;
-    }
+    drop_day_graph(s);  // captured with the old grids
   }
   return SAMPO_OK;
 }
@@ -807,7 +917,14 @@ extern "C" int sampo_kernel_times(sampo_sim* s, double out[3], uint64_t* launche
   if (!s || !out) return SAMPO_ERR_ARG;
   SETTLE(s);
   out[0] = s->t_count; out[1] = s->t_scatter; out[2] = s->t_total;
-  if (launches) *launches = s->launches;
+  if (launches) {
+    // launches made by the host, plus those of device-picked day graphs
+    unsigned long long dev = 0;
+    cudaSetDevice(s->device);
+    CK(cudaMemcpyAsync(&dev, &s->bat_dev->dev_launches, sizeof(dev), cudaMemcpyDeviceToHost, s->stream), "launch count");
+    CK(cudaStreamSynchronize(s->stream), "launch count");
+    *launches = s->launches + dev;
+  }
   return SAMPO_OK;
 }
 

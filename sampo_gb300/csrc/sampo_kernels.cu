@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <mutex>
 #include "sampo_step_kernels.cuh"
+#include "sampo_small_step.cuh"
 
 namespace sampo {
 
@@ -185,6 +186,33 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
   *grid_scatter = bs * sms;
   if (best_ms) *best_ms = tc[bc] + ts[bs];
   return e;
+}
+int grid_blocks_small() {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_small, kSmallThreads, kSmallStage) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return sm_count() * per;
+}
+cudaError_t launch_small(const KParams& p, int grid, bool cooperative, cudaStream_t st) {
+  KParams q = p;
+  void* args[] = {&q};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kSmallThreads);
+  cfg.dynamicSmemBytes = kSmallStage;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = cooperative ? 1 : 0;
+  return cudaLaunchKernelExC(&cfg, (const void*)k_step_small, args);
+}
+cudaError_t launch_select(const KParams& p, cudaStream_t st) {
+  k_select<<<1, 1, 0, st>>>(p);
+  return cudaGetLastError();
 }
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {
   k_eval_math<<<sm_count() * 2, 256, 0, st>>>(fn, x, y, out, n);

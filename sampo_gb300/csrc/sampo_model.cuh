@@ -14,7 +14,8 @@
 // (only the fields that decide survival, the next state and the number of
 // eggs laid) and FULL=true by the scatter pass (the complete record). Both
 // instantiations run the same decision code on the same inputs, so they
-// agree bit for bit.
+// agree bit for bit. EGGS adds the eggs laid to Acc::newEggs (the counting
+// pass, and the one-launch step, whose single update decides and writes).
 #pragma once
 #include <stdint.h>
 #include "sampo_math.h"
@@ -158,7 +159,7 @@ __device__ __forceinline__ uint32_t age_days_uncapped(float age) {
 
 // Kill then update one valid agent of range rg at slot gid.
 // Returns the next state (0..7), or -1 when the agent dies this step.
-template <bool FULL>
+template <bool FULL, bool EGGS = !FULL>
 __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& mc, int rg, uint32_t gid, Rec& a, Acc& acc) {
   // ---- killAgents (kernel/killAgents.cl:52-147) ----
   {
@@ -277,13 +278,13 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& m
 #ifdef SAMPO_USER_SPECIES
             uint32_t pe = 0;
             avail = species_lay_eggs(c, gid, a, avail, pe);
-            if (!FULL) acc.newEggs += pe;
+            if (EGGS) acc.newEggs += pe;
 #else
             // layEggs (include/properties.h:296-307)
             float nbm = u32_to_f32_rn(c.totalBiomass) / ((u32_to_f32_rn(a.uni) + 1.0f) * c.env.carryingCapacity);
             float pbm = sampo_fmaxf(0.0f, 1.0f - nbm);
             uint32_t pe = f2u_sat_fast(ceilf(u32_to_f32_rn(avail) * pbm));
-            if (!FULL) acc.newEggs += pe;
+            if (EGGS) acc.newEggs += pe;
             avail = avail - pe;
 #endif
           }

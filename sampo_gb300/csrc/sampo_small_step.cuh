@@ -1,0 +1,525 @@
+// sampo_small_step.cuh - the hourly step of one simulation in one launch, for
+// pools of up to a few hundred 1024-slot tiles (sm_103a).
+//
+// At that size the three-kernel step (k_count, k_scatter, k_publish) is bound
+// by each kernel's start-up and latency chain, not by bandwidth. k_step_small
+// does the same step in one cooperative launch with one CTA per tile:
+//
+//  phase 1  CTA b loads tile b (TMA bulk copies) and runs the full update of
+//           its agents once (killAgents + updateAgents with the species
+//           functions and the normal draws). The updated records stay in the
+//           CTA's shared memory with their next state in the flag byte; the
+//           CTA builds the tile's prefix table over its (round, warp) chunks
+//           in shared memory and publishes the tile's survivors per next
+//           state and its eggs laid to global memory.
+//  barrier  a grid barrier with a bounded wait.
+//  phase 2  every CTA sums the per-tile counts: the totals give the next
+//           layout (kernel/oldToNewAgents.cl:57-95), the tiles before its own
+//           the tile's first slot in each next-state range. It writes its
+//           survivors from shared memory to their slots in the next buffer,
+//           the new eggs of its egg tiles at [0, newEggs)
+//           (kernel/initAgents.cl:26-65), and adds its share of the next
+//           pool's statistics (calcL1de.cl, calcGender.cl).
+//  publish  the last CTA to finish publishes the next step (the k_publish
+//           code) and, in a day graph that picks each step's path on the
+//           device, sets the path of the step after.
+//
+// Pools with more tiles than CTAs are still stepped correctly: CTA b also
+// takes tiles b + G, b + 2G, ... (G CTAs); their decisions are counted in
+// phase 1 and the tile is loaded and updated again in phase 2.
+//
+// Built into the library for the built-in species only (a user species keeps
+// the three-kernel step).
+#pragma once
+#include "sampo_step_kernels.cuh"
+
+namespace sampo {
+
+constexpr int kSmallThreads = kBlock;      // eight warps, kItems slots per thread
+constexpr int kSmallMinBlocks = 3;         // resident CTAs per SM the registers are sized for
+constexpr uint32_t kSmallStage = kPreOff;  // the ten columns of one tile
+constexpr uint32_t kSmallRows = 9;         // per-tile counts: survivors by next state, eggs laid
+constexpr uint8_t kGone = 0xffu;           // flag byte of a slot without a survivor
+static_assert(kSmallRows <= kPreWords, "the per-tile count rows fit the prefix-table array");
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// All CTAs of the grid (co-resident: a cooperative launch) wait until each
+// has arrived. Bounded: false when the others did not arrive within the
+// limit. Every thread calls it; every thread gets the same answer.
+__device__ bool small_grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // this CTA's writes before its arrival
+    atomicAdd(bar, 1u);
+    uint32_t ok = 0;
+    for (uint32_t i = 0; i < kWaitLimit; i++) {
+      if (ld_acquire_u32(bar) >= nblocks) { ok = 1; break; }
+      __nanosleep(64);
+    }
+    __threadfence();
+    *s_flag = ok;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+struct SmallAcc {
+  Acc acc;                            // counters of the update (bites, cycles, eggs laid, table misses)
+  uint32_t l1, fem, inf, dmin, dmax;  // statistics of the next pool
+  uint32_t devoob, tilebad;
+};
+
+// Phase 1 (and phase 2 for a tile updated again): the full update of the
+// tile in stage memory st (slots lo .. lo + kTile of the current pool). With
+// KEEP the updated records and their next state (flag byte; kGone for none)
+// are written back to the stage. Every (round, warp) chunk's survivors by
+// next state go to s_ent. EGGS / STATS: the eggs laid / the update's
+// counters and the next pool's statistics go to sa (a tile updated twice
+// counts its eggs the first time and the rest the second).
+template <bool KEEP, bool EGGS, bool STATS>
+__device__ __forceinline__ void small_update_tile(const StepCtx& c, const ModelConst& mc, const sampo_population& pop,
+                                                  uint8_t* st, uint32_t lo, uint32_t end, uint2* s_ent, SmallAcc& sa) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float* c_age = (float*)(st + 0 * kColBytes);
+  float* c_his = (float*)(st + 1 * kColBytes);
+  float* c_delay = (float*)(st + 2 * kColBytes);
+  float* c_sporo = (float*)(st + 3 * kColBytes);
+  uint32_t* c_uni = (uint32_t*)(st + 4 * kColBytes);
+  uint32_t* c_avail = (uint32_t*)(st + 5 * kColBytes);
+  uint32_t* c_cycle = (uint32_t*)(st + 6 * kColBytes);
+  uint32_t* c_hbc = (uint32_t*)(st + 7 * kColBytes);
+  uint32_t* c_batches = (uint32_t*)(st + 8 * kColBytes);
+  uint8_t* c_flags = st + 9 * kColBytes;
+  Acc t = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+  for (int k = 0; k < kItems; k++) {
+    const uint32_t i = k * kBlock + tid;
+    const uint32_t g = lo + i;
+    const int rg = g < end ? range_of(pop, g) : -1;
+    uint32_t pk0 = 0, pk1 = 0;  // this slot's next state as an 8-bit counter: states 0-3, 4-7
+    uint8_t fb = kGone;
+    if (rg >= 0) {
+      Rec a;
+      a.age = c_age[i]; a.his = c_his[i]; a.delay = c_delay[i]; a.sporo = c_sporo[i];
+      a.uni = c_uni[i]; a.avail = c_avail[i]; a.cycle = c_cycle[i]; a.hbc = c_hbc[i];
+      a.batches = c_batches[i];
+      a.female = (c_flags[i] >> 3) & 1u;
+      a.bm = BM_NONE;
+      sa.devoob |= (rg == LARVA) & c.devOOB;
+      const int ns = update_agent<true, true>(c, mc.kill, rg, g, a, t);
+      if (ns >= 0) {
+        if (a.bm != BM_NONE) {  // the owed normal draw (include/gpuRand.h:56-63)
+          const uint32_t v = finish_box_muller(c, mc, g, a.bm, a.batches);
+          if (a.bm == BM_LARVA_DELAY) a.delay = __uint_as_float(v);
+          else a.avail = v;
+        }
+        if (ns < 4) pk0 = 1u << (8 * ns);
+        else pk1 = 1u << (8 * (ns - 4));
+        fb = (uint8_t)(ns | (a.female << 3));
+        if (STATS) {  // kernel/calcL1de.cl:28-30, kernel/calcGender.cl:24-37
+          if (ns == LARVA) {
+            sa.l1 += age_days_uncapped(a.age);
+            const uint32_t dd = age_days(a.age);
+            sa.dmin = min(sa.dmin, dd); sa.dmax = max(sa.dmax, dd);
+          } else if (ns >= IMMATURE && a.female) {
+            sa.fem += 1u;
+            sa.inf += a.sporo >= 1.0f ? 1u : 0u;
+          }
+        }
+        if (KEEP) {
+          c_age[i] = a.age; c_his[i] = a.his; c_delay[i] = a.delay; c_sporo[i] = a.sporo;
+          c_uni[i] = a.uni; c_avail[i] = a.avail; c_cycle[i] = a.cycle; c_hbc[i] = a.hbc;
+          c_batches[i] = a.batches;
+        }
+      }
+    }
+    if (KEEP) c_flags[i] = fb;
+    pk0 = __reduce_add_sync(0xffffffffu, pk0);
+    pk1 = __reduce_add_sync(0xffffffffu, pk1);
+    if (lane == 0) s_ent[k * kWarps + warp] = make_uint2(pk0, pk1);
+  }
+  if (EGGS) sa.acc.newEggs += t.newEggs;
+  if (STATS) {
+    sa.acc.bites += t.bites; sa.acc.infectBites += t.infectBites;
+    sa.acc.cycles += t.cycles; sa.acc.sumCycles += t.sumCycles;
+  }
+  sa.acc.bad |= t.bad;
+}
+
+// Warp 0, after the tile's chunk counts are in s_ent: the tile's prefix table
+// (the same 16-bit packed entries as the count pass's) into s_tab, and the
+// tile's survivors of next state `lane` to lanes 0..7.
+__device__ __forceinline__ uint32_t small_build_table(const uint2* s_ent, uint32_t* s_tab) {
+  const int lane = threadIdx.x & 31;
+  const uint2 e = lane < (int)kChunks ? s_ent[lane] : make_uint2(0u, 0u);
+  uint32_t w[5], x[5];
+  w[0] = (e.x & 0xffu) | ((e.x & 0xff00u) << 8);
+  w[1] = ((e.x >> 16) & 0xffu) | ((e.x >> 8) & 0xff0000u);
+  w[2] = (e.y & 0xffu) | ((e.y & 0xff00u) << 8);
+  w[3] = ((e.y >> 16) & 0xffu) | ((e.y >> 8) & 0xff0000u);
+  w[4] = ((e.x * 0x01010101u) >> 24) + ((e.y * 0x01010101u) >> 24);  // byte sums <= 32 cannot carry
+#pragma unroll
+  for (int q = 0; q < 5; q++) x[q] = w[q];
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x[q], o);
+      if (lane >= o) x[q] += y;
+    }
+  }
+  if (lane < (int)kChunks) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) s_tab[lane * kPreEntryWords + q] = x[q] - w[q];
+  }
+  if (lane == (int)kChunks - 1) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) s_tab[kChunks * kPreEntryWords + q] = x[q];
+  }
+  uint32_t tw = 0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const uint32_t tq = __shfl_sync(0xffffffffu, x[q], kChunks - 1);
+    if ((lane >> 1) == q) tw = (tq >> (16 * (lane & 1))) & 0xffffu;
+  }
+  return tw;
+}
+
+// Phase 2: the survivors of the tile in stage memory st (after
+// small_update_tile<true, ...> and its table) to their slots in the next
+// buffer: the tile's first slot of the state (s_d0) + the survivors of that
+// state in earlier chunks (s_tab) + the rank within the chunk. A survivor
+// whose slot falls outside its chunk's run sets tilebad and is not stored.
+__device__ __forceinline__ void small_scatter_tile(const uint8_t* st, const uint32_t* s_tab, const uint32_t* s_d0,
+                                                   const DevPool& dst, uint32_t& tilebad) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const float* c_age = (const float*)(st + 0 * kColBytes);
+  const float* c_his = (const float*)(st + 1 * kColBytes);
+  const float* c_delay = (const float*)(st + 2 * kColBytes);
+  const float* c_sporo = (const float*)(st + 3 * kColBytes);
+  const uint32_t* c_uni = (const uint32_t*)(st + 4 * kColBytes);
+  const uint32_t* c_avail = (const uint32_t*)(st + 5 * kColBytes);
+  const uint32_t* c_cycle = (const uint32_t*)(st + 6 * kColBytes);
+  const uint32_t* c_hbc = (const uint32_t*)(st + 7 * kColBytes);
+  const uint32_t* c_batches = (const uint32_t*)(st + 8 * kColBytes);
+  const uint8_t* c_flags = st + 9 * kColBytes;
+#pragma unroll
+  for (int k = 0; k < kItems; k++) {
+    const uint32_t i = k * kBlock + tid;
+    const uint8_t fb = c_flags[i];
+    const int b = fb == kGone ? 8 : (fb & 7);
+    const uint32_t peers = __match_any_sync(0xffffffffu, (uint32_t)b);
+    const uint32_t rk = __popc(peers & lanemask_lt());
+    if (b < 8) {
+      const uint32_t* e0 = s_tab + (k * kWarps + warp) * kPreEntryWords;
+      const uint32_t* e1 = e0 + kPreEntryWords;
+      const uint32_t sh = 16 * (b & 1);
+      const uint32_t j = ((e0[b >> 1] >> sh) & 0xffffu) + rk;
+      if (j < ((e1[b >> 1] >> sh) & 0xffffu)) {
+        const uint32_t d = s_d0[b] + j;
+        dst.age[d] = c_age[i]; dst.his[d] = c_his[i]; dst.delay[d] = c_delay[i]; dst.sporo[d] = c_sporo[i];
+        dst.uni[d] = c_uni[i]; dst.avail[d] = c_avail[i]; dst.cycle[d] = c_cycle[i]; dst.hbc[d] = c_hbc[i];
+        dst.batches[d] = c_batches[i];
+        dst.flags[d] = fb;
+      } else {
+        tilebad = 1;
+      }
+    }
+  }
+}
+
+// Phase 2, warps 0..7 (row w; warp 0 also row 8): the sums over the per-tile
+// counts of tiles [0, t) into s_ex and, with `totals`, over all nold tiles
+// into s_tot. Rows are state-major: rows[row * stride + tile], read through L2.
+__device__ __forceinline__ void small_sum_rows(const uint32_t* rows, uint32_t stride, uint32_t nold, uint32_t t,
+                                               bool totals, uint32_t* s_ex, uint32_t* s_tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int row = warp; row < (int)kSmallRows; row += kWarps) {
+    const uint32_t* r = rows + (size_t)row * stride;
+    const uint32_t lim = totals ? nold : t;
+    uint32_t ex = 0, tot = 0;
+    for (uint32_t j = lane; j < lim; j += 32) {
+      const uint32_t v = __ldcg(r + j);
+      tot += v;
+      ex += j < t ? v : 0u;
+    }
+    ex = __reduce_add_sync(0xffffffffu, ex);
+    tot = __reduce_add_sync(0xffffffffu, tot);
+    if (lane == 0) {
+      s_ex[row] = ex;
+      if (totals) s_tot[row] = tot;
+    }
+  }
+}
+
+// Every thread waits (bounded) for the bulk copies of the stage's tile;
+// false for all when any wait ran out.
+__device__ __forceinline__ bool small_wait_stage(uint64_t* bar, uint32_t& phase) {
+  const bool ok = mbar_wait(bar, phase);
+  phase ^= 1u;
+  return __syncthreads_and(ok) != 0;
+}
+
+__device__ __forceinline__ void small_issue_tile(const DevPool& src, uint8_t* st, uint64_t* bar, uint32_t lo, uint32_t n) {
+  const uint32_t b4 = (n * 4 + 15) & ~15u, b1 = (n + 15) & ~15u;
+  mbar_arrive_tx(bar, 9 * b4 + b1);
+  bulk_load(st + 0 * kColBytes, src.age + lo, b4, bar);
+  bulk_load(st + 1 * kColBytes, src.his + lo, b4, bar);
+  bulk_load(st + 2 * kColBytes, src.delay + lo, b4, bar);
+  bulk_load(st + 3 * kColBytes, src.sporo + lo, b4, bar);
+  bulk_load(st + 4 * kColBytes, src.uni + lo, b4, bar);
+  bulk_load(st + 5 * kColBytes, src.avail + lo, b4, bar);
+  bulk_load(st + 6 * kColBytes, src.cycle + lo, b4, bar);
+  bulk_load(st + 7 * kColBytes, src.hbc + lo, b4, bar);
+  bulk_load(st + 8 * kColBytes, src.batches + lo, b4, bar);
+  bulk_load(st + 9 * kColBytes, src.flags + lo, b1, bar);
+}
+
+// The one-launch step of p.reps[0] (a single simulation). The per-tile count
+// rows use the replicate's prefix-table array (tilePre: kPreWords words per
+// tile, of which the rows take kSmallRows), which the three-kernel step
+// rewrites before it reads it.
+__global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(KParams p) {
+  extern __shared__ __align__(128) uint8_t stage[];
+  __shared__ StepCtx s_c;
+  __shared__ ModelConst s_mc;
+  __shared__ sampo_population s_pop;
+  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ uint2 s_ent[kChunks];
+  __shared__ __align__(16) uint32_t s_tab[(kChunks + 1) * kPreEntryWords];
+  __shared__ uint32_t s_ex[kSmallRows], s_tot[kSmallRows], s_d0[8], s_ne[kWarps];
+  __shared__ uint32_t s_red[kWarps][10];
+  __shared__ uint32_t s_flag, s_ok, s_last;
+  __shared__ uint32_t s_active, s_end, s_nold, s_cur, s_cap, s_stride;
+  const RepParams& rp = p.reps[0];
+  SimDev* sim = rp.sim;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t G = gridDim.x, b = blockIdx.x;
+  uint32_t phase = 0;
+
+  // ---- prologue: the tile's copies first, then the step's constants ----
+  if (tid == 0) {
+    mbar_init(&s_mbar);
+    fence_mbar_init();
+    const uint32_t active = sim->active;
+    const sampo_population pop = sim->pop;
+    const uint32_t end = active ? pop.r[GRAVID].end : 0u;
+    const uint32_t cur = sim->cur;
+    s_pop = pop;
+    s_active = active;
+    s_end = end;
+    s_nold = (end + kTile - 1) / kTile;
+    s_cur = cur;
+    s_cap = sim->capacity;
+    s_stride = rp.maxTiles;
+    if (b < s_nold) {
+      const uint32_t lo = b * kTile;
+      small_issue_tile(rp.pool[cur], stage, &s_mbar, lo, min((uint32_t)kTile, end - lo));
+    }
+  }
+  copy16(&s_c, &sim->ctx, (int)sizeof(StepCtx), tid, blockDim.x);
+  load_model_const(p.mc, s_mc);
+  __syncthreads();
+  const uint32_t nold = s_nold, end = s_end, stride = s_stride;
+  uint32_t* rows = rp.tilePre;  // [kSmallRows][stride]
+  SmallAcc sa;
+  sa.acc = Acc{0, 0, 0, 0, 0, 0};
+  sa.l1 = sa.fem = sa.inf = sa.dmax = sa.devoob = sa.tilebad = 0;
+  sa.dmin = 0xffffffffu;
+  bool ok = true;
+
+  // ---- phase 1: decide (and, for tile b, finish) every tile of this CTA ----
+  if (nold > G && b < nold) {
+    // more tiles than CTAs: count tile b (its copies were issued above)
+    // without keeping it, then the other tiles of this CTA one after the
+    // other in the stage, then load tile b again and keep it
+    ok = small_wait_stage(&s_mbar, phase);
+    for (uint32_t t = b; t < nold && ok; t += G) {
+      if (t != b) {
+        if (tid == 0) {
+          fence_proxy_async();  // the stage was last read through the generic proxy
+          small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+        }
+        ok = small_wait_stage(&s_mbar, phase);
+        if (!ok) break;
+      }
+      const uint32_t eggs_before = sa.acc.newEggs;
+      small_update_tile<false, true, false>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
+      const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
+      if (lane == 0) s_ne[warp] = ne;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t tw = small_build_table(s_ent, s_tab);
+        if (lane < 8) __stcg(rows + (size_t)lane * stride + t, tw);
+        uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
+        e = __reduce_add_sync(0xffffffffu, e);
+        if (lane == 0) __stcg(rows + (size_t)8 * stride + t, e);
+      }
+      __syncthreads();  // the stage is read before the next copy overwrites it
+    }
+    if (ok) {
+      if (tid == 0) {
+        fence_proxy_async();
+        small_issue_tile(rp.pool[s_cur], stage, &s_mbar, b * kTile, min((uint32_t)kTile, end - b * kTile));
+      }
+      ok = small_wait_stage(&s_mbar, phase);
+      if (ok) {
+        small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);  // eggs counted above
+        __syncthreads();
+        if (warp == 0) (void)small_build_table(s_ent, s_tab);
+      }
+    }
+  } else if (b < nold) {
+    ok = small_wait_stage(&s_mbar, phase);
+    if (ok) {
+      const uint32_t eggs_before = sa.acc.newEggs;
+      small_update_tile<true, true, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);
+      const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
+      if (lane == 0) s_ne[warp] = ne;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t tw = small_build_table(s_ent, s_tab);
+        if (lane < 8) __stcg(rows + (size_t)lane * stride + b, tw);
+        uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
+        e = __reduce_add_sync(0xffffffffu, e);
+        if (lane == 0) __stcg(rows + (size_t)8 * stride + b, e);
+      }
+    }
+  }
+  if (tid == 0) s_ok = ok ? 1u : 0u;
+
+  // ---- grid barrier: every tile's counts are published ----
+  const bool met = small_grid_barrier(&p.bat->bar, G, &s_flag);
+  ok = s_ok != 0;  // this CTA's copies all landed
+
+  // ---- phase 2: totals, next layout, this tile's first slots; scatter ----
+  small_sum_rows(rows, stride, nold, b < nold ? b : nold, true, s_ex, s_tot);
+  __syncthreads();
+  uint32_t tot[8], base[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) tot[k] = s_tot[k];
+  const uint32_t ne = s_tot[8];
+  const bool fits = layout_fits(tot, ne, s_cap);
+  {
+    sampo_population np;
+    next_layout(tot, ne, np, base);
+  }
+  if (b == 0 && tid == 0 && s_active && met) {
+    // the totals the publish reads (the three-kernel step adds them up by atomics)
+#pragma unroll
+    for (int k = 0; k < 8; k++) sim->cnt[k] = tot[k];
+    sim->newEggs = ne;
+    if (!fits) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
+  }
+  const bool write = ok && met && fits && s_active;
+  const DevPool dst = rp.pool[s_cur ^ 1u];
+  if (write && b < nold) {
+    if (tid < 8) s_d0[tid] = base[tid] + s_ex[tid];
+    __syncthreads();
+    small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
+    // more tiles than CTAs: the other tiles of this CTA, loaded and updated again
+    for (uint32_t t = b + G; t < nold; t += G) {
+      __syncthreads();  // the stage is read
+      if (tid == 0) {
+        fence_proxy_async();
+        small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+      }
+      if (!small_wait_stage(&s_mbar, phase)) { ok = false; break; }
+      small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
+      small_sum_rows(rows, stride, nold, t, false, s_ex, s_tot);
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t tw = small_build_table(s_ent, s_tab);
+        // the update again must give the counts of phase 1
+        if (lane < 8 && tw != __ldcg(rows + (size_t)lane * stride + t)) sa.tilebad = 1;
+        if (lane < 8) s_d0[lane] = base[lane] + s_ex[lane];
+      }
+      if (__syncthreads_or(sa.tilebad)) break;
+      small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
+    }
+  }
+  if (write) {
+    // new eggs at [0, newEggs) of the next buffer, egg tile e on CTA G-1-(e mod G)
+    const uint32_t negg = (ne + kTile - 1) / kTile;
+    for (uint32_t e = G - 1 - b; e < negg; e += G) {
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        const uint32_t id = e * kTile + k * kBlock + tid;
+        if (id < ne) {
+          Rec a;
+          new_egg(s_c, id, a);
+          dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
+          dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
+          dst.batches[id] = a.batches;
+          dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
+        }
+      }
+    }
+  }
+
+  // ---- this CTA's statistics: reduced in the CTA, one atomic per counter ----
+  {
+    uint32_t v[10] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
+                      (sa.acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (sa.tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u) |
+                          (sa.devoob ? SAMPO_DEV_ERR_DEVRATES : 0u) | (ok ? 0u : SAMPO_DEV_ERR_TMA) |
+                          (met ? 0u : SAMPO_DEV_ERR_BARRIER),
+                      sa.dmin, sa.dmax};
+#pragma unroll
+    for (int j = 0; j < 7; j++) v[j] = __reduce_add_sync(0xffffffffu, v[j]);
+    v[7] = __reduce_or_sync(0xffffffffu, v[7]);
+    v[8] = __reduce_min_sync(0xffffffffu, v[8]);
+    v[9] = __reduce_max_sync(0xffffffffu, v[9]);
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < 10; j++) s_red[warp][j] = v[j];
+    }
+    __syncthreads();
+    if (tid < 10 && s_active) {
+      uint32_t x = s_red[0][tid];
+      for (int w = 1; w < kWarps; w++) {
+        const uint32_t y = s_red[w][tid];
+        x = tid < 7 ? x + y : tid == 7 ? (x | y) : tid == 8 ? min(x, y) : max(x, y);
+      }
+      uint32_t* const acc0 = tid == 0 ? &sim->acc_L1de : tid == 1 ? &sim->acc_fem : tid == 2 ? &sim->acc_inf
+                                                                                            : &sim->acc_bnc[tid < 7 ? tid - 3 : 0];
+      if (tid < 7) { if (x) atomicAdd(acc0, x); }
+      else if (tid == 7) { if (x) atomicOr(&sim->error, x); }
+      else if (tid == 8) { if (x != 0xffffffffu) atomicMin(&sim->acc_dmin, x); }
+      else { if (x) atomicMax(&sim->acc_dmax, x); }
+    }
+  }
+  // a copy that did not land in time may still be in flight: let it land
+  // (bounded) before the CTA can exit
+  if (!ok && tid == 0) (void)mbar_wait(&s_mbar, phase ^ 1u);
+
+  // ---- the last CTA out publishes the next step ----
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    s_last = atomicAdd(&p.bat->done, 1u) == G - 1u ? 1u : 0u;
+    if (s_last) __threadfence();
+  }
+  __syncthreads();
+  if (!s_last) return;
+  const uint32_t next_end = publish_rep(p, 0u, PUB_AFTER_STEP);
+  if (tid == 0) {
+    p.bat->bar = 0u;
+    p.bat->done = 0u;
+    set_next_path(p, next_end, 1u);
+  }
+}
+
+// The first conditional node of a day graph: the path of its first step from
+// the current pool.
+__global__ void k_select(KParams p) {
+  const SimDev* sim = p.reps[0].sim;
+  const uint32_t end = sim->active ? sim->pop.r[GRAVID].end : 0u;
+  set_next_path(p, end, 1u);
+}
+
+}  // namespace sampo

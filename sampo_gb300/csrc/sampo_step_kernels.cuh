@@ -606,31 +606,50 @@ __global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
 }
 
 // ------------------------------------------------------------------------
-// Publishing the start of a step for every replicate of p (one CTA each):
-// after a step, the next layout from the survivor counts
-// (kernel/oldToNewAgents.cl:57-95); then the pool's L1de, female and
-// infective counts (calcStats, src/abms.c:230-310), the stats row, the next
-// step's constants and the larval hourly mortality for every larva age
-// present (kernel/killAgents.cl:117-133 depends on the age and L1de only).
-// Reads and clears the acc_* accumulators; block 0 rearms the tickets.
-// mode PUB_REFRESH only recomputes the input-dependent step constants (the
-// inputs of the coming step may have been written after its publish).
+// Publishing the start of a step
 // ------------------------------------------------------------------------
 // warp 0 publishes; warps 1-4 fill the 100 entries of the larval table at once
 constexpr int kPublishThreads = 160;
-__global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode) {
-  __shared__ uint32_t s_go, s_l1, s_dmin, s_dmax;
+
+// A replicate's state read through L2 (ld.global.cg): in the one-launch step
+// other CTAs of the same kernel wrote it, and this SM's L1 may hold older
+// copies of the same lines.
+template <class T>
+__device__ __forceinline__ T ld_l2(const T* p) {
+  static_assert(sizeof(T) % 4 == 0, "whole words");
+  T v;
+  uint32_t* d = reinterpret_cast<uint32_t*>(&v);
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+#pragma unroll
+  for (int k = 0; k < (int)(sizeof(T) / 4); k++) d[k] = __ldcg(q + k);
+  return v;
+}
+
+// Whether a pool ending at slot `end` takes the one-launch step.
+__device__ __forceinline__ uint32_t small_pick(uint32_t end, uint32_t small_tiles) {
+  return (end + kTile - 1) / kTile <= small_tiles ? 1u : 0u;
+}
+
+// The publish of replicate r by the calling CTA (at least kPublishThreads
+// threads; all of them call it): after a step, the next layout from the
+// survivor counts (kernel/oldToNewAgents.cl:57-95); then the pool's L1de,
+// female and infective counts (calcStats, src/abms.c:230-310), the stats
+// row, the next step's constants and the larval hourly mortality for every
+// larva age present (kernel/killAgents.cl:117-133 depends on the age and
+// L1de only). Reads and clears the acc_* accumulators. Mode PUB_REFRESH only
+// recomputes the input-dependent step constants (the inputs of the coming
+// step may have been written after its publish). Returns the end of the
+// replicate's pool after the publish (0 when it is inactive) to every thread.
+__device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
+  __shared__ uint32_t s_go, s_l1, s_dmin, s_dmax, s_end;
   __shared__ float s_cc;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    p.bat->ticket1 = 0u;
-    p.bat->ticket2 = 0u;
-  }
-  const RepParams& rp = p.reps[blockIdx.x];
+  const RepParams& rp = p.reps[r];
   SimDev* sim = rp.sim;
   if (threadIdx.x < 32) {
     // a device seed stream draws the coming step's seeds once, before thread 0 reads them
-    const uint32_t coming = sim->step + (mode == PUB_AFTER_STEP ? 1u : 0u);
-    if (sim->active && sim->rnd.next == coming && coming < sim->stop_step) draw_step_seeds(rp, coming);
+    const uint32_t coming = __ldcg(&sim->step) + (mode == PUB_AFTER_STEP ? 1u : 0u);
+    if (__ldcg(&sim->active) && __ldcg(&sim->rnd.next) == coming && coming < __ldcg(&sim->stop_step))
+      draw_step_seeds(rp, coming);
     __syncwarp();
   }
   if (mode == PUB_REFRESH) {
@@ -641,7 +660,7 @@ __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode
       make_ctx(in, sim->larvaHMR, sim->pop, c);
       sim->ctx = c;
     }
-    return;
+    return 0u;
   }
   const bool after_step = mode == PUB_AFTER_STEP;
   // Thread 0 reads all it needs before its first store (a store that may
@@ -654,23 +673,23 @@ __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode
   uint32_t step = 0, stop = 0, epoch = 0, cur = 0, warn = 0;
   bool relayout = false, shared_end_warn = false;
   if (threadIdx.x == 0) {
-    const uint32_t active = sim->active;
-    np = sim->pop;
-    bnc = sim->bnc;
+    const uint32_t active = __ldcg(&sim->active);
+    np = ld_l2(&sim->pop);
+    bnc = ld_l2(&sim->bnc);
     uint32_t cnt[8], abnc[4];
 #pragma unroll
-    for (int k = 0; k < 8; k++) cnt[k] = sim->cnt[k];
+    for (int k = 0; k < 8; k++) cnt[k] = __ldcg(&sim->cnt[k]);
 #pragma unroll
-    for (int q = 0; q < 4; q++) abnc[q] = sim->acc_bnc[q];
-    const uint32_t ne = sim->newEggs, capacity = sim->capacity;
-    const uint32_t aL1 = sim->acc_L1de, afem = sim->acc_fem, ainf = sim->acc_inf;
-    const uint32_t dmin = sim->acc_dmin, dmax = sim->acc_dmax;
-    const float cc = sim->cc;
-    step = sim->step;
-    stop = sim->stop_step;
-    epoch = sim->epoch;
-    cur = sim->cur;
-    warn = sim->warn;
+    for (int q = 0; q < 4; q++) abnc[q] = __ldcg(&sim->acc_bnc[q]);
+    const uint32_t ne = __ldcg(&sim->newEggs), capacity = __ldcg(&sim->capacity);
+    const uint32_t aL1 = __ldcg(&sim->acc_L1de), afem = __ldcg(&sim->acc_fem), ainf = __ldcg(&sim->acc_inf);
+    const uint32_t dmin = __ldcg(&sim->acc_dmin), dmax = __ldcg(&sim->acc_dmax);
+    const float cc = __ldcg(&sim->cc);
+    step = __ldcg(&sim->step);
+    stop = __ldcg(&sim->stop_step);
+    epoch = __ldcg(&sim->epoch);
+    cur = __ldcg(&sim->cur);
+    warn = __ldcg(&sim->warn);
     if (after_step) {
       // the reference's shared empty initial ranges (src/abms.c:204-219) make
       // oldToNewAgents read one prefix-sum entry for several range ends
@@ -697,13 +716,15 @@ __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode
     np.numPotentiallyInfective = ainf;
     if (active) load_ctx_inputs(rp, step, in);
     s_go = active;
+    s_end = active ? np.r[GRAVID].end : 0u;
     s_l1 = np.numLarvae1DayEquiv;
     s_dmin = dmin;
     s_dmax = dmax;
     s_cc = cc;
   }
   __syncthreads();
-  if (!s_go) return;
+  const uint32_t pool_end = s_end;
+  if (!s_go) return pool_end;
   if (threadIdx.x == 0) {
     if (shared_end_warn) sim->warn = warn | SAMPO_DEV_WARN_REF_LAYOUT;
     if (after_step) {
@@ -741,6 +762,27 @@ __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode
       sim->larvaHMR[d] = hmr;
     }
   }
+  return pool_end;
+}
+
+// Sets a day graph's conditional node of the coming step (the path of the
+// step after a pool ending at `end`) and counts the kernels the step ran.
+__device__ __forceinline__ void set_next_path(const KParams& p, uint32_t end, uint32_t kernels) {
+#ifndef __CUDACC_RTC__
+  if (p.dflags & DF_COND) cudaGraphSetConditional(p.cond, small_pick(end, p.small_tiles));
+  if (p.dflags & DF_COUNT) atomicAdd(&p.bat->dev_launches, (unsigned long long)kernels);
+#endif
+}
+
+// Publishing the start of a step for every replicate of p (one CTA each);
+// block 0 rearms the tickets.
+__global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.bat->ticket1 = 0u;
+    p.bat->ticket2 = 0u;
+  }
+  const uint32_t end = publish_rep(p, blockIdx.x, mode);
+  if (mode == PUB_AFTER_STEP && blockIdx.x == 0 && threadIdx.x == 0) set_next_path(p, end, 3u);
 }
 
 // ------------------------------------------------------------------------

@@ -205,6 +205,19 @@ class Simulation:
         """Fix the grid sizes (CTAs per SM of the two passes) without tuning."""
         self._check(self.lib.sampo_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))
 
+    def set_small_step(self, max_tiles: int | None = None):
+        """Pools of at most max_tiles 1024-slot tiles take the one-launch
+        step in day graphs (None: one tile per CTA of its grid; 0: never)."""
+        self._check(self.lib.sampo_set_small_step(self.h, 0xFFFFFFFF if max_tiles is None else max_tiles))
+
+    def small_step_info(self) -> dict:
+        """The one-launch step's grid, its current max_tiles and how the last
+        day graph was built (0 none, 1 three-kernel steps, 2 device-picked
+        with a cooperative launch, 3 device-picked with a plain launch)."""
+        g, m, k = C.c_uint32(), C.c_uint32(), C.c_int()
+        self._check(self.lib.sampo_small_step_info(self.h, C.byref(g), C.byref(m), C.byref(k)))
+        return {"grid": g.value, "max_tiles": m.value, "day_graph": k.value}
+
     def checkpoint(self, path: str):
         """Save the simulation at the current step boundary."""
         self._check(self.lib.sampo_checkpoint_save(self.h, os.fsencode(path)))
