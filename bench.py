@@ -177,6 +177,7 @@ def gpu_arm(args, wl, rank, world, device):
     sim.flush_l2()
     rows, ms = [], 0.0
     launches0 = sim.kernel_times()[1]
+    small0 = sim.small_step_info()
     sync_barrier(world)
     t0 = time.perf_counter()
     with ClockSampler(device) as clk:
@@ -190,9 +191,7 @@ def gpu_arm(args, wl, rank, world, device):
     live = live_counts(rows)
     agent_days = float(live.sum()) / 24.0
     # kernels the library launched in the timed region (its own count: the
-    # launches outside graphs, the kernel nodes of each replayed three-kernel
-    # day graph, and the kernels counted on the device by day graphs that
-    # pick each hour's path there)
+    # kernel nodes of each replayed day graph plus the launches outside graphs)
     gpu_launches = sim.kernel_times()[1] - launches0
     small = sim.small_step_info()
 
@@ -262,7 +261,7 @@ def gpu_arm(args, wl, rank, world, device):
     return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(), passes=passes,
                 gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, publish_ms=publish_ms, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
-                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned, small=small)
+                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned, small=small, small0=small0)
 
 
 def cpu_reference(wl, seconds: float, first_steps: int | None = None, warmup: int = 0):
@@ -570,9 +569,10 @@ def main():
                "pool_bytes": [float(pool_bytes.min()), float(pool_bytes.max())], "parallelism": f"replicas x{world}",
                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1],
                                "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"},
-               "small_step": {"grid_ctas": r["small"]["grid"], "max_tiles": r["small"]["max_tiles"],
-                              "day_graph": {0: "none", 1: "three-kernel steps", 2: "path picked on the device, cooperative one-launch step",
-                                            3: "path picked on the device, one-launch step as a plain launch"}[r["small"]["day_graph"]]}}
+               "small_step": {"largest_grid_ctas": r["small"]["grid"], "max_tiles": r["small"]["max_tiles"],
+                              "timed_days_one_launch": r["small"]["days_one_launch"] - r["small0"]["days_one_launch"],
+                              "timed_days_three_kernel": r["small"]["days_three_kernel"] - r["small0"]["days_three_kernel"],
+                              "one_launch_kind": {0: "-", 1: "-", 2: "cooperative launch", 3: "plain launch of a co-resident grid"}[r["small"]["last_day"]]}}
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,

@@ -184,21 +184,26 @@ int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_
 int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
 /* One-launch step for small pools (for such pools it replaces the per-step
  * launch sequence of src/abms.c:502-529 that the three-kernel step already
- * shortens): the day graphs of sampo_run pick each hourly step's path on the
- * device. A pool of at most max_tiles 1024-slot tiles takes one cooperative
- * kernel (update, scan and compaction with one grid barrier, publish by its
- * last CTA); a larger one the count, update/scatter and publish kernels. Both
- * give the same results at any size. SAMPO_SMALL_STEP_DEFAULT: one tile per
- * CTA of the one-launch grid (the default); 0: never. sampo_step and runs
- * with timing on always take the three-kernel path; a run-time species
- * (sampo_set_species) too. */
+ * shortens). sampo_run picks each day's graph from the pool size it last
+ * saw (it learns the size after each day, one day behind the queued work):
+ * a pool of at most max_tiles 1024-slot tiles takes 24 launches of one
+ * cooperative kernel (update, scan and compaction with one grid barrier,
+ * publish by its last CTA) on a grid sized to the pool, a larger one the
+ * count, update/scatter and publish kernels. Both give the same results at
+ * any size. SAMPO_SMALL_STEP_DEFAULT: the largest co-resident grid of the
+ * one-launch kernel, one tile per CTA (the default); 0: never.
+ * sampo_run_async picks by the size seen at its call; sampo_step, runs with
+ * timing on and a run-time species (sampo_set_species) always take the
+ * three-kernel step. */
 #define SAMPO_SMALL_STEP_DEFAULT 0xffffffffu
 int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles);
-/* The one-launch step's grid (CTAs; 0 when it cannot run here), the current
- * max_tiles, and how the last day graph was built: 0 none yet, 1 three-kernel
- * steps only, 2 path picked on the device with a cooperative one-launch
- * step, 3 the same with a plain launch of the same co-resident grid. */
-int sampo_small_step_info(sampo_sim* s, uint32_t* grid, uint32_t* max_tiles, int* day_graph_kind);
+/* The one-launch step's largest grid (CTAs; 0 when it cannot run here), the
+ * current max_tiles, the kind of the last day launched (0 none yet, 1
+ * three-kernel steps, 2 one-launch steps launched cooperatively, 3 the same
+ * as plain launches of the same co-resident grid) and the days of each path
+ * since creation or sampo_set_timing. */
+int sampo_small_step_info(sampo_sim* s, uint32_t* grid, uint32_t* max_tiles, int* last_day_kind, uint64_t* days_one_launch,
+                          uint64_t* days_three_kernel);
 int sampo_checkpoint_load(sampo_sim* s, const char* path);
 /* Header of a checkpoint file (no device needed): the step it resumes at,
  * the population then, and the population at the previous step's start

@@ -210,10 +210,6 @@ cudaError_t launch_small(const KParams& p, int grid, bool cooperative, cudaStrea
   cfg.numAttrs = cooperative ? 1 : 0;
   return cudaLaunchKernelExC(&cfg, (const void*)k_step_small, args);
 }
-cudaError_t launch_select(const KParams& p, cudaStream_t st) {
-  k_select<<<1, 1, 0, st>>>(p);
-  return cudaGetLastError();
-}
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {
   k_eval_math<<<sm_count() * 2, 256, 0, st>>>(fn, x, y, out, n);
   return cudaGetLastError();

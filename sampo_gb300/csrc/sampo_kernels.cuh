@@ -67,7 +67,6 @@ struct BatchDev {
   uint32_t ticket2;           // scatter pass tile ticket
   uint32_t bar;               // one-launch step: CTAs past the decision phase (reset by its last CTA)
   uint32_t done;              // one-launch step: CTAs finished (reset by its last CTA)
-  unsigned long long dev_launches;  // kernels run by day graphs that pick the step's path on the device
 };
 
 // The count pass's in-tile prefix table of one tile: for each (round, warp)
@@ -103,16 +102,7 @@ struct KParams {
   BatchDev* bat;
   const ModelConst* mc;
   const void* ks;             // host: the kernels compiled for a user species (sampo_species.cu), or null
-  // Day graphs that pick each hourly step's path on the device (a single
-  // simulation): with DF_COND the step's last kernel sets the conditional
-  // node of the coming step to 1 (one-launch step) when the next pool has at
-  // most small_tiles tiles, else to 0 (count, scatter, publish); with
-  // DF_COUNT it adds the kernels the step ran to BatchDev::dev_launches.
-  unsigned long long cond = 0;
-  uint32_t dflags = 0;
-  uint32_t small_tiles = 0;
 };
-enum : uint32_t { DF_COND = 1u, DF_COUNT = 2u };
 
 // Modes of k_publish: PUB_AFTER_STEP turns the step's counts into the next
 // pool's start; PUB_INITIAL publishes the current pool (after init/load);
@@ -205,12 +195,10 @@ cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
 // The one-launch step of a single simulation (sampo_small_step.cuh): its
-// grid (CTAs resident on all SMs, 0 if it cannot run), its launch (a
-// cooperative launch when `cooperative`), and the kernel that sets a day
-// graph's first conditional node from the current pool.
+// largest grid (CTAs resident on all SMs, 0 if it cannot run) and its launch
+// (a cooperative launch when `cooperative`) on `grid` CTAs.
 int grid_blocks_small();
 cudaError_t launch_small(const KParams& p, int grid, bool cooperative, cudaStream_t st);
-cudaError_t launch_select(const KParams& p, cudaStream_t st);
 // Times count + scatter of the coming step at every (count, scatter) number
 // of CTAs per SM the occupancy allows and returns the fastest grids. The
 // trials leave the simulations' course unchanged (k_trial_reset); the coming

@@ -21,8 +21,7 @@
 //           (kernel/initAgents.cl:26-65), and adds its share of the next
 //           pool's statistics (calcL1de.cl, calcGender.cl).
 //  publish  the last CTA to finish publishes the next step (the k_publish
-//           code) and, in a day graph that picks each step's path on the
-//           device, sets the path of the step after.
+//           code).
 //
 // Pools with more tiles than CTAs are still stepped correctly: CTA b also
 // takes tiles b + G, b + 2G, ... (G CTAs); their decisions are counted in
@@ -506,20 +505,11 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
   }
   __syncthreads();
   if (!s_last) return;
-  const uint32_t next_end = publish_rep(p, 0u, PUB_AFTER_STEP);
+  (void)publish_rep(p, 0u, PUB_AFTER_STEP);
   if (tid == 0) {
     p.bat->bar = 0u;
     p.bat->done = 0u;
-    set_next_path(p, next_end, 1u);
   }
-}
-
-// The first conditional node of a day graph: the path of its first step from
-// the current pool.
-__global__ void k_select(KParams p) {
-  const SimDev* sim = p.reps[0].sim;
-  const uint32_t end = sim->active ? sim->pop.r[GRAVID].end : 0u;
-  set_next_path(p, end, 1u);
 }
 
 }  // namespace sampo

@@ -625,11 +625,6 @@ __device__ __forceinline__ T ld_l2(const T* p) {
   return v;
 }
 
-// Whether a pool ending at slot `end` takes the one-launch step.
-__device__ __forceinline__ uint32_t small_pick(uint32_t end, uint32_t small_tiles) {
-  return (end + kTile - 1) / kTile <= small_tiles ? 1u : 0u;
-}
-
 // The publish of replicate r by the calling CTA (at least kPublishThreads
 // threads; all of them call it): after a step, the next layout from the
 // survivor counts (kernel/oldToNewAgents.cl:57-95); then the pool's L1de,
@@ -765,15 +760,6 @@ __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
   return pool_end;
 }
 
-// Sets a day graph's conditional node of the coming step (the path of the
-// step after a pool ending at `end`) and counts the kernels the step ran.
-__device__ __forceinline__ void set_next_path(const KParams& p, uint32_t end, uint32_t kernels) {
-#ifndef __CUDACC_RTC__
-  if (p.dflags & DF_COND) cudaGraphSetConditional(p.cond, small_pick(end, p.small_tiles));
-  if (p.dflags & DF_COUNT) atomicAdd(&p.bat->dev_launches, (unsigned long long)kernels);
-#endif
-}
-
 // Publishing the start of a step for every replicate of p (one CTA each);
 // block 0 rearms the tickets.
 __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode) {
@@ -781,8 +767,7 @@ __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode
     p.bat->ticket1 = 0u;
     p.bat->ticket2 = 0u;
   }
-  const uint32_t end = publish_rep(p, blockIdx.x, mode);
-  if (mode == PUB_AFTER_STEP && blockIdx.x == 0 && threadIdx.x == 0) set_next_path(p, end, 3u);
+  (void)publish_rep(p, blockIdx.x, mode);
 }
 
 // ------------------------------------------------------------------------

@@ -207,16 +207,19 @@ class Simulation:
 
     def set_small_step(self, max_tiles: int | None = None):
         """Pools of at most max_tiles 1024-slot tiles take the one-launch
-        step in day graphs (None: one tile per CTA of its grid; 0: never)."""
+        step in day graphs (None: one tile per CTA of its largest grid; 0: never)."""
         self._check(self.lib.sampo_set_small_step(self.h, 0xFFFFFFFF if max_tiles is None else max_tiles))
 
     def small_step_info(self) -> dict:
-        """The one-launch step's grid, its current max_tiles and how the last
-        day graph was built (0 none, 1 three-kernel steps, 2 device-picked
-        with a cooperative launch, 3 device-picked with a plain launch)."""
+        """The one-launch step's largest grid, its current max_tiles, the
+        kind of the last day launched (0 none, 1 three-kernel steps, 2
+        one-launch steps launched cooperatively, 3 the same as plain launches)
+        and the days run on each path."""
         g, m, k = C.c_uint32(), C.c_uint32(), C.c_int()
-        self._check(self.lib.sampo_small_step_info(self.h, C.byref(g), C.byref(m), C.byref(k)))
-        return {"grid": g.value, "max_tiles": m.value, "day_graph": k.value}
+        d1, d3 = C.c_uint64(), C.c_uint64()
+        self._check(self.lib.sampo_small_step_info(self.h, C.byref(g), C.byref(m), C.byref(k), C.byref(d1), C.byref(d3)))
+        return {"grid": g.value, "max_tiles": m.value, "last_day": k.value, "days_one_launch": d1.value,
+                "days_three_kernel": d3.value}
 
     def checkpoint(self, path: str):
         """Save the simulation at the current step boundary."""

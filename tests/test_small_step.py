@@ -50,23 +50,28 @@ def test_paths_agree(gpu_ready, oracle_mod, sizes, n, cc):
     ranges, arrays, T, env, seeds = _workload(sizes, n, cc, seed=11)
     cap = 1 << 22
     ref = _run(ranges, arrays, T, env, seeds, cc, n, 0, cap)
-    assert ref[4] == 0 and ref[5]["day_graph"] == 1
+    assert ref[4] == 0 and ref[5]["days_one_launch"] == 0 and ref[5]["days_three_kernel"] == n // 24
     tiles = (ref[0]["ranges"][:, 7, 1].astype(np.int64) + 1023) // 1024
     mid = int(np.median(tiles))
     for max_tiles in (1 << 30, None, mid):
         got = _run(ranges, arrays, T, env, seeds, cc, n, max_tiles, cap)
         assert got[4] == 0, f"max_tiles={max_tiles}: device status {got[4]:#x}"
-        assert got[5]["day_graph"] in (2, 3), got[5]
+        info = got[5]
+        assert info["days_one_launch"] + info["days_three_kernel"] == n // 24, info
+        if max_tiles == 1 << 30 or (max_tiles is None and sizes[0] == 8000):  # every day small enough for the pick
+            assert info["days_one_launch"] == n // 24, info
+        if max_tiles == mid and sizes[0] == 8000:  # the pick changes during the ten days
+            assert 0 < info["days_one_launch"] < n // 24, info
         for i in range(n):
             assert got[0][i].tobytes() == ref[0][i].tobytes(), f"max_tiles={max_tiles}: row {i}"
         assert np.array_equal(got[1]["ranges"], ref[1]["ranges"])
         assert oracle_mod.pool_hash(got[1]["ranges"], got[2]) == oracle_mod.pool_hash(ref[1]["ranges"], ref[2])
         assert np.array_equal(got[3], ref[3])
     if sizes[0] == 8000:
-        # a small pool takes one launch per hour (plus one path pick per day
-        # and the constants refresh at the start of the run)
+        # a small pool takes one launch per hour (plus the constants refresh
+        # at the start of the run)
         got = _run(ranges, arrays, T, env, seeds, cc, n, None, cap)
-        assert got[6] == 1 + (n // 24) * (1 + 24), got[6]
+        assert got[6] == 1 + n, got[6]
 
 
 def test_small_step_matches_oracle(gpu_ready, oracle_mod):
@@ -77,7 +82,7 @@ def test_small_step_matches_oracle(gpu_ready, oracle_mod):
     cc = 30000.0
     ranges, arrays, T, env, seeds = _workload((3000, 2500, 1000, 2000), n, cc, seed=4)
     rows, pop, pool, hist, status, info, _ = _run(ranges, arrays, T, env, seeds, cc, n, None, 1 << 20)
-    assert status == 0 and info["day_graph"] in (2, 3)
+    assert status == 0 and info["days_one_launch"] == n // 24 and info["last_day"] in (2, 3)
     orc = OracleSim(1 << 20)
     orc.load_pool(ranges, arrays)
     for i in range(n):
