@@ -378,6 +378,26 @@ int sampo_batch_sync(sampo_batch* b);
 int sampo_batch_rows(sampo_batch* b, uint32_t slot, uint32_t first, uint32_t n, sampo_stats_row* out);
 /* Step reached, whether still active, and device error/warning bits. */
 int sampo_batch_state(sampo_batch* b, uint32_t slot, uint32_t* step, uint32_t* active, uint32_t* status_bits);
+/* Growing pools (no counterpart in the reference, whose maxAgents is a
+ * compile-time constant with an assert at 95 %, include/abms.h:16,
+ * src/abms.c:305-307). A replicate whose next layout does not fit its
+ * capacity does not stop: it pauses at that step, inactive, with
+ * SAMPO_DEV_ERR_CAPACITY set and its pool, constants and seed stream as they
+ * were. sampo_batch_grow moves its pool into a new allocation of `capacity`
+ * slots (at least the pool's current end) - the slots keep their indices, so
+ * the generator keys do not change - clears the capacity bit and reactivates
+ * it; the paused step then runs again with the same result. A running slot
+ * may be grown too (ahead of need). Stream-ordered after the work queued so
+ * far; the old buffers are freed stream-ordered. */
+int sampo_batch_grow(sampo_batch* b, uint32_t slot, uint64_t capacity);
+/* State of every slot in one read (after the queued work): step, active,
+ * device status bits, the pool's end (live slots plus gaps) and capacity;
+ * unused slots report capacity 0. */
+typedef struct {
+  uint32_t step, active, status, end;
+  uint64_t capacity;
+} sampo_slot_state;
+int sampo_batch_states(sampo_batch* b, sampo_slot_state* out, uint32_t nslots);
 int sampo_batch_histogram(sampo_batch* b, uint32_t slot, uint32_t out[100]);
 int sampo_batch_read_pool(sampo_batch* b, uint32_t slot, sampo_population* pop, sampo_pool_view* v);
 /* The autotuner of sampo_autotune over the batch's coming step. */

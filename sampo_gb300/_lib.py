@@ -99,6 +99,11 @@ class ReplicateConfig(C.Structure):
     _fields_ = [("capacity", C.c_uint64), ("carrying_capacity", C.c_float), ("stop_step", C.c_uint32)]
 
 
+class SlotState(C.Structure):
+    _fields_ = [("step", C.c_uint32), ("active", C.c_uint32), ("status", C.c_uint32), ("end", C.c_uint32),
+                ("capacity", C.c_uint64)]
+
+
 SIGNATURES = {
     "sampo_abi_version": (C.c_int, []),
     "sampo_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
@@ -168,6 +173,8 @@ SIGNATURES = {
     "sampo_batch_sync": (C.c_int, [_P]),
     "sampo_batch_rows": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
     "sampo_batch_state": (C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "sampo_batch_grow": (C.c_int, [_P, C.c_uint32, C.c_uint64]),
+    "sampo_batch_states": (C.c_int, [_P, C.c_void_p, C.c_uint32]),
     "sampo_batch_histogram": (C.c_int, [_P, C.c_uint32, _P]),
     "sampo_batch_read_pool": (C.c_int, [_P, C.c_uint32, C.POINTER(Population), C.POINTER(PoolView)]),
     "sampo_batch_last_run_ms": (C.c_int, [_P, C.POINTER(C.c_double)]),

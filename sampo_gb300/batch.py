@@ -117,6 +117,21 @@ class Batch:
         self._check(self.lib.sampo_batch_state(self.h, slot, C.byref(step), C.byref(active), C.byref(bits)))
         return step.value, bool(active.value), bits.value
 
+    def grow(self, slot: int, capacity: int):
+        """sampo_batch_grow: move the slot's pool into `capacity` slots per
+        buffer (slot indices kept) and resume it if it paused for capacity."""
+        self._check(self.lib.sampo_batch_grow(self.h, slot, capacity))
+
+    def states(self) -> np.ndarray:
+        """sampo_batch_states: step, active, status, end and capacity of every slot."""
+        out = (_lib.SlotState * self.max_replicates)()
+        self._check(self.lib.sampo_batch_states(self.h, C.addressof(out), self.max_replicates))
+        a = np.zeros(self.max_replicates, dtype=[("step", "u4"), ("active", "u4"), ("status", "u4"), ("end", "u4"),
+                                                 ("capacity", "u8")])
+        for i, o in enumerate(out):
+            a[i] = (o.step, o.active, o.status, o.end, o.capacity)
+        return a
+
     def histogram(self, slot: int) -> np.ndarray:
         h = np.zeros(100, dtype=np.uint32)
         self._check(self.lib.sampo_batch_histogram(self.h, slot, ptr(h)))

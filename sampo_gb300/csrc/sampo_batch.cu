@@ -207,6 +207,56 @@ extern "C" int sampo_batch_create(const sampo_batch_config* cfg, sampo_batch** o
   return SAMPO_OK;
 }
 
+// The kernels' view of one replicate's allocation `mem` (layout L).
+static RepParams carve(const RepLayout& L, void* mem, SimDev* sim, uint32_t ring) {
+  RepParams rp;
+  memset(&rp, 0, sizeof(rp));
+  char* m = (char*)mem;
+  rp.sim = sim;
+  for (int k = 0; k < 2; k++) {
+    char* q = m + k * L.pool;
+    DevPool& P = rp.pool[k];
+    P.age = (float*)(q + 0 * L.col4); P.his = (float*)(q + 1 * L.col4); P.delay = (float*)(q + 2 * L.col4);
+    P.sporo = (float*)(q + 3 * L.col4); P.uni = (uint32_t*)(q + 4 * L.col4); P.avail = (uint32_t*)(q + 5 * L.col4);
+    P.cycle = (uint32_t*)(q + 6 * L.col4); P.hbc = (uint32_t*)(q + 7 * L.col4); P.batches = (uint32_t*)(q + 8 * L.col4);
+    P.flags = (uint8_t*)(q + 9 * L.col4);
+  }
+  char* q = m + 2 * L.pool;
+  set_tile_arrays(rp, (uint32_t*)q, L.max_tiles);
+  q += L.tiles;
+  rp.T = (const float*)q; q += L.T;
+  rp.env = (const sampo_environment*)q; q += L.env;
+  rp.seeds = (sampo_seeds*)q; q += L.seeds;
+  rp.wt = (const uint32_t*)q; q += L.wt;
+  rp.rows = (sampo_stats_row*)q;
+  rp.ring = ring;
+  return rp;
+}
+
+// The device state of every slot up to its step constants (one strided copy).
+static int read_headers(sampo_batch* b, std::vector<SimDev>& h) {
+  h.resize(b->nslots);
+  BCK(cudaMemcpy2DAsync(h.data(), sizeof(SimDev), b->sims_dev, sizeof(SimDev), offsetof(SimDev, ctx), b->nslots,
+                        cudaMemcpyDeviceToHost, b->stream), "slot states");
+  BCK(cudaStreamSynchronize(b->stream), "slot states");
+  return SAMPO_OK;
+}
+
+// The host mirrors of the replicates' steps and activity from the device (a
+// replicate that paused for capacity did not advance).
+static int refresh_mirrors(sampo_batch* b) {
+  std::vector<SimDev> h;
+  const int rc = read_headers(b, h);
+  if (rc) return rc;
+  for (uint32_t i = 0; i < b->nslots; i++) {
+    Replicate& r = b->reps[i];
+    if (!r.used || !r.have_pop) continue;
+    r.step = h[i].step;
+    r.active = h[i].active != 0;
+  }
+  return SAMPO_OK;
+}
+
 static int upload_slot(sampo_batch* b, uint32_t slot, const SimDev& h) {
   BCK(cudaMemcpyAsync(b->sims_dev + slot, &h, sizeof(SimDev), cudaMemcpyHostToDevice, b->stream), "slot state");
   BCK(cudaMemcpyAsync(b->reps_dev + slot, &b->reps[slot].rp, sizeof(RepParams), cudaMemcpyHostToDevice, b->stream), "slot params");
@@ -237,26 +287,8 @@ extern "C" int sampo_batch_add(sampo_batch* b, const sampo_replicate_config* rc,
   r.input_step.assign(b->ring, 0xffffffffu);
   r.seed_step.assign(b->ring, 0xffffffffu);
   r.T_host.assign(b->ring, 0.0f);
-  char* m = (char*)mem;
   RepParams& rp = r.rp;
-  rp.sim = b->sims_dev + i;
-  for (int k = 0; k < 2; k++) {
-    char* q = m + k * L.pool;
-    DevPool& P = rp.pool[k];
-    P.age = (float*)(q + 0 * L.col4); P.his = (float*)(q + 1 * L.col4); P.delay = (float*)(q + 2 * L.col4);
-    P.sporo = (float*)(q + 3 * L.col4); P.uni = (uint32_t*)(q + 4 * L.col4); P.avail = (uint32_t*)(q + 5 * L.col4);
-    P.cycle = (uint32_t*)(q + 6 * L.col4); P.hbc = (uint32_t*)(q + 7 * L.col4); P.batches = (uint32_t*)(q + 8 * L.col4);
-    P.flags = (uint8_t*)(q + 9 * L.col4);
-  }
-  char* q = m + 2 * L.pool;
-  set_tile_arrays(rp, (uint32_t*)q, L.max_tiles);
-  q += L.tiles;
-  rp.T = (const float*)q; q += L.T;
-  rp.env = (const sampo_environment*)q; q += L.env;
-  rp.seeds = (sampo_seeds*)q; q += L.seeds;
-  rp.wt = (const uint32_t*)q; q += L.wt;
-  rp.rows = (sampo_stats_row*)q;
-  rp.ring = b->ring;
+  rp = carve(L, mem, b->sims_dev + i, b->ring);
   BCK(cudaMemsetAsync(rp.tilePre, 0, (size_t)L.max_tiles * kTileArrayWords * 4, b->stream), "tile arrays");
   SimDev h = initial_sim_state((uint32_t)rc->capacity, rc->carrying_capacity);
   h.stop_step = rc->stop_step;
@@ -396,6 +428,8 @@ extern "C" int sampo_batch_checkpoint_save(sampo_batch* b, uint32_t slot, const 
   BCK(cudaStreamSynchronize(b->stream), "checkpoint");  // the slot is at a step boundary
   SimDev h;
   BCK(cudaMemcpy(&h, b->sims_dev + slot, sizeof(SimDev), cudaMemcpyDeviceToHost), "state");
+  if ((h.error & SAMPO_DEV_ERR_CAPACITY) && !h.active && h.step < h.stop_step)
+    return bfail(b, SAMPO_ERR_STATE, "the slot is paused for capacity: grow it (sampo_batch_grow) first");
   CkHeader hd;
   memset(&hd, 0, sizeof(hd));
   memcpy(hd.magic, kCkMagic, 8);
@@ -546,7 +580,10 @@ extern "C" int sampo_batch_run(sampo_batch* b, uint32_t nsteps, int wait) {
     r.step = (uint32_t)std::min<uint64_t>((uint64_t)r.step + nsteps, r.stop_step);
     r.active = r.step < r.stop_step;
   }
-  if (wait) BCK(cudaStreamSynchronize(b->stream), "batch run");
+  if (wait) {
+    BCK(cudaStreamSynchronize(b->stream), "batch run");
+    return refresh_mirrors(b);
+  }
   return SAMPO_OK;
 }
 
@@ -622,6 +659,83 @@ extern "C" int sampo_batch_sync(sampo_batch* b) {
   if (!b) return SAMPO_ERR_ARG;
   cudaSetDevice(b->device);
   BCK(cudaStreamSynchronize(b->stream), "batch sync");
+  return refresh_mirrors(b);
+}
+
+extern "C" int sampo_batch_states(sampo_batch* b, sampo_slot_state* out, uint32_t nslots) {
+  if (!b || !out || nslots > b->nslots) return SAMPO_ERR_ARG;
+  cudaSetDevice(b->device);
+  std::vector<SimDev> h;
+  const int rc = read_headers(b, h);
+  if (rc) return rc;
+  for (uint32_t i = 0; i < nslots; i++) {
+    const Replicate& r = b->reps[i];
+    sampo_slot_state& o = out[i];
+    o.step = h[i].step;
+    o.active = h[i].active;
+    o.status = h[i].error | h[i].warn;
+    o.end = r.have_pop ? h[i].pop.r[7].end : 0u;
+    o.capacity = r.used ? r.capacity : 0u;
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_grow(sampo_batch* b, uint32_t slot, uint64_t capacity) {
+  Replicate* r = get_slot(b, slot);
+  if (!r) return SAMPO_ERR_ARG;
+  if (!r->have_pop) return bfail(b, SAMPO_ERR_STATE, "no population");
+  if (capacity > 0xFFFFFF00ull) return bfail(b, SAMPO_ERR_ARG, "capacity above 0xFFFFFF00 slots");
+  cudaSetDevice(b->device);
+  std::vector<SimDev> hs;
+  int rc = read_headers(b, hs);  // waits for the queued work
+  if (rc) return rc;
+  SimDev h = hs[slot];
+  const uint32_t end = h.pop.r[7].end;
+  if (capacity < end || capacity < 128) return bfail(b, SAMPO_ERR_ARG, "capacity below the pool's end");
+  const RepLayout L(capacity, b->ring), L0(r->capacity, b->ring);
+  void* mem = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&mem, L.total, b->mempool, b->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, SAMPO_ERR_CAPACITY, std::string("grown replicate buffers: ") + cudaGetErrorString(e));
+  }
+  const RepParams rp = carve(L, mem, b->sims_dev + slot, b->ring);
+  const RepParams& old = r->rp;
+  // the current pool into buffer 0, column by column: slot indices unchanged
+  const DevPool& S = old.pool[h.cur & 1u];
+  const DevPool& D = rp.pool[0];
+  const size_t b4 = (size_t)end * 4;
+  if (end) {
+    BCK(cudaMemcpyAsync(D.age, S.age, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.his, S.his, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.delay, S.delay, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.sporo, S.sporo, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.uni, S.uni, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.avail, S.avail, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.cycle, S.cycle, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.hbc, S.hbc, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.batches, S.batches, b4, cudaMemcpyDeviceToDevice, b->stream), "grow");
+    BCK(cudaMemcpyAsync(D.flags, S.flags, end, cudaMemcpyDeviceToDevice, b->stream), "grow");
+  }
+  // the rings of inputs, seeds and rows (same ring length, same layout)
+  BCK(cudaMemcpyAsync((void*)rp.T, old.T, L.T + L.env + L.seeds + L.wt + L.rows, cudaMemcpyDeviceToDevice, b->stream),
+      "grow rings");
+  // fresh look-back arrays: zero epochs never match the running step's
+  BCK(cudaMemsetAsync(rp.tilePre, 0, (size_t)L.max_tiles * kTileArrayWords * 4, b->stream), "tile arrays");
+  h.capacity = (uint32_t)capacity;
+  h.cur = 0;
+  h.error &= ~SAMPO_DEV_ERR_CAPACITY;
+  h.active = h.step < h.stop_step ? 1u : 0u;
+  BCK(cudaMemcpyAsync(b->sims_dev + slot, &h, offsetof(SimDev, ctx), cudaMemcpyHostToDevice, b->stream), "slot state");
+  BCK(cudaMemcpyAsync(b->reps_dev + slot, &rp, sizeof(RepParams), cudaMemcpyHostToDevice, b->stream), "slot params");
+  BCK(cudaFreeAsync(r->mem, b->stream), "free replicate");
+  (void)L0;
+  r->mem = mem;
+  r->rp = rp;
+  r->capacity = capacity;
+  r->step = h.step;
+  r->active = h.active != 0;
+  BCK(cudaStreamSynchronize(b->stream), "grow");  // h lives on this stack
   return SAMPO_OK;
 }
 

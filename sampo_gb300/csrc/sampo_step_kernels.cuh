@@ -633,10 +633,16 @@ __device__ __forceinline__ T ld_l2(const T* p) {
 // larva age present (kernel/killAgents.cl:117-133 depends on the age and
 // L1de only). Reads and clears the acc_* accumulators. Mode PUB_REFRESH only
 // recomputes the input-dependent step constants (the inputs of the coming
-// step may have been written after its publish). Returns the end of the
-// replicate's pool after the publish (0 when it is inactive) to every thread.
+// step may have been written after its publish). When the next layout does
+// not fit the replicate's capacity (the scatter pass then flagged
+// SAMPO_DEV_ERR_CAPACITY and wrote nothing), the replicate pauses instead:
+// it becomes inactive at the same step with the same pool, constants and
+// larval table, and only the step's counters are cleared, so that the step
+// runs again, with the same result, once its pool has been moved into a
+// larger one (sampo_batch_grow). Returns the end of the replicate's pool
+// after the publish (0 when it is inactive) to every thread.
 __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
-  __shared__ uint32_t s_go, s_l1, s_dmin, s_dmax, s_end;
+  __shared__ uint32_t s_go, s_l1, s_dmin, s_dmax, s_end, s_pause;
   __shared__ float s_cc;
   const RepParams& rp = p.reps[r];
   SimDev* sim = rp.sim;
@@ -666,7 +672,7 @@ __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
   sampo_bites_cycles bnc;
   CtxInputs in;
   uint32_t step = 0, stop = 0, epoch = 0, cur = 0, warn = 0;
-  bool relayout = false, shared_end_warn = false;
+  bool relayout = false, shared_end_warn = false, pause = false;
   if (threadIdx.x == 0) {
     const uint32_t active = __ldcg(&sim->active);
     np = ld_l2(&sim->pop);
@@ -695,10 +701,12 @@ __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
         moved += cnt[k];
       }
       shared_end_warn = shared_end && moved;
-      if (layout_fits(cnt, ne, capacity)) {  // else the scatter pass flagged the capacity error
+      if (layout_fits(cnt, ne, capacity)) {
         uint32_t base[8];
         next_layout(cnt, ne, np, base);
         relayout = true;
+      } else {
+        pause = true;  // the scatter pass flagged the capacity error and wrote nothing
       }
       step += 1u;
       bnc.numCyclesReported = abnc[0];
@@ -711,6 +719,7 @@ __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
     np.numPotentiallyInfective = ainf;
     if (active) load_ctx_inputs(rp, step, in);
     s_go = active;
+    s_pause = pause;
     s_end = active ? np.r[GRAVID].end : 0u;
     s_l1 = np.numLarvae1DayEquiv;
     s_dmin = dmin;
@@ -720,6 +729,18 @@ __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
   __syncthreads();
   const uint32_t pool_end = s_end;
   if (!s_go) return pool_end;
+  if (s_pause) {
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) sim->cnt[k] = 0;
+      sim->newEggs = 0;
+      sim->acc_L1de = 0; sim->acc_fem = 0; sim->acc_inf = 0;
+      sim->acc_dmin = 0xffffffffu; sim->acc_dmax = 0;
+      sim->acc_bnc[0] = sim->acc_bnc[1] = sim->acc_bnc[2] = sim->acc_bnc[3] = 0;
+      sim->active = 0;
+    }
+    return 0u;
+  }
   if (threadIdx.x == 0) {
     if (shared_end_warn) sim->warn = warn | SAMPO_DEV_WARN_REF_LAYOUT;
     if (after_step) {

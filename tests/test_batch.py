@@ -124,3 +124,53 @@ def test_replicate_bytes_without_gpu(sampo_lib):
     assert abs((b2 - b1) - 2 * 37 * (1 << 20)) < 2 * 37 * (1 << 20) * 0.02
     assert sampo_lib.sampo_batch_destroy(None) == 0
     assert sampo_lib.sampo_batch_create(None, None) == -1
+
+
+@pytest.mark.gpu
+def test_grown_replicates_equal_plain_runs(gpu_ready):
+    """Pools that start small and grow: a replicate whose next layout does not
+    fit pauses at that step; sampo_batch_grow moves its pool (slot indices
+    kept) into a larger allocation and the step runs again. Rows, pool and
+    histogram still equal the plain run with room to spare, whether the slot
+    was grown after a pause or ahead of need."""
+    import dataclasses
+    from sampo_gb300.batch import Batch, admit
+    # the first two outgrow their pools on day 12 (the oracle's layout ends
+    # pass 4096 at step 310 and 6000 at step 314, then reach 18714 slots)
+    specs = [ReplicateSpec(initial=2000, seed=21, mean_t=29.0, amplitude=2.0, rain_mean=3.0, days=16, capacity=4096),
+             ReplicateSpec(initial=2000, seed=21, mean_t=29.0, amplitude=2.0, rain_mean=3.0, days=16, capacity=6000),
+             ReplicateSpec(initial=9000, seed=12, mean_t=24.0, amplitude=6.0, rain_mean=2.0, days=10, capacity=20000)]
+    steps = [s.steps for s in specs]
+    paused, grown_ahead = set(), False
+    with Batch(max_replicates=4, ring_steps=max(steps) + 1) as b:
+        slots = [admit(b, s, st, device_seeds=i == 0) for i, (s, st) in enumerate(zip(specs, steps))]
+        for _ in range(max(steps) // 24 + 16):
+            b.run(24)
+            st = b.states()
+            if all(st[s]["step"] == n for s, n in zip(slots, steps)):
+                break
+            for s, n in zip(slots, steps):
+                o = st[s]
+                if o["step"] < n and not o["active"]:
+                    assert o["status"] & 0x1, o  # paused for capacity, nothing else
+                    paused.add(s)
+                    b.grow(s, 4 * int(o["end"]) + 1024)
+                elif s == slots[2] and not grown_ahead and o["step"] >= 96:
+                    b.grow(s, 3 * int(o["capacity"]))  # a running slot, ahead of need
+                    grown_ahead = True
+        assert len(paused) >= 2 and grown_ahead
+        for s, spec, n in zip(slots, specs, steps):
+            roomy = dataclasses.replace(spec, capacity=400_000)
+            rows, pop, arrays, hist, status = plain_run(roomy, n)
+            assert b.rows(s, 0, n + 1).tobytes() == rows.tobytes(), f"seed {spec.seed}: rows"
+            bpop, barrays = b.read_pool(s)
+            assert np.array_equal(bpop["ranges"], pop["ranges"])
+            for name in arrays:
+                x, y = barrays[name], arrays[name]
+                if x.dtype == np.float32:
+                    x, y = x.view(np.uint32), y.view(np.uint32)
+                for k in range(8):
+                    lo, hi = int(pop["ranges"][k][0]), int(pop["ranges"][k][1])
+                    assert np.array_equal(x[lo:hi], y[lo:hi]), f"seed {spec.seed}: {name}"
+            assert np.array_equal(b.histogram(s), hist)
+            assert b.state(s)[2] == status == 0

@@ -45,3 +45,30 @@ def test_served_results_equal_solo_runs(gpu_ready):
         assert np.array_equal(res.histogram, hist), f"request {res.rid}: histogram differs"
         assert res.status == status
         assert res.completed >= res.admitted >= res.arrival
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grow_at", [0, 3])
+def test_served_pools_grow_and_match_solo_runs(gpu_ready, grow_at):
+    """Requests admitted with pools far smaller than they grow to: the server
+    moves them into larger ones, after a pause for capacity (grow_at = 0) or
+    ahead of need, and every result still equals the request run alone in a
+    fixed roomy pool."""
+    from sampo_gb300.batch import ReplicateSpec
+    from sampo_gb300.serve import Request, Server, plain_result
+    # seed 21 outgrows 4096 slots at step 310 and reaches 18714 (oracle)
+    specs = [ReplicateSpec(initial=2000, seed=21, mean_t=29.0, amplitude=2.0, rain_mean=3.0, days=16, capacity=4096),
+             ReplicateSpec(initial=2000, seed=21, mean_t=29.0, amplitude=2.0, rain_mean=3.0, days=15, capacity=6000),
+             ReplicateSpec(initial=300, seed=5, mean_t=26.0, amplitude=4.0, rain_mean=3.0, days=6, capacity=1024)]
+    reqs = [Request(i, s, 0.0) for i, s in enumerate(specs)]
+    srv = Server(budget_bytes=1 << 40, max_replicates=4, max_days=16, grow_at=grow_at)
+    results = srv.serve(reqs)
+    srv.close()
+    assert srv.grows >= 2
+    if grow_at == 0:
+        assert srv.pauses >= 2
+    for res in results:
+        rows, hist, status = plain_result(specs[res.rid])
+        assert res.rows.tobytes() == rows.tobytes(), f"request {res.rid}: rows differ from its solo run"
+        assert np.array_equal(res.histogram, hist)
+        assert res.status == status == 0
