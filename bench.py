@@ -441,6 +441,63 @@ def ensemble_arm(args):
     }
 
 
+def ensemble_year_arm(args):
+    """The ensemble at its stated horizon: every replicate runs its 365 days,
+    admitted in waves under the HBM budget by the server (all arrive at time
+    0; pools start at 2 x initial and grow). Against the plain path one
+    replicate at a time, timed on a sample (every `--plain-every`-th replicate,
+    scaled to all) and compared bit for bit on that sample."""
+    from sampo_gb300.batch import ensemble_specs
+    from sampo_gb300.serve import Request, Server, plain_result
+    n, days = args.replicates, 365
+    specs = ensemble_specs(n, seed=4, days=days, growth=2.0)
+    reqs = [Request(i, s, 0.0) for i, s in enumerate(specs)]
+    srv = Server(budget_bytes=int(args.budget_gb * 1e9), max_replicates=min(n, 1024), max_days=days)
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        res = srv.serve(reqs)
+        wall = time.perf_counter() - t0
+    srv.close()
+    agent_days = sum(float(live_counts(r.rows[:-1]).sum()) for r in res) / 24.0
+    sample = list(range(0, n, args.plain_every))
+    plain_s, exact = 0.0, 0
+    by_id = {r.rid: r for r in res}
+    for i in sample:
+        t1 = time.perf_counter()
+        rows, hist, status = plain_result(specs[i])
+        plain_s += time.perf_counter() - t1
+        r = by_id[i]
+        exact += int(rows is not None and r.rows.tobytes() == rows.tobytes() and np.array_equal(r.histogram, hist)
+                     and r.status == status)
+    plain_all = plain_s * n / len(sample)
+    value = n * days / wall
+    return {
+        "metric": "replicate-days/s", "value": value, "unit": "replicate-days/s", "n_gpus": 1, "steps": days,
+        "warmup": 0, "ms_per_step": wall * 1e3 / days, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
+        "config": {"workload": f"ensemble at its horizon: {n} replicates x 365 days, initial eggs log-uniform in "
+                               "[1e3, 1e6] aged U{0..3} days, own seed and weather each (mean T U[20,30] C, amplitude "
+                               f"U[2,8] C, sd 0.5); admitted in waves under a {args.budget_gb:g} GB HBM budget, pools "
+                               "start at 2 x initial + 65536 slots and grow",
+                   "step": "one simulated day of every resident replicate (24 hourly steps, one CUDA graph)",
+                   "seeds": "batched: drawn on the device per replicate; one at a time: uploaded",
+                   "initial_agents_total": int(sum(s.initial for s in specs))},
+        "batched": {"wall_s": wall, "replicate_days_per_s": value, "sims_per_s": n / wall,
+                    "agent_days_per_s": agent_days / wall, "agent_days": agent_days,
+                    "days_stepped": srv.days_run, "peak_resident": srv.peak_resident,
+                    "peak_hbm_gb": srv.peak_bytes / 1e9, "pool_growths": srv.grows,
+                    "growths_after_a_pause": srv.pauses, "growths_over_budget": srv.over_budget},
+        "one_at_a_time": {"sample": f"{len(sample)} of {n} replicates (every {args.plain_every}th)",
+                          "sample_s": plain_s, "scaled_s": plain_all, "sims_per_s": n / plain_all},
+        "speedup_vs_one_at_a_time": plain_all / wall,
+        "bit_exact_sample": f"{exact}/{len(sample)}",
+        "e2e": {"value": value, "unit": "replicate-days/s", "h2d_bytes_per_step": n * 24 * (4 + 24 + 4),
+                "d2h_bytes_per_step": n * 24 * 92,
+                "note": "value is already end to end: wall clock through sampo_gb300.serve.Server, inputs up and rows down"},
+        "clocks": clk.summary(),
+    }
+
+
 def served_arm(args):
     """The served request stream, a bounded number of requests per rate."""
     from sampo_gb300.serve import Server, latency_summary, one_at_a_time, request_stream
@@ -476,7 +533,9 @@ def served_arm(args):
             "one_at_a_time": {"sims_per_s": len(reqs) / plain_makespan, "latency_s": latency_summary(lat_plain)},
             "speedup_sims_per_s": (len(res) / makespan) / (len(reqs) / plain_makespan),
             "bit_exact": f"{exact}/{len(res)}", "peak_resident": srv.peak_resident,
-            "peak_hbm_gb": srv.peak_bytes / 1e9, "days_stepped": srv.days_run, "wall_s": time.perf_counter() - t0}
+            "peak_hbm_gb": srv.peak_bytes / 1e9, "days_stepped": srv.days_run, "pool_growths": srv.grows,
+            "growths_after_a_pause": srv.pauses, "growths_over_budget": srv.over_budget,
+            "days_admission_held": srv.held_days, "wall_s": time.perf_counter() - t0}
     first = per_rate[str(rates[0])]
     # host traffic per request (the line's step): its inputs up at admission
     # (temperature, environment row, world time per hourly step) and its stats
@@ -486,7 +545,8 @@ def served_arm(args):
     out.update({"value": first["sims_per_s"], "ms_per_step": None,
                 "config": {"workload": f"served stream: {args.requests} requests per rate, Poisson arrivals, initial eggs "
                                        f"log-uniform in [1e2, 5e6], horizons U{{{args.min_days}..{args.max_days}}} days, "
-                                       f"own seed and weather each, {args.budget_gb:g} GB HBM budget, capacity 96 x initial + 65536",
+                                       f"own seed and weather each, {args.budget_gb:g} GB HBM budget; pools admitted at 2 x initial + "
+                                       "65536 slots and grown (one at a time: a fixed pool of 96 x initial + 65536)",
                            "rates_per_s": rates},
                 "per_rate": per_rate,
                 "e2e": {"value": first["sims_per_s"], "unit": "sims/s", "h2d_bytes_per_step": float(hours.mean() * (4 + 24 + 4)),
@@ -501,7 +561,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="roofline", choices=list(WORKLOADS) + ["ensemble", "served"])
+    ap.add_argument("--workload", default="roofline", choices=list(WORKLOADS) + ["ensemble", "ensemble-year", "served"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ctas-per-sm", default="",
                     help="COUNT,SCATTER: fixed grid sizes of the plain-path workloads instead of the autotuner")
@@ -509,7 +569,10 @@ def main():
                     help="plain-path workloads: 'auto' (one-launch step for pools of up to one tile per CTA of its "
                          "grid), 'off' (the three-kernel step every hour) or a largest pool in 1024-slot tiles")
     ap.add_argument("--replicates", type=int, default=512, help="ensemble: replicates")
-    ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
+    ap.add_argument("--requests", type=int, default=200, help="served: requests per rate")
+    ap.add_argument("--plain-every", type=int, default=8, help="ensemble-year: the one-at-a-time arm's sample stride")
+    ap.add_argument("--batched-sample", type=int, default=64,
+                    help="plain workloads: replicates of the compact batched-vs-one-at-a-time figure (0: none)")
     ap.add_argument("--rates", default="10,100,1000", help="served: arrival rates per second")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM budget")
     ap.add_argument("--min-days", type=int, default=30)
@@ -517,7 +580,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
-    if args.workload in ("ensemble", "served"):
+    if args.workload in ("ensemble", "ensemble-year", "served"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference runs one simulation per process; "
                               "its arm is the plain workloads"}))
@@ -526,6 +589,8 @@ def main():
             if "--steps" not in sys.argv:
                 args.steps = 12
             print(json.dumps(ensemble_arm(args)))
+        elif args.workload == "ensemble-year":
+            print(json.dumps(ensemble_year_arm(args)))
         else:
             print(json.dumps(served_arm(args)))
         return
@@ -593,6 +658,19 @@ def main():
         "clocks": r["clocks"],
         "wall_s_timed": r["wall"],
     }
+    if args.batched_sample and world == 1:
+        # a compact record of batching: the ensemble workload's replicates,
+        # fewer of them, over days 3..6, batched against one at a time
+        import copy
+        a2 = copy.copy(args)
+        a2.replicates, a2.warmup, a2.steps = args.batched_sample, 3, 3
+        e = ensemble_arm(a2)
+        line["batched_vs_one_at_a_time"] = {
+            "workload": f"{a2.replicates} replicates of the ensemble workload (initial eggs log-uniform in [1e3, 1e6]), "
+                        "days 3..6, device time of the timed days",
+            "batched_replicate_days_per_s": e["value"],
+            "one_at_a_time_replicate_days_per_s": e["one_at_a_time"]["replicate_days_per_s"],
+            "speedup": e["speedup_vs_one_at_a_time"], "bit_exact_replicates": e["bit_exact_replicates"]}
     if cpu:
         line["cpu_baseline"] = {"value": cpu["value"], "unit": "agent-days/s", "cores": cpu["threads"], "kind": "port",
                                 "sample": f"first {cpu['steps']} hourly steps of the same workload ({cpu['seconds']:.1f} s), oracle port, OpenMP"}

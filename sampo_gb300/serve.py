@@ -9,8 +9,8 @@ histogram and status are read back), grows the pools that need it and admits
 waiting ones, first fit in arrival order, while the device bytes of the
 resident requests stay within the HBM budget and a slot is free. A request
 is admitted with a pool of twice its initial size (plus 65,536 slots) and
-grows with it: a pool whose end passes a third of its capacity is moved into
-one six times its end (sampo_batch_grow, slot indices kept), and a replicate
+grows with it: a pool whose end passes half its capacity is moved into one
+three times its end (sampo_batch_grow, slot indices kept), and a replicate
 whose next layout does not fit pauses at that step until it has been grown
 (the step then runs again). Residents' growth comes before admissions; when
 every resident is paused and none fits the budget, the smallest growth is
@@ -85,8 +85,8 @@ class _Prepared:
 
 
 CAPACITY_BIT = 0x1       # SAMPO_DEV_ERR_CAPACITY: paused until its pool grows
-GROW_AT = 3              # grow a running pool once its end passes capacity / GROW_AT
-GROW_TO = 6              # ... into GROW_TO x its end (+ 65536 slots)
+GROW_AT = 2              # grow a running pool once its end passes capacity / GROW_AT
+GROW_TO = 3              # ... into GROW_TO x its end (+ 65536 slots): room for a day of the fastest growth seen (2.75x)
 
 
 class Server:
@@ -107,6 +107,7 @@ class Server:
         self.pauses = 0             # growth after a replicate paused for capacity
         self.over_budget = 0        # growths made over the budget to keep the batch moving
         self.held = False           # a paused resident waits for memory: no admissions
+        self.held_days = 0
 
     def close(self):
         self.batch.close()
@@ -222,6 +223,7 @@ class Server:
             self.days_run += 1
             self._retire(clock() - t0, done)
             self._grow()
+            self.held_days += int(self.held)
         return sorted(done, key=lambda r: r.rid)
 
 

@@ -48,7 +48,7 @@ def test_served_results_equal_solo_runs(gpu_ready):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("grow_at", [0, 3])
+@pytest.mark.parametrize("grow_at", [0, 2])
 def test_served_pools_grow_and_match_solo_runs(gpu_ready, grow_at):
     """Requests admitted with pools far smaller than they grow to: the server
     moves them into larger ones, after a pause for capacity (grow_at = 0) or
