@@ -463,9 +463,9 @@ static void drop_day_graph(sampo_sim* s) {
   }
 }
 
-// A day of 24 one-launch steps on grid bucket b, cooperative where a graph
-// takes a cooperative launch, else a plain launch of the same co-resident
-// grid (its grid barrier is bounded either way).
+// A day on grid bucket b: one launch of 24 one-launch steps, cooperative
+// where a graph takes a cooperative launch, else a plain launch of the same
+// co-resident grid (its grid barriers are bounded either way).
 static cudaError_t build_small_graph(sampo_sim* s, int b) {
   const KParams p = make_params(s);
   const int grid = (int)small_bucket_grid(s, b);
@@ -474,7 +474,7 @@ static cudaError_t build_small_graph(sampo_sim* s, int b) {
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) break;
-    for (int h = 0; h < 24 && e == cudaSuccess; h++) e = launch_small(p, grid, kind == DG_SMALL_COOP, s->stream);
+    e = launch_small(p, grid, kind == DG_SMALL_COOP, 24u, s->stream);
     const cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&s->small_graph[b], g, 0);
@@ -502,7 +502,7 @@ static int day_graph_for(sampo_sim* s, cudaGraphExec_t* gx, uint32_t* kernels, i
     while (b + 1 < kSmallBuckets && small_bucket_grid(s, b) < want) b++;
     if (s->small_graph[b] || build_small_graph(s, b) == cudaSuccess) {
       *gx = s->small_graph[b];
-      *kernels = 24;
+      *kernels = 1;
       *kind = s->small_graph_kind[b];
       return SAMPO_OK;
     }

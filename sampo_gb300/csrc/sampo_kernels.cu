@@ -195,9 +195,9 @@ int grid_blocks_small() {
   }
   return sm_count() * per;
 }
-cudaError_t launch_small(const KParams& p, int grid, bool cooperative, cudaStream_t st) {
+cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st) {
   KParams q = p;
-  void* args[] = {&q};
+  void* args[] = {&q, &nsteps};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kSmallThreads);

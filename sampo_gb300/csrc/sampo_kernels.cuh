@@ -194,11 +194,12 @@ cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo
 cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
-// The one-launch step of a single simulation (sampo_small_step.cuh): its
-// largest grid (CTAs resident on all SMs, 0 if it cannot run) and its launch
-// (a cooperative launch when `cooperative`) on `grid` CTAs.
+// The one-launch steps of a single simulation (sampo_small_step.cuh): the
+// largest grid (CTAs resident on all SMs, 0 if it cannot run) and a launch
+// of `nsteps` hourly steps (a cooperative launch when `cooperative`) on
+// `grid` CTAs.
 int grid_blocks_small();
-cudaError_t launch_small(const KParams& p, int grid, bool cooperative, cudaStream_t st);
+cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st);
 // Times count + scatter of the coming step at every (count, scatter) number
 // of CTAs per SM the occupancy allows and returns the fastest grids. The
 // trials leave the simulations' course unchanged (k_trial_reset); the coming

@@ -16,6 +16,9 @@
 // instantiations run the same decision code on the same inputs, so they
 // agree bit for bit. EGGS adds the eggs laid to Acc::newEggs (the counting
 // pass, and the one-launch step, whose single update decides and writes).
+// LDG reads the larval mortality table through the read-only cache; the
+// one-launch step, which rewrites the table between the hours of one launch,
+// keeps a copy in shared memory instead.
 #pragma once
 #include <stdint.h>
 #include "sampo_math.h"
@@ -159,7 +162,7 @@ __device__ __forceinline__ uint32_t age_days_uncapped(float age) {
 
 // Kill then update one valid agent of range rg at slot gid.
 // Returns the next state (0..7), or -1 when the agent dies this step.
-template <bool FULL, bool EGGS = !FULL>
+template <bool FULL, bool EGGS = !FULL, bool LDG = true>
 __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& mc, int rg, uint32_t gid, Rec& a, Acc& acc) {
   // ---- killAgents (kernel/killAgents.cl:52-147) ----
   {
@@ -168,7 +171,7 @@ __device__ __forceinline__ int update_agent(const StepCtx& c, const KillConst& m
     if (rg >= IMMATURE) {
       hmr = mc.adultHMR[age_days(a.age)];
     } else if (rg == LARVA) {
-      hmr = __ldg(c.larvaHMR + age_days(a.age));
+      hmr = LDG ? __ldg(c.larvaHMR + age_days(a.age)) : c.larvaHMR[age_days(a.age)];
       if (hmr != hmr) acc.bad = 1;  // table entry not prepared
     } else {
       hmr = mc.aquaticHMR;

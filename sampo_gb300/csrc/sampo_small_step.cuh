@@ -110,7 +110,7 @@ __device__ __forceinline__ void small_update_tile(const StepCtx& c, const ModelC
       a.female = (c_flags[i] >> 3) & 1u;
       a.bm = BM_NONE;
       sa.devoob |= (rg == LARVA) & c.devOOB;
-      const int ns = update_agent<true, true>(c, mc.kill, rg, g, a, t);
+      const int ns = update_agent<true, true, false>(c, mc.kill, rg, g, a, t);
       if (ns >= 0) {
         if (a.bm != BM_NONE) {  // the owed normal draw (include/gpuRand.h:56-63)
           const uint32_t v = finish_box_muller(c, mc, g, a.bm, a.batches);
@@ -279,14 +279,22 @@ __device__ __forceinline__ void small_issue_tile(const DevPool& src, uint8_t* st
   bulk_load(st + 9 * kColBytes, src.flags + lo, b1, bar);
 }
 
-// The one-launch step of p.reps[0] (a single simulation). The per-tile count
-// rows use the replicate's prefix-table array (tilePre: kPreWords words per
-// tile, of which the rows take kSmallRows), which the three-kernel step
-// rewrites before it reads it.
-__global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(KParams p) {
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+// The one-launch steps of p.reps[0] (a single simulation): `nsteps` hourly
+// steps in one cooperative launch, each one update, one scatter and one
+// publish separated by grid barriers (a day graph launches it once with 24).
+// The per-tile count rows use the replicate's prefix-table array (tilePre:
+// kPreWords words per tile, of which the rows take kSmallRows), which the
+// three-kernel step rewrites before it reads it. Within the launch the
+// replicate's state, step constants and larval table are read through L2
+// (another CTA published them), and the pool that the scatter wrote with
+// ordinary stores is read by the next hour's bulk copies after proxy fences.
+__global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(KParams p, uint32_t nsteps) {
   extern __shared__ __align__(128) uint8_t stage[];
   __shared__ StepCtx s_c;
   __shared__ ModelConst s_mc;
+  __shared__ float s_hmr[100];
   __shared__ sampo_population s_pop;
   __shared__ __align__(8) uint64_t s_mbar;
   __shared__ uint2 s_ent[kChunks];
@@ -299,216 +307,239 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
   SimDev* sim = rp.sim;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t G = gridDim.x, b = blockIdx.x;
-  uint32_t phase = 0;
-
-  // ---- prologue: the tile's copies first, then the step's constants ----
+  uint32_t phase = 0, barriers = 0;
+  bool met = true, ok = true;
   if (tid == 0) {
     mbar_init(&s_mbar);
     fence_mbar_init();
-    const uint32_t active = sim->active;
-    const sampo_population pop = sim->pop;
-    const uint32_t end = active ? pop.r[GRAVID].end : 0u;
-    const uint32_t cur = sim->cur;
-    s_pop = pop;
-    s_active = active;
-    s_end = end;
-    s_nold = (end + kTile - 1) / kTile;
-    s_cur = cur;
-    s_cap = sim->capacity;
-    s_stride = rp.maxTiles;
-    if (b < s_nold) {
-      const uint32_t lo = b * kTile;
-      small_issue_tile(rp.pool[cur], stage, &s_mbar, lo, min((uint32_t)kTile, end - lo));
-    }
   }
-  copy16(&s_c, &sim->ctx, (int)sizeof(StepCtx), tid, blockDim.x);
   load_model_const(p.mc, s_mc);
-  __syncthreads();
-  const uint32_t nold = s_nold, end = s_end, stride = s_stride;
   uint32_t* rows = rp.tilePre;  // [kSmallRows][stride]
-  SmallAcc sa;
-  sa.acc = Acc{0, 0, 0, 0, 0, 0};
-  sa.l1 = sa.fem = sa.inf = sa.dmax = sa.devoob = sa.tilebad = 0;
-  sa.dmin = 0xffffffffu;
-  bool ok = true;
 
-  // ---- phase 1: decide (and, for tile b, finish) every tile of this CTA ----
-  if (nold > G && b < nold) {
-    // more tiles than CTAs: count tile b (its copies were issued above)
-    // without keeping it, then the other tiles of this CTA one after the
-    // other in the stage, then load tile b again and keep it
-    ok = small_wait_stage(&s_mbar, phase);
-    for (uint32_t t = b; t < nold && ok; t += G) {
-      if (t != b) {
+  for (uint32_t hour = 0; hour < nsteps; hour++) {
+    // ---- prologue: the replicate's state, the tile's copies, the step's constants ----
+    if (tid == 0) {
+      const uint32_t active = __ldcg(&sim->active);
+      const sampo_population pop = ld_l2(&sim->pop);
+      const uint32_t end = active ? pop.r[GRAVID].end : 0u;
+      const uint32_t cur = __ldcg(&sim->cur);
+      s_pop = pop;
+      s_active = active;
+      s_end = end;
+      s_nold = (end + kTile - 1) / kTile;
+      s_cur = cur;
+      s_cap = __ldcg(&sim->capacity);
+      s_stride = rp.maxTiles;
+      if (b < s_nold) {
+        const uint32_t lo = b * kTile;
+        fence_proxy_async_global();  // the last hour's scatter wrote this pool with ordinary stores
+        fence_proxy_async();         // and this stage was last read through the generic proxy
+        small_issue_tile(rp.pool[cur], stage, &s_mbar, lo, min((uint32_t)kTile, end - lo));
+      }
+    }
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(&sim->ctx);
+      uint4* dst = reinterpret_cast<uint4*>(&s_c);
+      for (int k = tid; k < (int)(sizeof(StepCtx) / 16); k += blockDim.x) dst[k] = __ldcg(src + k);
+      for (int k = tid; k < 100; k += blockDim.x) s_hmr[k] = __ldcg(&sim->larvaHMR[k]);
+    }
+    __syncthreads();
+    if (tid == 0) s_c.larvaHMR = s_hmr;
+    if (!s_active) break;  // stopped or paused: the launch has nothing more to do (uniform)
+    const uint32_t nold = s_nold, end = s_end, stride = s_stride;
+    SmallAcc sa;
+    sa.acc = Acc{0, 0, 0, 0, 0, 0};
+    sa.l1 = sa.fem = sa.inf = sa.dmax = sa.devoob = sa.tilebad = 0;
+    sa.dmin = 0xffffffffu;
+    __syncthreads();  // s_c.larvaHMR
+
+    // ---- phase 1: decide (and, for tile b, finish) every tile of this CTA ----
+    if (nold > G && b < nold) {
+      // more tiles than CTAs: count tile b (its copies were issued above)
+      // without keeping it, then the other tiles of this CTA one after the
+      // other in the stage, then load tile b again and keep it
+      ok = small_wait_stage(&s_mbar, phase);
+      for (uint32_t t = b; t < nold && ok; t += G) {
+        if (t != b) {
+          if (tid == 0) {
+            fence_proxy_async();
+            small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+          }
+          ok = small_wait_stage(&s_mbar, phase);
+          if (!ok) break;
+        }
+        const uint32_t eggs_before = sa.acc.newEggs;
+        small_update_tile<false, true, false>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
+        const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
+        if (lane == 0) s_ne[warp] = ne;
+        __syncthreads();
+        if (warp == 0) {
+          const uint32_t tw = small_build_table(s_ent, s_tab);
+          if (lane < 8) __stcg(rows + (size_t)lane * stride + t, tw);
+          uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
+          e = __reduce_add_sync(0xffffffffu, e);
+          if (lane == 0) __stcg(rows + (size_t)8 * stride + t, e);
+        }
+        __syncthreads();  // the stage is read before the next copy overwrites it
+      }
+      if (ok) {
         if (tid == 0) {
-          fence_proxy_async();  // the stage was last read through the generic proxy
-          small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+          fence_proxy_async();
+          small_issue_tile(rp.pool[s_cur], stage, &s_mbar, b * kTile, min((uint32_t)kTile, end - b * kTile));
         }
         ok = small_wait_stage(&s_mbar, phase);
-        if (!ok) break;
+        if (ok) {
+          small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);  // eggs counted above
+          __syncthreads();
+          if (warp == 0) (void)small_build_table(s_ent, s_tab);
+        }
       }
-      const uint32_t eggs_before = sa.acc.newEggs;
-      small_update_tile<false, true, false>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
-      const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
-      if (lane == 0) s_ne[warp] = ne;
-      __syncthreads();
-      if (warp == 0) {
-        const uint32_t tw = small_build_table(s_ent, s_tab);
-        if (lane < 8) __stcg(rows + (size_t)lane * stride + t, tw);
-        uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
-        e = __reduce_add_sync(0xffffffffu, e);
-        if (lane == 0) __stcg(rows + (size_t)8 * stride + t, e);
-      }
-      __syncthreads();  // the stage is read before the next copy overwrites it
-    }
-    if (ok) {
-      if (tid == 0) {
-        fence_proxy_async();
-        small_issue_tile(rp.pool[s_cur], stage, &s_mbar, b * kTile, min((uint32_t)kTile, end - b * kTile));
-      }
+    } else if (b < nold) {
       ok = small_wait_stage(&s_mbar, phase);
       if (ok) {
-        small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);  // eggs counted above
+        const uint32_t eggs_before = sa.acc.newEggs;
+        small_update_tile<true, true, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);
+        const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
+        if (lane == 0) s_ne[warp] = ne;
         __syncthreads();
-        if (warp == 0) (void)small_build_table(s_ent, s_tab);
-      }
-    }
-  } else if (b < nold) {
-    ok = small_wait_stage(&s_mbar, phase);
-    if (ok) {
-      const uint32_t eggs_before = sa.acc.newEggs;
-      small_update_tile<true, true, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);
-      const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
-      if (lane == 0) s_ne[warp] = ne;
-      __syncthreads();
-      if (warp == 0) {
-        const uint32_t tw = small_build_table(s_ent, s_tab);
-        if (lane < 8) __stcg(rows + (size_t)lane * stride + b, tw);
-        uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
-        e = __reduce_add_sync(0xffffffffu, e);
-        if (lane == 0) __stcg(rows + (size_t)8 * stride + b, e);
-      }
-    }
-  }
-  if (tid == 0) s_ok = ok ? 1u : 0u;
-
-  // ---- grid barrier: every tile's counts are published ----
-  const bool met = small_grid_barrier(&p.bat->bar, G, &s_flag);
-  ok = s_ok != 0;  // this CTA's copies all landed
-
-  // ---- phase 2: totals, next layout, this tile's first slots; scatter ----
-  small_sum_rows(rows, stride, nold, b < nold ? b : nold, true, s_ex, s_tot);
-  __syncthreads();
-  uint32_t tot[8], base[8];
-#pragma unroll
-  for (int k = 0; k < 8; k++) tot[k] = s_tot[k];
-  const uint32_t ne = s_tot[8];
-  const bool fits = layout_fits(tot, ne, s_cap);
-  {
-    sampo_population np;
-    next_layout(tot, ne, np, base);
-  }
-  if (b == 0 && tid == 0 && s_active && met) {
-    // the totals the publish reads (the three-kernel step adds them up by atomics)
-#pragma unroll
-    for (int k = 0; k < 8; k++) sim->cnt[k] = tot[k];
-    sim->newEggs = ne;
-    if (!fits) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
-  }
-  const bool write = ok && met && fits && s_active;
-  const DevPool dst = rp.pool[s_cur ^ 1u];
-  if (write && b < nold) {
-    if (tid < 8) s_d0[tid] = base[tid] + s_ex[tid];
-    __syncthreads();
-    small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
-    // more tiles than CTAs: the other tiles of this CTA, loaded and updated again
-    for (uint32_t t = b + G; t < nold; t += G) {
-      __syncthreads();  // the stage is read
-      if (tid == 0) {
-        fence_proxy_async();
-        small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
-      }
-      if (!small_wait_stage(&s_mbar, phase)) { ok = false; break; }
-      small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
-      small_sum_rows(rows, stride, nold, t, false, s_ex, s_tot);
-      __syncthreads();
-      if (warp == 0) {
-        const uint32_t tw = small_build_table(s_ent, s_tab);
-        // the update again must give the counts of phase 1
-        if (lane < 8 && tw != __ldcg(rows + (size_t)lane * stride + t)) sa.tilebad = 1;
-        if (lane < 8) s_d0[lane] = base[lane] + s_ex[lane];
-      }
-      if (__syncthreads_or(sa.tilebad)) break;
-      small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
-    }
-  }
-  if (write) {
-    // new eggs at [0, newEggs) of the next buffer, egg tile e on CTA G-1-(e mod G)
-    const uint32_t negg = (ne + kTile - 1) / kTile;
-    for (uint32_t e = G - 1 - b; e < negg; e += G) {
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        const uint32_t id = e * kTile + k * kBlock + tid;
-        if (id < ne) {
-          Rec a;
-          new_egg(s_c, id, a);
-          dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
-          dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
-          dst.batches[id] = a.batches;
-          dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
+        if (warp == 0) {
+          const uint32_t tw = small_build_table(s_ent, s_tab);
+          if (lane < 8) __stcg(rows + (size_t)lane * stride + b, tw);
+          uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
+          e = __reduce_add_sync(0xffffffffu, e);
+          if (lane == 0) __stcg(rows + (size_t)8 * stride + b, e);
         }
       }
     }
-  }
+    if (tid == 0) s_ok = ok ? 1u : 0u;
 
-  // ---- this CTA's statistics: reduced in the CTA, one atomic per counter ----
-  {
-    uint32_t v[10] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
-                      (sa.acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (sa.tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u) |
-                          (sa.devoob ? SAMPO_DEV_ERR_DEVRATES : 0u) | (ok ? 0u : SAMPO_DEV_ERR_TMA) |
-                          (met ? 0u : SAMPO_DEV_ERR_BARRIER),
-                      sa.dmin, sa.dmax};
-#pragma unroll
-    for (int j = 0; j < 7; j++) v[j] = __reduce_add_sync(0xffffffffu, v[j]);
-    v[7] = __reduce_or_sync(0xffffffffu, v[7]);
-    v[8] = __reduce_min_sync(0xffffffffu, v[8]);
-    v[9] = __reduce_max_sync(0xffffffffu, v[9]);
-    if (lane == 0) {
-#pragma unroll
-      for (int j = 0; j < 10; j++) s_red[warp][j] = v[j];
-    }
+    // ---- grid barrier A: every tile's counts are published ----
+    met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
+    ok = s_ok != 0;  // this CTA's copies all landed
+
+    // ---- phase 2: totals, next layout, this tile's first slots; scatter ----
+    small_sum_rows(rows, stride, nold, b < nold ? b : nold, true, s_ex, s_tot);
     __syncthreads();
-    if (tid < 10 && s_active) {
-      uint32_t x = s_red[0][tid];
-      for (int w = 1; w < kWarps; w++) {
-        const uint32_t y = s_red[w][tid];
-        x = tid < 7 ? x + y : tid == 7 ? (x | y) : tid == 8 ? min(x, y) : max(x, y);
+    uint32_t tot[8], base[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) tot[k] = s_tot[k];
+    const uint32_t ne = s_tot[8];
+    const bool fits = layout_fits(tot, ne, s_cap);
+    {
+      sampo_population np;
+      next_layout(tot, ne, np, base);
+    }
+    if (b == 0 && tid == 0 && met) {
+      // the totals the publish reads (the three-kernel step adds them up by atomics)
+#pragma unroll
+      for (int k = 0; k < 8; k++) sim->cnt[k] = tot[k];
+      sim->newEggs = ne;
+      if (!fits) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
+    }
+    const bool write = ok && met && fits;
+    const DevPool dst = rp.pool[s_cur ^ 1u];
+    if (write && b < nold) {
+      if (tid < 8) s_d0[tid] = base[tid] + s_ex[tid];
+      __syncthreads();
+      small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
+      // more tiles than CTAs: the other tiles of this CTA, loaded and updated again
+      for (uint32_t t = b + G; t < nold; t += G) {
+        __syncthreads();  // the stage is read
+        if (tid == 0) {
+          fence_proxy_async();
+          small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+        }
+        if (!small_wait_stage(&s_mbar, phase)) { ok = false; break; }
+        small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
+        small_sum_rows(rows, stride, nold, t, false, s_ex, s_tot);
+        __syncthreads();
+        if (warp == 0) {
+          const uint32_t tw = small_build_table(s_ent, s_tab);
+          // the update again must give the counts of phase 1
+          if (lane < 8 && tw != __ldcg(rows + (size_t)lane * stride + t)) sa.tilebad = 1;
+          if (lane < 8) s_d0[lane] = base[lane] + s_ex[lane];
+        }
+        if (__syncthreads_or(sa.tilebad)) break;
+        small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
       }
-      uint32_t* const acc0 = tid == 0 ? &sim->acc_L1de : tid == 1 ? &sim->acc_fem : tid == 2 ? &sim->acc_inf
-                                                                                            : &sim->acc_bnc[tid < 7 ? tid - 3 : 0];
-      if (tid < 7) { if (x) atomicAdd(acc0, x); }
-      else if (tid == 7) { if (x) atomicOr(&sim->error, x); }
-      else if (tid == 8) { if (x != 0xffffffffu) atomicMin(&sim->acc_dmin, x); }
-      else { if (x) atomicMax(&sim->acc_dmax, x); }
+    }
+    if (write) {
+      // new eggs at [0, newEggs) of the next buffer, egg tile e on CTA G-1-(e mod G)
+      const uint32_t negg = (ne + kTile - 1) / kTile;
+      for (uint32_t e = G - 1 - b; e < negg; e += G) {
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+          const uint32_t id = e * kTile + k * kBlock + tid;
+          if (id < ne) {
+            Rec a;
+            new_egg(s_c, id, a);
+            dst.age[id] = a.age; dst.his[id] = a.his; dst.delay[id] = a.delay; dst.sporo[id] = a.sporo;
+            dst.uni[id] = a.uni; dst.avail[id] = a.avail; dst.cycle[id] = a.cycle; dst.hbc[id] = a.hbc;
+            dst.batches[id] = a.batches;
+            dst.flags[id] = (uint8_t)(EGG | (a.female << 3));
+          }
+        }
+      }
+    }
+    fence_proxy_async_global();  // the next hour reads these stores with bulk copies
+
+    // ---- this CTA's statistics: reduced in the CTA, one atomic per counter ----
+    {
+      uint32_t v[10] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
+                        (sa.acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (sa.tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u) |
+                            (sa.devoob ? SAMPO_DEV_ERR_DEVRATES : 0u) | (ok ? 0u : SAMPO_DEV_ERR_TMA) |
+                            (met ? 0u : SAMPO_DEV_ERR_BARRIER),
+                        sa.dmin, sa.dmax};
+#pragma unroll
+      for (int j = 0; j < 7; j++) v[j] = __reduce_add_sync(0xffffffffu, v[j]);
+      v[7] = __reduce_or_sync(0xffffffffu, v[7]);
+      v[8] = __reduce_min_sync(0xffffffffu, v[8]);
+      v[9] = __reduce_max_sync(0xffffffffu, v[9]);
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < 10; j++) s_red[warp][j] = v[j];
+      }
+      __syncthreads();
+      if (tid < 10) {
+        uint32_t x = s_red[0][tid];
+        for (int w = 1; w < kWarps; w++) {
+          const uint32_t y = s_red[w][tid];
+          x = tid < 7 ? x + y : tid == 7 ? (x | y) : tid == 8 ? min(x, y) : max(x, y);
+        }
+        uint32_t* const acc0 = tid == 0 ? &sim->acc_L1de : tid == 1 ? &sim->acc_fem : tid == 2 ? &sim->acc_inf
+                                                                                              : &sim->acc_bnc[tid < 7 ? tid - 3 : 0];
+        if (tid < 7) { if (x) atomicAdd(acc0, x); }
+        else if (tid == 7) { if (x) atomicOr(&sim->error, x); }
+        else if (tid == 8) { if (x != 0xffffffffu) atomicMin(&sim->acc_dmin, x); }
+        else { if (x) atomicMax(&sim->acc_dmax, x); }
+      }
+    }
+    if (!met || !ok) break;  // the error bits are set; nothing after this hour is valid
+
+    // ---- grid barrier B: every CTA's stores and statistics are in ----
+    met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
+    if (!met) break;
+    if (b == 0) (void)publish_rep(p, 0u, PUB_AFTER_STEP);  // the whole CTA
+    // ---- grid barrier C: the next hour's state is published ----
+    if (hour + 1 < nsteps) {
+      met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
+      if (!met) break;
     }
   }
+  if (!met && tid == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_BARRIER);
   // a copy that did not land in time may still be in flight: let it land
   // (bounded) before the CTA can exit
   if (!ok && tid == 0) (void)mbar_wait(&s_mbar, phase ^ 1u);
 
-  // ---- the last CTA out publishes the next step ----
+  // ---- the last CTA out rearms the barrier for the next launch ----
   __syncthreads();
   if (tid == 0) {
     __threadfence();
     s_last = atomicAdd(&p.bat->done, 1u) == G - 1u ? 1u : 0u;
-    if (s_last) __threadfence();
-  }
-  __syncthreads();
-  if (!s_last) return;
-  (void)publish_rep(p, 0u, PUB_AFTER_STEP);
-  if (tid == 0) {
-    p.bat->bar = 0u;
-    p.bat->done = 0u;
+    if (s_last) {
+      p.bat->bar = 0u;
+      p.bat->done = 0u;
+    }
   }
 }
 

@@ -68,10 +68,10 @@ def test_paths_agree(gpu_ready, oracle_mod, sizes, n, cc):
         assert oracle_mod.pool_hash(got[1]["ranges"], got[2]) == oracle_mod.pool_hash(ref[1]["ranges"], ref[2])
         assert np.array_equal(got[3], ref[3])
     if sizes[0] == 8000:
-        # a small pool takes one launch per hour (plus the constants refresh
-        # at the start of the run)
+        # a small pool takes one launch per simulated day (plus the constants
+        # refresh at the start of the run)
         got = _run(ranges, arrays, T, env, seeds, cc, n, None, cap)
-        assert got[6] == 1 + n, got[6]
+        assert got[6] == 1 + n // 24, got[6]
 
 
 def test_small_step_matches_oracle(gpu_ready, oracle_mod):
