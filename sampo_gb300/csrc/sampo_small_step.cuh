@@ -47,20 +47,22 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   return v;
 }
 
-// All CTAs of the grid (co-resident: a cooperative launch) wait until each
-// has arrived. Bounded: false when the others did not arrive within the
-// limit. Every thread calls it; every thread gets the same answer.
-__device__ bool small_grid_barrier(uint32_t* bar, uint32_t nblocks, uint32_t* s_flag) {
+// All CTAs of the grid (co-resident: a cooperative launch) wait until the
+// arrival counter reaches `target` (the grid size times the barriers passed
+// so far in the launch). The CTA's writes are ordered before its arrival by
+// the CTA barrier and the release of the arrival; the acquire of the counter
+// orders the reads that follow. Bounded: false when the others did not
+// arrive within the limit. Every thread calls it; every thread gets the same
+// answer.
+__device__ bool small_grid_barrier(uint32_t* bar, uint32_t target, uint32_t* s_flag) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();  // this CTA's writes before its arrival
-    atomicAdd(bar, 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
     uint32_t ok = 0;
     for (uint32_t i = 0; i < kWaitLimit; i++) {
-      if (ld_acquire_u32(bar) >= nblocks) { ok = 1; break; }
-      __nanosleep(64);
+      if (ld_acquire_u32(bar) >= target) { ok = 1; break; }
+      if (i >= 32) __nanosleep(32);
     }
-    __threadfence();
     *s_flag = ok;
   }
   __syncthreads();
@@ -281,15 +283,27 @@ __device__ __forceinline__ void small_issue_tile(const DevPool& src, uint8_t* st
 
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
-// The one-launch steps of p.reps[0] (a single simulation): `nsteps` hourly
-// steps in one cooperative launch, each one update, one scatter and one
-// publish separated by grid barriers (a day graph launches it once with 24).
-// The per-tile count rows use the replicate's prefix-table array (tilePre:
-// kPreWords words per tile, of which the rows take kSmallRows), which the
-// three-kernel step rewrites before it reads it. Within the launch the
-// replicate's state, step constants and larval table are read through L2
-// (another CTA published them), and the pool that the scatter wrote with
-// ordinary stores is read by the next hour's bulk copies after proxy fences.
+// Per-hour statistics of the next pool, accumulated by every CTA with
+// atomics (words: L1de, females, infective, cycles, sum of cycles, bites,
+// infective bites, min and max larva age in days). Two sets alternate by
+// hour, so that one is cleared while the other is read.
+constexpr uint32_t kSmallAcc = 16;
+enum : uint32_t { SA_L1 = 0, SA_FEM, SA_INF, SA_CYC, SA_SUMCYC, SA_BITES, SA_IBITES, SA_DMIN, SA_DMAX };
+
+// The one-launch steps of p.reps[0] (a single simulation without a device
+// seed stream): `nsteps` hourly steps in one cooperative launch (a day graph
+// launches it once with 24). Per hour: the update (phase 1), a grid barrier,
+// the scatter (phase 2) and the statistics, a second grid barrier; then
+// every CTA computes the next hour's layout, statistics row, step constants
+// and larval table itself from the same totals (the k_publish arithmetic),
+// while the next hour's tile is already on its way, and the last CTA (the
+// one least likely to hold a tile) writes them to the replicate's state for
+// the host. The per-tile count rows and the two
+// sets of hourly statistics use the replicate's prefix-table array (tilePre:
+// kPreWords words per tile; the rows take kSmallRows per tile, the
+// statistics 2 x kSmallAcc words after them), which the three-kernel step
+// rewrites before it reads it. The pool the scatter wrote with ordinary
+// stores is read by the next hour's bulk copies after proxy fences.
 __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(KParams p, uint32_t nsteps) {
   extern __shared__ __align__(128) uint8_t stage[];
   __shared__ StepCtx s_c;
@@ -300,62 +314,62 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
   __shared__ uint2 s_ent[kChunks];
   __shared__ __align__(16) uint32_t s_tab[(kChunks + 1) * kPreEntryWords];
   __shared__ uint32_t s_ex[kSmallRows], s_tot[kSmallRows], s_d0[8], s_ne[kWarps];
-  __shared__ uint32_t s_red[kWarps][10];
+  __shared__ uint32_t s_red[kWarps][10], s_acc[kSmallAcc];
   __shared__ uint32_t s_flag, s_ok, s_last;
-  __shared__ uint32_t s_active, s_end, s_nold, s_cur, s_cap, s_stride;
+  __shared__ uint32_t s_active, s_end, s_nold, s_cur, s_cap, s_step, s_epoch, s_stop;
+  __shared__ float s_cc;
   const RepParams& rp = p.reps[0];
   SimDev* sim = rp.sim;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t G = gridDim.x, b = blockIdx.x;
   uint32_t phase = 0, barriers = 0;
   bool met = true, ok = true;
+  const uint32_t stride = rp.maxTiles;
+  uint32_t* rows = rp.tilePre;                       // [kSmallRows][stride]
+  uint32_t* accs = rows + (size_t)kSmallRows * stride;  // [2][kSmallAcc]
+
+  // ---- the replicate's state at the launch (the previous kernel wrote it) ----
   if (tid == 0) {
     mbar_init(&s_mbar);
     fence_mbar_init();
+    const uint32_t active = sim->active;
+    s_pop = sim->pop;
+    s_active = active;
+    s_end = active ? s_pop.r[GRAVID].end : 0u;
+    s_nold = (s_end + kTile - 1) / kTile;
+    s_cur = sim->cur;
+    s_cap = sim->capacity;
+    s_step = sim->step;
+    s_epoch = sim->epoch;
+    s_stop = sim->stop_step;
+    s_cc = sim->cc;
+    if (b < s_nold) {
+      const uint32_t lo = b * kTile;
+      small_issue_tile(rp.pool[s_cur], stage, &s_mbar, lo, min((uint32_t)kTile, s_end - lo));
+    }
+    if (b == G - 1u) {  // both sets of hourly statistics start cleared
+      for (uint32_t k = 0; k < 2 * kSmallAcc; k++) accs[k] = (k % kSmallAcc) == SA_DMIN ? 0xffffffffu : 0u;
+    }
   }
+  copy16(&s_c, &sim->ctx, (int)sizeof(StepCtx), tid, blockDim.x);
+  for (int k = tid; k < 100; k += blockDim.x) s_hmr[k] = sim->larvaHMR[k];
   load_model_const(p.mc, s_mc);
-  uint32_t* rows = rp.tilePre;  // [kSmallRows][stride]
+  __syncthreads();
+  if (tid == 0) s_c.larvaHMR = s_hmr;
+  __syncthreads();
 
   for (uint32_t hour = 0; hour < nsteps; hour++) {
-    // ---- prologue: the replicate's state, the tile's copies, the step's constants ----
-    if (tid == 0) {
-      const uint32_t active = __ldcg(&sim->active);
-      const sampo_population pop = ld_l2(&sim->pop);
-      const uint32_t end = active ? pop.r[GRAVID].end : 0u;
-      const uint32_t cur = __ldcg(&sim->cur);
-      s_pop = pop;
-      s_active = active;
-      s_end = end;
-      s_nold = (end + kTile - 1) / kTile;
-      s_cur = cur;
-      s_cap = __ldcg(&sim->capacity);
-      s_stride = rp.maxTiles;
-      if (b < s_nold) {
-        const uint32_t lo = b * kTile;
-        fence_proxy_async_global();  // the last hour's scatter wrote this pool with ordinary stores
-        fence_proxy_async();         // and this stage was last read through the generic proxy
-        small_issue_tile(rp.pool[cur], stage, &s_mbar, lo, min((uint32_t)kTile, end - lo));
-      }
-    }
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(&sim->ctx);
-      uint4* dst = reinterpret_cast<uint4*>(&s_c);
-      for (int k = tid; k < (int)(sizeof(StepCtx) / 16); k += blockDim.x) dst[k] = __ldcg(src + k);
-      for (int k = tid; k < 100; k += blockDim.x) s_hmr[k] = __ldcg(&sim->larvaHMR[k]);
-    }
-    __syncthreads();
-    if (tid == 0) s_c.larvaHMR = s_hmr;
-    if (!s_active) break;  // stopped or paused: the launch has nothing more to do (uniform)
-    const uint32_t nold = s_nold, end = s_end, stride = s_stride;
+    if (!s_active) break;  // stopped or paused (uniform)
+    const uint32_t nold = s_nold, end = s_end;
+    uint32_t* acc = accs + (hour & 1u) * kSmallAcc;
     SmallAcc sa;
     sa.acc = Acc{0, 0, 0, 0, 0, 0};
     sa.l1 = sa.fem = sa.inf = sa.dmax = sa.devoob = sa.tilebad = 0;
     sa.dmin = 0xffffffffu;
-    __syncthreads();  // s_c.larvaHMR
 
     // ---- phase 1: decide (and, for tile b, finish) every tile of this CTA ----
     if (nold > G && b < nold) {
-      // more tiles than CTAs: count tile b (its copies were issued above)
+      // more tiles than CTAs: count tile b (its copies are on their way)
       // without keeping it, then the other tiles of this CTA one after the
       // other in the stage, then load tile b again and keep it
       ok = small_wait_stage(&s_mbar, phase);
@@ -416,6 +430,10 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     // ---- grid barrier A: every tile's counts are published ----
     met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
     ok = s_ok != 0;  // this CTA's copies all landed
+    if (b == G - 1u && tid == 0) {  // every CTA has read the other set of statistics (last hour's): clear it
+      uint32_t* other = accs + ((hour + 1u) & 1u) * kSmallAcc;
+      for (uint32_t k = 0; k < kSmallAcc; k++) other[k] = k == SA_DMIN ? 0xffffffffu : 0u;
+    }
 
     // ---- phase 2: totals, next layout, this tile's first slots; scatter ----
     small_sum_rows(rows, stride, nold, b < nold ? b : nold, true, s_ex, s_tot);
@@ -425,17 +443,8 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     for (int k = 0; k < 8; k++) tot[k] = s_tot[k];
     const uint32_t ne = s_tot[8];
     const bool fits = layout_fits(tot, ne, s_cap);
-    {
-      sampo_population np;
-      next_layout(tot, ne, np, base);
-    }
-    if (b == 0 && tid == 0 && met) {
-      // the totals the publish reads (the three-kernel step adds them up by atomics)
-#pragma unroll
-      for (int k = 0; k < 8; k++) sim->cnt[k] = tot[k];
-      sim->newEggs = ne;
-      if (!fits) atomicOr(&sim->error, SAMPO_DEV_ERR_CAPACITY);
-    }
+    sampo_population np;
+    next_layout(tot, ne, np, base);
     const bool write = ok && met && fits;
     const DevPool dst = rp.pool[s_cur ^ 1u];
     if (write && b < nold) {
@@ -488,7 +497,7 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
       uint32_t v[10] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
                         (sa.acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (sa.tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u) |
                             (sa.devoob ? SAMPO_DEV_ERR_DEVRATES : 0u) | (ok ? 0u : SAMPO_DEV_ERR_TMA) |
-                            (met ? 0u : SAMPO_DEV_ERR_BARRIER),
+                            (met ? 0u : SAMPO_DEV_ERR_BARRIER) | (fits ? 0u : SAMPO_DEV_ERR_CAPACITY),
                         sa.dmin, sa.dmax};
 #pragma unroll
       for (int j = 0; j < 7; j++) v[j] = __reduce_add_sync(0xffffffffu, v[j]);
@@ -506,12 +515,10 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
           const uint32_t y = s_red[w][tid];
           x = tid < 7 ? x + y : tid == 7 ? (x | y) : tid == 8 ? min(x, y) : max(x, y);
         }
-        uint32_t* const acc0 = tid == 0 ? &sim->acc_L1de : tid == 1 ? &sim->acc_fem : tid == 2 ? &sim->acc_inf
-                                                                                              : &sim->acc_bnc[tid < 7 ? tid - 3 : 0];
-        if (tid < 7) { if (x) atomicAdd(acc0, x); }
-        else if (tid == 7) { if (x) atomicOr(&sim->error, x); }
-        else if (tid == 8) { if (x != 0xffffffffu) atomicMin(&sim->acc_dmin, x); }
-        else { if (x) atomicMax(&sim->acc_dmax, x); }
+        if (tid < 7) { if (x) atomicAdd(&acc[tid], x); }
+        else if (tid == 7) { if (x && (b == 0 || (x & ~SAMPO_DEV_ERR_CAPACITY))) atomicOr(&sim->error, x); }
+        else if (tid == 8) { if (x != 0xffffffffu) atomicMin(&acc[SA_DMIN], x); }
+        else { if (x) atomicMax(&acc[SA_DMAX], x); }
       }
     }
     if (!met || !ok) break;  // the error bits are set; nothing after this hour is valid
@@ -519,17 +526,94 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     // ---- grid barrier B: every CTA's stores and statistics are in ----
     met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
     if (!met) break;
-    if (b == 0) (void)publish_rep(p, 0u, PUB_AFTER_STEP);  // the whole CTA
-    // ---- grid barrier C: the next hour's state is published ----
-    if (hour + 1 < nsteps) {
-      met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
-      if (!met) break;
+    if (!fits) {
+      // the next layout does not fit: the replicate pauses at this step with
+      // its pool and constants (k_publish does the same for the three-kernel step)
+      if (b == G - 1u && tid == 0) sim->active = 0;
+      break;
     }
+
+    // ---- the next hour's tile is on its way while every CTA computes the
+    //      next hour's state (the k_publish arithmetic, publish_rep) ----
+    const uint32_t step = s_step + 1u;
+    const bool active = step < s_stop;
+    const uint32_t next_end = np.r[GRAVID].end, next_nold = (next_end + kTile - 1) / kTile;
+    if (tid == 0 && b < next_nold && active && hour + 1u < nsteps) {  // (no copy is left in flight at the exit)
+      fence_proxy_async_global();
+      fence_proxy_async();
+      small_issue_tile(dst, stage, &s_mbar, b * kTile, min((uint32_t)kTile, next_end - b * kTile));
+    }
+    if (tid == 0) {
+      uint32_t st[kSmallAcc];
+#pragma unroll
+      for (int k = 0; k < (int)kSmallAcc; k++) st[k] = __ldcg(&acc[k]);
+      s_acc[0] = st[SA_L1]; s_acc[1] = st[SA_FEM]; s_acc[2] = st[SA_INF]; s_acc[3] = st[SA_CYC];
+      s_acc[4] = st[SA_SUMCYC]; s_acc[5] = st[SA_BITES]; s_acc[6] = st[SA_IBITES]; s_acc[7] = st[SA_DMIN]; s_acc[8] = st[SA_DMAX];
+    }
+    __syncthreads();
+    // the next pool's statistics (kernel/calcL1de.cl:259-280, calcGender.cl)
+    np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? s_acc[0] : 0u;
+    np.numFemale = s_acc[1];
+    np.numPotentiallyInfective = s_acc[2];
+    sampo_bites_cycles nbnc;
+    nbnc.numCyclesReported = s_acc[3];
+    nbnc.sumCyclesReported = s_acc[4];
+    nbnc.numBitesReported = s_acc[5];
+    nbnc.numInfectBitesReported = s_acc[6];
+    // the reference's shared empty initial ranges (src/abms.c:204-219)
+    bool shared_end = false;
+    uint32_t moved = 0;
+    for (int k = 1; k < 8; k++) {
+      shared_end |= s_pop.r[k].end == s_pop.r[k - 1].end;
+      moved += tot[k];
+    }
+    if (tid == 0) {
+      CtxInputs in;
+      load_ctx_inputs(rp, step, in);
+      StepCtx c;
+      make_ctx(in, sim->larvaHMR, np, c);  // the global table: the last CTA stores this one
+      if (b == G - 1u) {
+        // the replicate's state and the coming step's row for the host
+        if (shared_end && moved) sim->warn = __ldcg(&sim->warn) | SAMPO_DEV_WARN_REF_LAYOUT;
+        sim->ctx = c;
+        sim->pop = np;
+        sim->bnc = nbnc;
+        sim->step = step;
+        sim->cur = s_cur ^ 1u;
+        sim->epoch = s_epoch + 1u;
+        sampo_stats_row row;
+        row.pop = np;
+        row.bnc = nbnc;
+        rp.rows[step % rp.ring] = row;
+        if (!active) sim->active = 0;
+      }
+      c.larvaHMR = s_hmr;
+      s_c = c;
+    }
+    {  // the next hour's larval table (every CTA; the last one also stores it)
+      const uint32_t dmin = s_acc[7], dmax = s_acc[8], l1 = np.numLarvae1DayEquiv;
+      for (int d = tid - 32; d >= 0 && d < 100; d += blockDim.x - 32) {
+        const float h = larva_hmr_entry((uint32_t)d, dmin, dmax, l1, s_cc);
+        s_hmr[d] = h;
+        if (b == G - 1u) sim->larvaHMR[d] = h;
+      }
+    }
+    __syncthreads();  // s_acc, s_c, s_hmr are read and written
+    if (tid == 0) {
+      s_pop = np;
+      s_step = step;
+      s_epoch += 1u;
+      s_cur ^= 1u;
+      s_end = next_end;
+      s_nold = next_nold;
+      s_active = active;
+    }
+    __syncthreads();
   }
   if (!met && tid == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_BARRIER);
   // a copy that did not land in time may still be in flight: let it land
   // (bounded) before the CTA can exit
-  if (!ok && tid == 0) (void)mbar_wait(&s_mbar, phase ^ 1u);
+  if (tid == 0 && !ok) (void)mbar_wait(&s_mbar, phase ^ 1u);  // the phase whose wait ran out
 
   // ---- the last CTA out rearms the barrier for the next launch ----
   __syncthreads();

@@ -625,6 +625,17 @@ __device__ __forceinline__ T ld_l2(const T* p) {
   return v;
 }
 
+// The larval hourly mortality of larvae d days old in a pool of L1de l1
+// (kernel/killAgents.cl:117-125); NaN outside the ages [dmin, dmax] present.
+__device__ __forceinline__ float larva_hmr_entry(uint32_t d, uint32_t dmin, uint32_t dmax, uint32_t l1, float cc) {
+  if (d < dmin || d > dmax) return SAMPO_NAN_F;
+  float dmr = 0.1f * sampo_expf((float)l1 / ((float)d * cc * 1.0f));
+  dmr = sampo_fminf(dmr, 0.8f);
+  const float dsr = 1.0f - dmr;
+  const float hsr = sampo_powf(dsr, 1.0f / 24.0f);
+  return 1.0f - hsr;
+}
+
 // The publish of replicate r by the calling CTA (at least kPublishThreads
 // threads; all of them call it): after a step, the next layout from the
 // survivor counts (kernel/oldToNewAgents.cl:57-95); then the pool's L1de,
@@ -766,16 +777,7 @@ __device__ uint32_t publish_rep(const KParams& p, uint32_t r, int mode) {
     if (step >= stop) sim->active = 0;
   } else if (threadIdx.x >= 32) {
     for (int d = threadIdx.x - 32; d < 100; d += blockDim.x - 32) {
-      float hmr = SAMPO_NAN_F;
-      if ((uint32_t)d >= s_dmin && (uint32_t)d <= s_dmax) {
-        // kernel/killAgents.cl:117-125
-        float dmr = 0.1f * sampo_expf((float)s_l1 / ((float)(uint32_t)d * s_cc * 1.0f));
-        dmr = sampo_fminf(dmr, 0.8f);
-        float dsr = 1.0f - dmr;
-        float hsr = sampo_powf(dsr, 1.0f / 24.0f);
-        hmr = 1.0f - hsr;
-      }
-      sim->larvaHMR[d] = hmr;
+      sim->larvaHMR[d] = larva_hmr_entry((uint32_t)d, s_dmin, s_dmax, s_l1, s_cc);
     }
   }
   return pool_end;
