@@ -528,7 +528,13 @@ def served_arm(args):
                 return True
             return x.rows is not None and x.rows.tobytes() == p["rows"].tobytes()
         exact = sum(int(same(x)) for x in res)
+        # the stream's work, and how fast each path does it: batching cannot
+        # beat the rate at which the HBM-bound large requests already run alone
+        agent_days = sum(float(live_counts(x.rows[:-1]).sum()) for x in res if x.rows is not None) / 24.0
+        service = sum(p["service"] for p in plain.values())
         per_rate[str(rate)] = {
+            "agent_days": agent_days, "batched_agent_days_per_s": agent_days / makespan,
+            "one_at_a_time_agent_days_per_s": agent_days / service,
             "sims_per_s": len(res) / makespan, "latency_s": latency_summary([r.latency for r in res]),
             "one_at_a_time": {"sims_per_s": len(reqs) / plain_makespan, "latency_s": latency_summary(lat_plain)},
             "speedup_sims_per_s": (len(res) / makespan) / (len(reqs) / plain_makespan),
