@@ -174,14 +174,22 @@ int sampo_read_pool(sampo_sim* s, sampo_population* pop, sampo_pool_view* pool);
  * carrying capacity and room for its pool. */
 int sampo_checkpoint_save(sampo_sim* s, const char* path);
 /* Autotuner (no counterpart in the reference): times the step kernels on the
- * coming step of this simulation at every persistent grid size the occupancy
- * allows (CTAs per SM of the count and update/scatter passes), keeps the
- * fastest for the following steps and returns them. The trials leave the
- * simulation's course unchanged. Needs the coming step's inputs. */
+ * coming step of this simulation for each tile size (1024- and 512-slot
+ * tiles: 4 or 2 slots per thread) at every persistent grid size the
+ * occupancy allows (CTAs per SM of the count and update/scatter passes),
+ * keeps the fastest for the following steps and returns the grids (the tile
+ * size: sampo_items_per_thread). The trials leave the simulation's course
+ * unchanged. Needs the coming step's inputs. */
 int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
 /* Sets the grid sizes sampo_autotune would pick, e.g. a choice tuned earlier
  * on the same workload: 1 .. the occupancy limit of each pass. */
 int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
+/* Slots per thread of the count and update/scatter passes: 4 (1024-slot
+ * tiles, the default) or 2 (512-slot tiles); results do not depend on it. A
+ * run-time species runs 4. Setting it resets the grids to the largest the
+ * occupancy allows. */
+int sampo_set_items_per_thread(sampo_sim* s, uint32_t items);
+int sampo_items_per_thread(sampo_sim* s, uint32_t* items);
 /* One-launch step for small pools (for such pools it replaces the per-step
  * launch sequence of src/abms.c:502-529 that the three-kernel step already
  * shortens). sampo_run picks each day's graph from the pool size it last
@@ -279,7 +287,7 @@ int sampo_read_environment_file(const char* path, sampo_environment* out, uint32
  * buffers; the step's scratch (step state, per-tile prefix tables and
  * look-back counts, one step of inputs and stats) lives in a fixed array
  * inside the library, sized for pools of up to SAMPO_NOALLOC_MAX_SLOTS slots
- * (about 12 MB, held by every GPU that loads the library until the process
+ * (about 15 MB, held by every GPU that loads the library until the process
  * exits).
  *
  * in/out: device columns of two pool buffers; each column 16-byte aligned
@@ -403,6 +411,9 @@ int sampo_batch_read_pool(sampo_batch* b, uint32_t slot, sampo_population* pop, 
 /* The autotuner of sampo_autotune over the batch's coming step. */
 int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm, uint32_t* scatter_ctas_per_sm);
 int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm, uint32_t scatter_ctas_per_sm);
+/* As sampo_set_items_per_thread / sampo_items_per_thread, for the batch. */
+int sampo_batch_set_items_per_thread(sampo_batch* b, uint32_t items);
+int sampo_batch_items_per_thread(sampo_batch* b, uint32_t* items);
 /* The species of every replicate of the batch (NULL: built in); as
  * sampo_set_species. */
 int sampo_batch_set_species(sampo_batch* b, const sampo_species* sp);

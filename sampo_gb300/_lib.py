@@ -142,6 +142,10 @@ SIGNATURES = {
     "sampo_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "sampo_set_small_step": (C.c_int, [_P, C.c_uint32]),
+    "sampo_set_items_per_thread": (C.c_int, [_P, C.c_uint32]),
+    "sampo_items_per_thread": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "sampo_batch_set_items_per_thread": (C.c_int, [_P, C.c_uint32]),
+    "sampo_batch_items_per_thread": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "sampo_small_step_info": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int),
                                          C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "sampo_species_compile": (C.c_int, [C.c_char_p, C.c_int, C.c_char_p, C.c_size_t, C.POINTER(_P)]),

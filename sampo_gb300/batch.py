@@ -164,6 +164,15 @@ class Batch:
         """sampo_batch_set_grids: fix the grid sizes without tuning."""
         self._check(self.lib.sampo_batch_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))
 
+    def set_items_per_thread(self, items: int):
+        """sampo_batch_set_items_per_thread: 2 or 4 slots per thread."""
+        self._check(self.lib.sampo_batch_set_items_per_thread(self.h, items))
+
+    def items_per_thread(self) -> int:
+        v = C.c_uint32()
+        self._check(self.lib.sampo_batch_items_per_thread(self.h, C.byref(v)))
+        return v.value
+
     def last_run_ms(self) -> float:
         v = C.c_double()
         self._check(self.lib.sampo_batch_last_run_ms(self.h, C.byref(v)))

@@ -54,6 +54,7 @@ struct sampo_sim {
   bool have_pop = false;
   bool pending = false;                // steps queued by sampo_run_async, not yet synced
   int grid_count = 0, grid_scatter = 0;
+  int items = kItems;                  // slots per thread of the count and update/scatter passes (2 or 4)
   cudaGraphExec_t day_graph = nullptr;  // 24 three-kernel steps
   uint32_t day_graph_kernels = 0;      // kernel nodes of day_graph (counted at capture)
   // One-launch step for small pools: day graphs of 24 one-launch steps on
@@ -195,9 +196,9 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
       P.flags = (uint8_t*)(m + 9 * col4);
     }
     if (rc) break;
-    s->max_tiles = (uint32_t)((C + kTile - 1) / kTile);
-    if ((e = cudaMalloc(&s->tile_mem, (size_t)s->max_tiles * kTileArrayWords * 4)) != cudaSuccess) { rc = cuda_fail(s, e, "tile arrays"); break; }
-    cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream);
+    s->max_tiles = (uint32_t)((C + kTileMin - 1) / kTileMin);  // room for the smaller tile's count
+    if ((e = cudaMalloc(&s->tile_mem, tile_array_words(s->max_tiles) * 4)) != cudaSuccess) { rc = cuda_fail(s, e, "tile arrays"); break; }
+    cudaMemsetAsync(s->tile_mem, 0, tile_array_words(s->max_tiles) * 4, s->stream);
     if ((e = cudaMalloc(&s->sim_dev, sizeof(SimDev))) != cudaSuccess ||
         (e = cudaMalloc(&s->rep_dev, sizeof(RepParams))) != cudaSuccess ||
         (e = cudaMalloc(&s->bat_dev, sizeof(BatchDev))) != cudaSuccess ||
@@ -309,7 +310,7 @@ static int reset_state(sampo_sim* s, const sampo_population& pop) {
   // running step's epoch. Epochs restart here, so flags left by an earlier
   // run must go: clear the tile arrays before the first step.
   h.epoch = 1;
-  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream), "tile reset");
+  CK(cudaMemsetAsync(s->tile_mem, 0, tile_array_words(s->max_tiles) * 4, s->stream), "tile reset");
   // the one-launch step's grid barrier and exit counters start from zero
   CK(cudaMemsetAsync(&s->bat_dev->bar, 0, 2 * sizeof(uint32_t), s->stream), "barrier reset");
   CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state reset");
@@ -396,9 +397,9 @@ static int check_device(sampo_sim* s) {
 }
 
 static cudaError_t launch_step(sampo_sim* s, const KParams& p) {
-  cudaError_t e = launch_count(p, s->grid_count, s->stream);
+  cudaError_t e = launch_count(p, s->grid_count, s->stream, s->items);
   if (e != cudaSuccess) return e;
-  if ((e = launch_scatter(p, s->grid_scatter, s->stream)) != cudaSuccess) return e;
+  if ((e = launch_scatter(p, s->grid_scatter, s->stream, s->items)) != cudaSuccess) return e;
   return launch_publish(p, PUB_AFTER_STEP, s->stream);
 }
 
@@ -576,9 +577,9 @@ static int queue_run(sampo_sim* s, uint32_t nsteps, sampo_stats_row* rows, bool 
     if (s->timing) {
       for (uint32_t i = 0; i < n; i++) {
         CK(cudaEventRecord(s->ev[0], s->stream), "event");
-        CK(launch_count(p, s->grid_count, s->stream), "count kernel");
+        CK(launch_count(p, s->grid_count, s->stream, s->items), "count kernel");
         CK(cudaEventRecord(s->ev[1], s->stream), "event");
-        CK(launch_scatter(p, s->grid_scatter, s->stream), "scatter kernel");
+        CK(launch_scatter(p, s->grid_scatter, s->stream, s->items), "scatter kernel");
         CK(cudaEventRecord(s->ev[2], s->stream), "event");
         CK(launch_publish(p, PUB_AFTER_STEP, s->stream), "publish kernel");
         CK(cudaEventRecord(s->ev[4], s->stream), "event");
@@ -840,7 +841,7 @@ extern "C" int sampo_checkpoint_load(sampo_sim* s, const char* path) {
   h.bnc = hd.bnc;
   h.step = hd.step;
   h.active = 1;
-  CK(cudaMemsetAsync(s->tile_mem, 0, (size_t)s->max_tiles * kTileArrayWords * 4, s->stream), "tile reset");
+  CK(cudaMemsetAsync(s->tile_mem, 0, tile_array_words(s->max_tiles) * 4, s->stream), "tile reset");
   CK(cudaMemcpyAsync(s->sim_dev, &h, sizeof(SimDev), cudaMemcpyHostToDevice, s->stream), "state");
   s->step = hd.step;
   const int rc = publish_initial(s);
@@ -866,14 +867,15 @@ extern "C" int sampo_autotune(sampo_sim* s, uint32_t* count_ctas_per_sm, uint32_
   cudaSetDevice(s->device);
   const KParams p = make_params(s);
   CK(launch_publish(p, PUB_REFRESH, s->stream), "step constants");
-  int gc = 0, gs = 0;
-  CK(tune_grids(p, s->stream, &gc, &gs, nullptr), "autotune");
+  int gc = 0, gs = 0, items = kItems;
+  CK(tune_grids(p, s->stream, &gc, &gs, &items, nullptr), "autotune");
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
   if (sms <= 0) sms = 1;
-  if (gc != s->grid_count || gs != s->grid_scatter) {
+  if (gc != s->grid_count || gs != s->grid_scatter || items != s->items) {
     s->grid_count = gc;
     s->grid_scatter = gs;
+    s->items = items;
     drop_day_graph(s);  // captured with the old grids
   }
   if (count_ctas_per_sm) *count_ctas_per_sm = (uint32_t)(gc / sms);
@@ -888,8 +890,9 @@ extern "C" int sampo_set_species(sampo_sim* s, const sampo_species* sp) {
   cudaSetDevice(s->device);
   if (s->species == sp) return SAMPO_OK;
   s->species = sp;
-  s->grid_count = grid_blocks_count(1, sp);
-  s->grid_scatter = grid_blocks_scatter(1, sp);
+  if (sp) s->items = kItems;  // a run-time species is built for 4 slots per thread
+  s->grid_count = grid_blocks_count(1, sp, s->items);
+  s->grid_scatter = grid_blocks_scatter(1, sp, s->items);
   drop_day_graph(s);  // captured with the other kernels
   return SAMPO_OK;
 }
@@ -901,8 +904,8 @@ extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
   if (sms <= 0) sms = 1;
-  const uint32_t max_c = (uint32_t)(grid_blocks_count(1, s->species) / sms);
-  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(1, s->species) / sms);
+  const uint32_t max_c = (uint32_t)(grid_blocks_count(1, s->species, s->items) / sms);
+  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(1, s->species, s->items) / sms);
   if (count_ctas_per_sm < 1 || count_ctas_per_sm > max_c || scatter_ctas_per_sm < 1 || scatter_ctas_per_sm > max_s)
     return fail(s, SAMPO_ERR_ARG, "CTAs per SM outside 1.." + std::to_string(max_c) + " (count) / 1.." + std::to_string(max_s) +
                                       " (update/scatter)");
@@ -912,6 +915,27 @@ extern "C" int sampo_set_grids(sampo_sim* s, uint32_t count_ctas_per_sm, uint32_
     s->grid_scatter = gs;
     drop_day_graph(s);  // captured with the old grids
   }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_set_items_per_thread(sampo_sim* s, uint32_t items) {
+  if (!s) return SAMPO_ERR_ARG;
+  SETTLE(s);
+  if (items != 2 && items != 4) return fail(s, SAMPO_ERR_ARG, "items per thread must be 2 or 4");
+  if (s->species && items != (uint32_t)kItems) return fail(s, SAMPO_ERR_ARG, "a run-time species runs 4 items per thread");
+  cudaSetDevice(s->device);
+  if ((int)items != s->items) {
+    s->items = (int)items;
+    s->grid_count = grid_blocks_count(1, s->species, s->items);
+    s->grid_scatter = grid_blocks_scatter(1, s->species, s->items);
+    drop_day_graph(s);
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_items_per_thread(sampo_sim* s, uint32_t* items) {
+  if (!s || !items) return SAMPO_ERR_ARG;
+  *items = (uint32_t)s->items;
   return SAMPO_OK;
 }
 

@@ -33,8 +33,8 @@ struct RepLayout {
     col4 = align256(capacity * 4 + 16);
     col1 = align256(capacity + 16);
     pool = 9 * col4 + col1;
-    max_tiles = (uint32_t)((capacity + kTile - 1) / kTile);
-    tiles = align256((size_t)max_tiles * kTileArrayWords * 4);
+    max_tiles = (uint32_t)((capacity + kTileMin - 1) / kTileMin);  // room for the smaller tile's count
+    tiles = align256(tile_array_words(max_tiles) * 4);
     T = align256((size_t)ring * sizeof(float));
     env = align256((size_t)ring * sizeof(sampo_environment));
     seeds = align256((size_t)ring * 4 * sizeof(sampo_seeds));
@@ -76,6 +76,7 @@ struct sampo_batch {
   std::vector<Replicate> reps;
   std::vector<uint32_t> wt_staging;
   int grid_count = 0, grid_scatter = 0;
+  int items = kItems;                // slots per thread of the count and update/scatter passes (2 or 4)
   cudaGraphExec_t day_graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
@@ -289,7 +290,7 @@ extern "C" int sampo_batch_add(sampo_batch* b, const sampo_replicate_config* rc,
   r.T_host.assign(b->ring, 0.0f);
   RepParams& rp = r.rp;
   rp = carve(L, mem, b->sims_dev + i, b->ring);
-  BCK(cudaMemsetAsync(rp.tilePre, 0, (size_t)L.max_tiles * kTileArrayWords * 4, b->stream), "tile arrays");
+  BCK(cudaMemsetAsync(rp.tilePre, 0, tile_array_words(L.max_tiles) * 4, b->stream), "tile arrays");
   SimDev h = initial_sim_state((uint32_t)rc->capacity, rc->carrying_capacity);
   h.stop_step = rc->stop_step;
   const int st = upload_slot(b, i, h);
@@ -390,7 +391,7 @@ extern "C" int sampo_batch_init_population(sampo_batch* b, uint32_t slot, uint32
   h.stop_step = r->stop_step;
   const int st = upload_slot(b, slot, h);
   if (st) return st;
-  BCK(cudaMemsetAsync(r->rp.tilePre, 0, (size_t)r->rp.maxTiles * kTileArrayWords * 4, b->stream), "tile arrays");
+  BCK(cudaMemsetAsync(r->rp.tilePre, 0, tile_array_words(r->rp.maxTiles) * 4, b->stream), "tile arrays");
   BCK(cudaMemcpyAsync(b->init_seeds_dev + (size_t)slot * 4, init_seeds, 4 * sizeof(sampo_seeds), cudaMemcpyHostToDevice, b->stream),
       "seeds");
   const KParams p = slot_params(b, slot);
@@ -492,7 +493,7 @@ extern "C" int sampo_batch_checkpoint_load(sampo_batch* b, uint32_t slot, const 
   }
   const int st = upload_slot(b, slot, h);
   if (st) return st;
-  BCK(cudaMemsetAsync(r->rp.tilePre, 0, (size_t)r->rp.maxTiles * kTileArrayWords * 4, b->stream), "tile arrays");
+  BCK(cudaMemsetAsync(r->rp.tilePre, 0, tile_array_words(r->rp.maxTiles) * 4, b->stream), "tile arrays");
   BCK(launch_publish_start(slot_params(b, slot), b->stream), "checkpoint statistics");
   SimDev back;
   BCK(cudaMemcpyAsync(&back, b->sims_dev + slot, sizeof(SimDev), cudaMemcpyDeviceToHost, b->stream), "state");
@@ -520,8 +521,8 @@ extern "C" int sampo_batch_seed_state(sampo_batch* b, uint32_t slot, sampo_rand_
 }
 
 static cudaError_t launch_batch_step(sampo_batch* b, const KParams& p) {
-  cudaError_t e = launch_count(p, b->grid_count, b->stream);
-  if (e == cudaSuccess) e = launch_scatter(p, b->grid_scatter, b->stream);
+  cudaError_t e = launch_count(p, b->grid_count, b->stream, b->items);
+  if (e == cudaSuccess) e = launch_scatter(p, b->grid_scatter, b->stream, b->items);
   if (e == cudaSuccess) e = launch_publish(p, PUB_AFTER_STEP, b->stream);
   return e;
 }
@@ -599,14 +600,15 @@ extern "C" int sampo_batch_autotune(sampo_batch* b, uint32_t* count_ctas_per_sm,
   cudaSetDevice(b->device);
   const KParams p = all_params(b);
   BCK(launch_publish(p, PUB_REFRESH, b->stream), "step constants");
-  int gc = 0, gs = 0;
-  BCK(tune_grids(p, b->stream, &gc, &gs, nullptr), "autotune");
+  int gc = 0, gs = 0, items = kItems;
+  BCK(tune_grids(p, b->stream, &gc, &gs, &items, nullptr), "autotune");
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   if (sms <= 0) sms = 1;
-  if (gc != b->grid_count || gs != b->grid_scatter) {
+  if (gc != b->grid_count || gs != b->grid_scatter || items != b->items) {
     b->grid_count = gc;
     b->grid_scatter = gs;
+    b->items = items;
     if (b->day_graph) {
       cudaGraphExecDestroy(b->day_graph);
       b->day_graph = nullptr;
@@ -623,8 +625,9 @@ extern "C" int sampo_batch_set_species(sampo_batch* b, const sampo_species* sp) 
   cudaSetDevice(b->device);
   if (b->species == sp) return SAMPO_OK;
   b->species = sp;
-  b->grid_count = grid_blocks_count(b->nslots, sp);
-  b->grid_scatter = grid_blocks_scatter(b->nslots, sp);
+  if (sp) b->items = kItems;  // a run-time species is built for 4 slots per thread
+  b->grid_count = grid_blocks_count(b->nslots, sp, b->items);
+  b->grid_scatter = grid_blocks_scatter(b->nslots, sp, b->items);
   if (b->day_graph) {
     cudaGraphExecDestroy(b->day_graph);
     b->day_graph = nullptr;
@@ -638,8 +641,8 @@ extern "C" int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm,
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   if (sms <= 0) sms = 1;
-  const uint32_t max_c = (uint32_t)(grid_blocks_count(b->nslots, b->species) / sms);
-  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(b->nslots, b->species) / sms);
+  const uint32_t max_c = (uint32_t)(grid_blocks_count(b->nslots, b->species, b->items) / sms);
+  const uint32_t max_s = (uint32_t)(grid_blocks_scatter(b->nslots, b->species, b->items) / sms);
   if (count_ctas_per_sm < 1 || count_ctas_per_sm > max_c || scatter_ctas_per_sm < 1 || scatter_ctas_per_sm > max_s)
     return bfail(b, SAMPO_ERR_ARG, "CTAs per SM outside 1.." + std::to_string(max_c) + " (count) / 1.." +
                                        std::to_string(max_s) + " (update/scatter)");
@@ -652,6 +655,29 @@ extern "C" int sampo_batch_set_grids(sampo_batch* b, uint32_t count_ctas_per_sm,
       b->day_graph = nullptr;
     }
   }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_set_items_per_thread(sampo_batch* b, uint32_t items) {
+  if (!b) return SAMPO_ERR_ARG;
+  if (items != 2 && items != 4) return bfail(b, SAMPO_ERR_ARG, "items per thread must be 2 or 4");
+  if (b->species && items != (uint32_t)kItems) return bfail(b, SAMPO_ERR_ARG, "a run-time species runs 4 items per thread");
+  cudaSetDevice(b->device);
+  if ((int)items != b->items) {
+    b->items = (int)items;
+    b->grid_count = grid_blocks_count(b->nslots, b->species, b->items);
+    b->grid_scatter = grid_blocks_scatter(b->nslots, b->species, b->items);
+    if (b->day_graph) {
+      cudaGraphExecDestroy(b->day_graph);
+      b->day_graph = nullptr;
+    }
+  }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_items_per_thread(sampo_batch* b, uint32_t* items) {
+  if (!b || !items) return SAMPO_ERR_ARG;
+  *items = (uint32_t)b->items;
   return SAMPO_OK;
 }
 
@@ -721,7 +747,7 @@ extern "C" int sampo_batch_grow(sampo_batch* b, uint32_t slot, uint64_t capacity
   BCK(cudaMemcpyAsync((void*)rp.T, old.T, L.T + L.env + L.seeds + L.wt + L.rows, cudaMemcpyDeviceToDevice, b->stream),
       "grow rings");
   // fresh look-back arrays: zero epochs never match the running step's
-  BCK(cudaMemsetAsync(rp.tilePre, 0, (size_t)L.max_tiles * kTileArrayWords * 4, b->stream), "tile arrays");
+  BCK(cudaMemsetAsync(rp.tilePre, 0, tile_array_words(L.max_tiles) * 4, b->stream), "tile arrays");
   h.capacity = (uint32_t)capacity;
   h.cur = 0;
   h.error &= ~SAMPO_DEV_ERR_CAPACITY;

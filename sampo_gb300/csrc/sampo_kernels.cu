@@ -13,6 +13,10 @@ namespace sampo {
 // attribute applies to the device that is current when it is set, so every
 // device the library runs on gets its own). Devices beyond kMaxDevices are
 // set up on every call under a mutex.
+// The built-in count and update/scatter passes for `items` slots per thread.
+static const void* count_fn(int items) { return items == 2 ? (const void*)k_count<2> : (const void*)k_count<4>; }
+static const void* scatter_fn(int items) { return items == 2 ? (const void*)k_scatter<2> : (const void*)k_scatter<4>; }
+
 namespace {
 constexpr int kMaxDevices = 64;
 struct DeviceSetup {
@@ -25,8 +29,11 @@ std::mutex g_setup_mu;
 int setup_current_device(int dev) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kCountSmem + plan_bytes(kMaxRep)));
-  cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kScatterSmem + plan_bytes(kMaxRep)));
+  for (int items : {2, 4}) {
+    cudaFuncSetAttribute(count_fn(items), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(count_smem(items) + plan_bytes(kMaxRep)));
+    cudaFuncSetAttribute(scatter_fn(items), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(scatter_smem(items) + plan_bytes(kMaxRep)));
+  }
   return sms > 0 ? sms : 1;
 }
 }  // namespace
@@ -47,21 +54,21 @@ static void set_smem_attrs() { (void)sm_count(); }
 size_t count_smem_max() { return kCountSmem + plan_bytes(kMaxRep); }
 size_t scatter_smem_max() { return kScatterSmem + plan_bytes(kMaxRep); }
 
-// Resident CTAs per SM of a persistent kernel, built in or of p.ks.
-static int occupancy(const void* ks, int kid, int threads, size_t smem) {
+// Resident CTAs per SM of a persistent kernel, built in (for `items` slots
+// per thread) or of p.ks (4 slots per thread).
+static int occupancy(const void* ks, int kid, int items, int threads, size_t smem) {
   if (ks) return species_occupancy(ks, kid, threads, smem);
   set_smem_attrs();
   int per = 0;
-  if (kid == KID_COUNT) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_count, threads, smem);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scatter, threads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kid == KID_COUNT ? count_fn(items) : scatter_fn(items), threads, smem);
   return per;
 }
-int grid_blocks_count(uint32_t nrep, const void* ks) {
-  const int per = occupancy(ks, KID_COUNT, kBlock, kCountSmem + plan_bytes(nrep));
+int grid_blocks_count(uint32_t nrep, const void* ks, int items) {
+  const int per = occupancy(ks, KID_COUNT, items, kBlock, count_smem(items) + plan_bytes(nrep));
   return sm_count() * (per > 0 ? per : 1);
 }
-int grid_blocks_scatter(uint32_t nrep, const void* ks) {
-  const int per = occupancy(ks, KID_SCATTER, kScatterThreads, kScatterSmem + plan_bytes(nrep));
+int grid_blocks_scatter(uint32_t nrep, const void* ks, int items) {
+  const int per = occupancy(ks, KID_SCATTER, items, kScatterThreads, scatter_smem(items) + plan_bytes(nrep));
   return sm_count() * (per > 0 ? per : 1);
 }
 
@@ -73,15 +80,17 @@ static cudaError_t launch(const KParams& p, int kid, const void* fn, dim3 grid, 
   return cudaLaunchKernel(fn, grid, block, args, smem, st);
 }
 
-cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st) {
+cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st, int items) {
   KParams q = p;
   void* args[] = {&q};
-  return launch(p, KID_COUNT, (const void*)k_count, grid, kBlock, kCountSmem + plan_bytes(p.nrep), st, args);
+  if (p.ks) items = kItems;  // a run-time species is built for 4 slots per thread
+  return launch(p, KID_COUNT, count_fn(items), grid, kBlock, count_smem(items) + plan_bytes(p.nrep), st, args);
 }
-cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st) {
+cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st, int items) {
   KParams q = p;
   void* args[] = {&q};
-  return launch(p, KID_SCATTER, (const void*)k_scatter, grid, kScatterThreads, kScatterSmem + plan_bytes(p.nrep), st, args);
+  if (p.ks) items = kItems;
+  return launch(p, KID_SCATTER, scatter_fn(items), grid, kScatterThreads, scatter_smem(items) + plan_bytes(p.nrep), st, args);
 }
 cudaError_t launch_publish(const KParams& p, int mode, cudaStream_t st) {
   KParams q = p;
@@ -113,15 +122,15 @@ static cudaError_t launch_trial_reset(const KParams& p, cudaStream_t st) {
   void* args[] = {&q};
   return launch(p, KID_TRIAL_RESET, (const void*)k_trial_reset, (int)((p.nrep + 255) / 256), 256, 0, st, args);
 }
-cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, double* best_ms) {
-  int max_c = occupancy(p.ks, KID_COUNT, kBlock, kCountSmem + plan_bytes(p.nrep));
-  int max_s = occupancy(p.ks, KID_SCATTER, kScatterThreads, kScatterSmem + plan_bytes(p.nrep));
+// The grid tuner of one tile size: see tune_grids.
+static cudaError_t tune_grids_items(const KParams& p, cudaStream_t st, int items, cudaEvent_t* ev, int* grid_count,
+                                    int* grid_scatter, double* best_ms) {
+  int max_c = occupancy(p.ks, KID_COUNT, items, kBlock, count_smem(items) + plan_bytes(p.nrep));
+  int max_s = occupancy(p.ks, KID_SCATTER, items, kScatterThreads, scatter_smem(items) + plan_bytes(p.nrep));
   if (max_c < 1) max_c = 1;
   if (max_s < 1) max_s = 1;
   const int sms = sm_count();
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 3 && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
   // each kernel's time is taken on its own (the best count grid does not
   // depend on the scatter grid), minimum over every trial that ran it (eight
   // per pair: small pools run the kernels in tens of microseconds, where
@@ -135,9 +144,9 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
       for (int rep = (c == 1 && s == 1) ? -1 : 0; rep < 8 && e == cudaSuccess; rep++) {
         if ((e = launch_trial_reset(p, st)) != cudaSuccess) break;
         if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) break;
-        if ((e = launch_count(p, c * sms, st)) != cudaSuccess) break;
+        if ((e = launch_count(p, c * sms, st, items)) != cudaSuccess) break;
         if ((e = cudaEventRecord(ev[1], st)) != cudaSuccess) break;
-        if ((e = launch_scatter(p, s * sms, st)) != cudaSuccess) break;
+        if ((e = launch_scatter(p, s * sms, st, items)) != cudaSuccess) break;
         if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) break;
         if ((e = cudaEventSynchronize(ev[2])) != cudaSuccess) break;
         if (rep < 0) continue;
@@ -155,36 +164,64 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
   for (int s = 1; s <= max_s; s++)
     if (ts[s] < ts[bs]) bs = s;
   // the kernels run back to back in a step, where a small pool's times are
-  // mostly start-up and tail: keep the pick only if it also beats the
-  // largest grids run that way
-  if (e == cudaSuccess && (bc != max_c || bs != max_s)) {
-    double tj[2] = {1e30, 1e30};
-    const int gc[2] = {bc, max_c}, gs[2] = {bs, max_s};
-    for (int rep = 0; rep < 8 && e == cudaSuccess; rep++) {
-      for (int v = 0; v < 2 && e == cudaSuccess; v++) {
-        if ((e = launch_trial_reset(p, st)) != cudaSuccess) break;
-        if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) break;
-        if ((e = launch_count(p, gc[v] * sms, st)) != cudaSuccess) break;
-        if ((e = launch_scatter(p, gs[v] * sms, st)) != cudaSuccess) break;
-        if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) break;
-        if ((e = cudaEventSynchronize(ev[2])) != cudaSuccess) break;
-        float m = 0;
-        cudaEventElapsedTime(&m, ev[0], ev[2]);
-        if (m < tj[v]) tj[v] = m;
-      }
+  // mostly start-up and tail: the pick and the largest grids, run that way
+  double tj[2] = {1e30, 1e30};
+  const int gc[2] = {bc, max_c}, gs[2] = {bs, max_s};
+  for (int rep = 0; rep < 8 && e == cudaSuccess; rep++) {
+    for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+      if (v == 1 && bc == max_c && bs == max_s) break;
+      if ((e = launch_trial_reset(p, st)) != cudaSuccess) break;
+      if ((e = cudaEventRecord(ev[0], st)) != cudaSuccess) break;
+      if ((e = launch_count(p, gc[v] * sms, st, items)) != cudaSuccess) break;
+      if ((e = launch_scatter(p, gs[v] * sms, st, items)) != cudaSuccess) break;
+      if ((e = cudaEventRecord(ev[2], st)) != cudaSuccess) break;
+      if ((e = cudaEventSynchronize(ev[2])) != cudaSuccess) break;
+      float m = 0;
+      cudaEventElapsedTime(&m, ev[0], ev[2]);
+      if (m < tj[v]) tj[v] = m;
     }
+  }
+  if (bc != max_c || bs != max_s) {
     if (tj[1] <= tj[0]) {
       bc = max_c;
       bs = max_s;
+      tj[0] = tj[1];
+    }
+  }
+  *grid_count = bc * sms;
+  *grid_scatter = bs * sms;
+  *best_ms = tj[0];
+  return e;
+}
+
+cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, int* items, double* best_ms) {
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3 && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
+  // tile sizes: 1024-slot tiles (4 slots per thread) and, for the built-in
+  // species, 512-slot tiles; the step as a whole decides
+  double best = 1e30;
+  int bi = kItems, bgc = 0, bgs = 0;
+  for (int it : {4, 2}) {
+    if (e != cudaSuccess || (it != kItems && p.ks)) break;
+    int gc = 0, gs = 0;
+    double ms = 1e30;
+    e = tune_grids_items(p, st, it, ev, &gc, &gs, &ms);
+    if (e == cudaSuccess && ms < best) {
+      best = ms;
+      bi = it;
+      bgc = gc;
+      bgs = gs;
     }
   }
   if (e == cudaSuccess) e = launch_trial_reset(p, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   for (int i = 0; i < 3; i++)
     if (ev[i]) cudaEventDestroy(ev[i]);
-  *grid_count = bc * sms;
-  *grid_scatter = bs * sms;
-  if (best_ms) *best_ms = tc[bc] + ts[bs];
+  *grid_count = bgc;
+  *grid_scatter = bgs;
+  *items = bi;
+  if (best_ms) *best_ms = best;
   return e;
 }
 int grid_blocks_small() {

@@ -17,8 +17,9 @@
 namespace sampo {
 
 constexpr int kBlock = 256;                 // threads per CTA
-constexpr int kItems = 4;                   // slots per thread per tile (striped by kBlock)
+constexpr int kItems = 4;                   // slots per thread per tile (striped by kBlock); 2 or 4 in the count and update/scatter passes
 constexpr int kTile = kBlock * kItems;      // slots per tile
+constexpr int kTileMin = kBlock * 2;        // the smallest tile the passes run with (the tile arrays have room for its count)
 constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kMaxRep = 1024;          // replicates per batch
 
@@ -76,15 +77,28 @@ struct BatchDev {
 constexpr uint32_t kChunks = kItems * kWarps;
 constexpr uint32_t kPreEntryWords = 5;
 constexpr uint32_t kPreWords = ((kChunks + 1) * kPreEntryWords + 3) / 4 * 4;  // whole 16-byte units
-// Words per tile of a pool's tile arrays: prefix table, aggregates (8),
-// inclusive prefixes with their epochs (8 x 64 bits).
-constexpr uint32_t kTileArrayWords = kPreWords + 8 + 16;
+constexpr uint32_t kPreWordsMax = kPreWords;  // prefix-table words of one tile at I = 4, the largest
+constexpr uint32_t kPreWordsMin = ((2 * kWarps + 1) * kPreEntryWords + 3) / 4 * 4;  // at I = 2
+// Words of a pool's tile arrays for max_tiles tiles of kTileMin slots: the
+// prefix tables (max_tiles of the smaller tile's tables, plus one larger
+// table: ceil(C / kTile) tables of kPreWordsMax words fit in that too),
+// aggregates (8 per tile) and inclusive prefixes with their epochs (8 x 64 bits
+// per tile).
+constexpr uint32_t kPreRegionPad = kPreWordsMax;
+__host__ __device__ constexpr size_t tile_pre_words(uint32_t max_tiles) {
+  return (size_t)max_tiles * kPreWordsMin + kPreRegionPad;
+}
+__host__ __device__ constexpr size_t tile_array_words(uint32_t max_tiles) {
+  return tile_pre_words(max_tiles) + (size_t)max_tiles * (8 + 16);
+}
+static_assert(kPreWordsMin % 4 == 0 && kPreRegionPad % 4 == 0, "the inclusive prefixes start on a 16-byte boundary");
+static_assert(2 * kPreWordsMin >= kPreWordsMax, "two small tables hold one large table");
 
 // Everything the kernels need of one replicate.
 struct RepParams {
   SimDev* sim;
   DevPool pool[2];
-  uint32_t* tilePre;          // [maxTiles][kPreWords] in-tile prefix tables (count pass)
+  uint32_t* tilePre;          // [tiles][pre_words(I)] in-tile prefix tables (count pass), tile_pre_words(maxTiles) words
   uint32_t* tileAgg;          // [maxTiles][8] per-tile survivor counts (count pass)
   unsigned long long* tileIncl;  // [maxTiles][8] inclusive prefixes | epoch << 32 (scatter pass)
   const float* T;             // [ring] temperature per step
@@ -131,13 +145,13 @@ inline void fill_constant_tables(ModelConst& h) {
 }
 
 // Initial device state of a simulation (before its pool is published).
-// The tile arrays of a pool of max_tiles tiles at base (16-byte aligned, for
-// the bulk copies of the prefix tables): [max_tiles][kPreWords] prefix tables,
-// then aggregates and inclusive prefixes.
+// The tile arrays of a pool of max_tiles tiles of kTileMin slots at base
+// (16-byte aligned, for the bulk copies of the prefix tables): the prefix
+// tables (tile_pre_words words, indexed by the running tile size's table
+// length), then aggregates and inclusive prefixes.
 inline void set_tile_arrays(RepParams& r, uint32_t* base, uint32_t max_tiles) {
-  static_assert(kPreWords % 4 == 0, "the inclusive prefixes start on a 16-byte boundary");
   r.tilePre = base;
-  r.tileAgg = base + (size_t)max_tiles * kPreWords;
+  r.tileAgg = base + tile_pre_words(max_tiles);
   r.tileIncl = reinterpret_cast<unsigned long long*>(r.tileAgg + (size_t)max_tiles * 8);
   r.maxTiles = max_tiles;
 }
@@ -174,8 +188,8 @@ inline SimDev initial_sim_state(uint32_t capacity, float cc) {
 // p; init, pool statistics and the histogram take p.reps[0] only. They launch
 // the built-in kernels, or p.ks's when a species was compiled at run time.
 // persistent grid sizes (CTAs resident on all SMs) for batches of nrep replicates
-int grid_blocks_count(uint32_t nrep, const void* ks = nullptr);
-int grid_blocks_scatter(uint32_t nrep, const void* ks = nullptr);
+int grid_blocks_count(uint32_t nrep, const void* ks = nullptr, int items = kItems);
+int grid_blocks_scatter(uint32_t nrep, const void* ks = nullptr, int items = kItems);
 // The kernels of a run-time species (sampo_species.cu): launch one, and its
 // resident CTAs per SM.
 enum : int { KID_COUNT, KID_SCATTER, KID_PUBLISH, KID_INIT_EGGS, KID_POOL_STATS, KID_HISTOGRAM, KID_TRIAL_RESET, KID_N };
@@ -184,8 +198,10 @@ int species_occupancy(const void* ks, int kid, int threads, size_t smem);
 // dynamic shared memory the persistent kernels may request
 size_t count_smem_max();
 size_t scatter_smem_max();
-cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st);
-cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st);
+// (the built-in passes for `items` = 2 or 4 slots per thread; a run-time
+// species is built for 4)
+cudaError_t launch_count(const KParams& p, int grid, cudaStream_t st, int items = kItems);
+cudaError_t launch_scatter(const KParams& p, int grid, cudaStream_t st, int items = kItems);
 // k_publish over every replicate of p (modes PUB_*, above).
 cudaError_t launch_publish(const KParams& p, int mode, cudaStream_t st);
 cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo_seeds* seeds_dev,
@@ -200,11 +216,12 @@ cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out,
 // `grid` CTAs.
 int grid_blocks_small();
 cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st);
-// Times count + scatter of the coming step at every (count, scatter) number
-// of CTAs per SM the occupancy allows and returns the fastest grids. The
-// trials leave the simulations' course unchanged (k_trial_reset); the coming
-// step's constants must be current (PUB_REFRESH) before the call.
-cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, double* best_ms);
+// Times count + scatter of the coming step for each tile size (4 and, for
+// the built-in species, 2 slots per thread) at every (count, scatter) number
+// of CTAs per SM the occupancy allows, and returns the fastest tile size and
+// grids. The trials leave the simulations' course unchanged (k_trial_reset);
+// the coming step's constants must be current (PUB_REFRESH) before the call.
+cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* grid_scatter, int* items, double* best_ms);
 
 #endif  // __CUDACC_RTC__
 

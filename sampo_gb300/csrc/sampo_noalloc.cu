@@ -19,7 +19,7 @@ using namespace sampo;
 
 namespace {
 
-constexpr uint32_t kMaxTiles = SAMPO_NOALLOC_MAX_SLOTS / kTile;
+constexpr uint32_t kMaxTiles = SAMPO_NOALLOC_MAX_SLOTS / kTileMin;  // tile arrays in kTileMin-slot tiles
 
 // One step of inputs (ring of two, as the kernels index step % ring).
 struct InputBlock {
@@ -30,7 +30,7 @@ struct InputBlock {
 };
 
 struct Scratch {
-  __align__(16) uint32_t tiles[kMaxTiles * kTileArrayWords];  // prefix tables | counts | inclusive prefixes
+  __align__(16) uint32_t tiles[tile_array_words(kMaxTiles)];  // prefix tables | counts | inclusive prefixes
   SimDev sim;
   RepParams rep;
   BatchDev bat;

@@ -115,7 +115,7 @@ void open_driver(Driver& d) {
 }
 
 // the kernels of one compiled species, in KID_* order
-const char* const kKernelNames[KID_N] = {"&sampo::k_count",      "&sampo::k_scatter",   "&sampo::k_publish",
+const char* const kKernelNames[KID_N] = {"&sampo::k_count<4>",   "&sampo::k_scatter<4>", "&sampo::k_publish",
                                          "&sampo::k_init_eggs",  "&sampo::k_pool_stats", "&sampo::k_histogram",
                                          "&sampo::k_trial_reset"};
 

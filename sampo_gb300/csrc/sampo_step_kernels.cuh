@@ -49,6 +49,25 @@ constexpr uint32_t kCountStage = 5 * kColBytes + kTile;      // age, his, delay,
 constexpr uint32_t kPreOff = 9 * kColBytes + kTile;          // the nine 4-byte columns and the flags,
 constexpr uint32_t kScatterStage = kPreOff + kPreWords * 4;   // then the tile's prefix table
 static_assert(kPreOff % 16 == 0 && kScatterStage % 16 == 0, "bulk copies land on 16-byte boundaries");
+
+// The count and update/scatter passes are built for I slots per thread
+// (tiles of 256 * I slots: I = 2 or 4, picked per workload by the
+// autotuner). Inside them these local constants stand for the tile sizes
+// above, which are those of I = 4.
+#define SAMPO_TILE_CONSTANTS(I)                                                         \
+  constexpr int kItems = (I);                                                         \
+  constexpr int kTile = kBlock * (I);                                                 \
+  constexpr uint32_t kChunks = (uint32_t)(I) * kWarps;                                \
+  constexpr uint32_t kPreWords = ((kChunks + 1) * kPreEntryWords + 3) / 4 * 4;        \
+  constexpr uint32_t kColBytes = (uint32_t)kTile * 4;                                 \
+  constexpr uint32_t kCountStage = 5 * kColBytes + kTile;                             \
+  constexpr uint32_t kPreOff = 9 * kColBytes + kTile;                                 \
+  constexpr uint32_t kScatterStage = kPreOff + kPreWords * 4;                         \
+  constexpr size_t kCountSmem = 2 * (size_t)kCountStage;                              \
+  constexpr size_t kScatterSmem = 2 * (size_t)kScatterStage;                          \
+  static_assert(kPreOff % 16 == 0 && kScatterStage % 16 == 0 && kChunks <= 32 && kPreWords <= kPreWordsMax, \
+                "bulk copies land on 16-byte boundaries; one chunk per lane; tables fit the tile arrays"); \
+  (void)kItems; (void)kChunks; (void)kCountSmem; (void)kScatterSmem
 constexpr uint32_t kWaitLimit = 1u << 22;                    // bounded mbarrier waits
 
 // ---------------- memory-model and TMA helpers ----------------
@@ -299,8 +318,10 @@ __device__ __forceinline__ uint32_t count_cols(int rg, bool larvicide) {
   }
 }
 
+template <int I>
 __device__ void issue_count_tile(const DevPool& src, uint8_t* st, uint64_t* bar, const sampo_population& pop,
                                  uint32_t lo, uint32_t n, bool larvicide) {
+  SAMPO_TILE_CONSTANTS(I);
   uint32_t m = 0;
   for (int k = 0; k < 8; k++)
     if (pop.r[k].end > pop.r[k].start && pop.r[k].start < lo + n && pop.r[k].end > lo) m |= count_cols(k, larvicide);
@@ -336,6 +357,14 @@ struct alignas(16) CountStage {
 // simulation pays 8 bytes for it.
 constexpr size_t kCountSmem = 2 * kCountStage;
 constexpr size_t kScatterSmem = 2 * kScatterStage;
+// the same for I slots per thread (the stages scale with the tile; the
+// prefix table has 8 I + 1 entries)
+__host__ __device__ constexpr uint32_t pre_words(int items) { return ((items * kWarps + 1) * kPreEntryWords + 3) / 4 * 4; }
+__host__ __device__ constexpr size_t count_smem(int items) { return 2 * (size_t)(5 * kBlock * items * 4 + kBlock * items); }
+__host__ __device__ constexpr size_t scatter_smem(int items) {
+  return 2 * (size_t)(9 * kBlock * items * 4 + kBlock * items + pre_words(items) * 4);
+}
+static_assert(count_smem(kItems) == kCountSmem && scatter_smem(kItems) == kScatterSmem, "one definition");
 __host__ __device__ constexpr size_t plan_bytes(uint32_t nrep) { return ((size_t)(nrep + 1) * 4 + 15) & ~(size_t)15; }
 constexpr uint32_t kNoRep = 0xffffffffu;
 
@@ -344,9 +373,10 @@ constexpr uint32_t kNoRep = 0xffffffffu;
 // survivors by next state into ent (8-bit fields, states 0-3 | 4-7).
 // RG >= 0: every slot of the tile lies in range RG, so only that state's
 // code is compiled in; RG = -1: a tile that spans ranges.
-template <int RG>
+template <int I, int RG>
 __device__ __forceinline__ void count_items(const CountStage& cs, const uint8_t* st, const KillConst& mc, uint32_t lo,
                                             uint32_t end, int tid, uint2* ent, Acc& acc, uint32_t& devoob) {
+  SAMPO_TILE_CONSTANTS(I);
   const int lane = tid & 31, warp = tid >> 5;
   const StepCtx& c = cs.c;
   const bool larvicide = c.env.larvacideValue > 0.0f;
@@ -400,7 +430,9 @@ __device__ __forceinline__ void count_items(const CountStage& cs, const uint8_t*
 // tile's totals to the stage's counts, claims the next ticket and starts
 // that tile's copies into the stage it has just emptied. A warp's stall is
 // then the wait for a tile's data, never the wait for the slowest warp.
+template <int I>
 __global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
+  SAMPO_TILE_CONSTANTS(I);
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ CountStage s_cs[2];
   __shared__ KillConst s_mc;
@@ -476,7 +508,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
         const int u = range_of(cs.pop, lo);
         cs.urg = (u >= 0 && lo + n <= cs.pop.r[u].end) ? u : -1;
         fence_proxy_async();  // the stage was last read through the generic proxy
-        issue_count_tile(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, n, cs.larv != 0);
+        issue_count_tile<I>(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, n, cs.larv != 0);
       }
     }
   };
@@ -530,15 +562,15 @@ __global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
     const uint32_t end = cs.end, lo = cs.lt * kTile;
     uint2* ent = s_ent[sidx];
     switch (cs.urg) {  // CTA-uniform: a tile inside one range runs that state's code only
-      case EGG: count_items<EGG>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case LARVA: count_items<LARVA>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case PUPA: count_items<PUPA>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case IMMATURE: count_items<IMMATURE>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case MATESEEKING: count_items<MATESEEKING>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case BMS: count_items<BMS>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case BMD: count_items<BMD>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      case GRAVID: count_items<GRAVID>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
-      default: count_items<-1>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case EGG: count_items<I, EGG>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case LARVA: count_items<I, LARVA>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case PUPA: count_items<I, PUPA>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case IMMATURE: count_items<I, IMMATURE>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case MATESEEKING: count_items<I, MATESEEKING>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case BMS: count_items<I, BMS>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case BMD: count_items<I, BMD>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      case GRAVID: count_items<I, GRAVID>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
+      default: count_items<I, -1>(cs, st, s_mc, lo, end, tid, ent, acc, devoob); break;
     }
     // this warp is done with the stage: the last warp out does the tile's bookkeeping
     uint32_t last = 0;
@@ -796,7 +828,9 @@ __global__ void __launch_bounds__(kPublishThreads) k_publish(KParams p, int mode
 // ------------------------------------------------------------------------
 // Update + scatter pass
 // ------------------------------------------------------------------------
+template <int I>
 __device__ void issue_scatter_tile(const DevPool& src, const uint32_t* pre, uint8_t* st, uint64_t* bar, uint32_t lo, uint32_t n) {
+  SAMPO_TILE_CONSTANTS(I);
   const uint32_t b4 = (n * 4 + 15) & ~15u, b1 = (n + 15) & ~15u;
   mbar_arrive_tx(bar, 9 * b4 + b1 + kPreWords * 4);
   bulk_load(st + kPreOff, pre, kPreWords * 4, bar);
@@ -880,7 +914,8 @@ __device__ void tile_lookback(const LookbackArrays& rp, uint32_t t, uint32_t epo
 
 constexpr int kScatterThreads = kBlock + 32;  // eight consumer warps and one producer warp
 static_assert(kChunks <= 32, "one (round, warp) chunk per lane");
-constexpr int kScatterMinBlocks = kItems >= 4 ? 2 : 3;  // resident CTAs per SM the registers are sized for
+// resident CTAs per SM the registers of the update/scatter pass are sized for
+__host__ __device__ constexpr int scatter_min_blocks(int items) { return items >= 4 ? 2 : 3; }
 enum : uint32_t { TK_OLD = 0, TK_EGG = 1, TK_END = 2 };
 
 // What the producer warp hands the consumers with a tile. The replicate's
@@ -916,10 +951,11 @@ struct BmEntry { uint32_t d, gid, batches, kind; };
 // next state (8: none) | female << 4 | owed draw << 5. RG >= 0: every slot
 // of the tile lies in range RG, so only that state's code is compiled in;
 // RG = -1: a tile that spans ranges.
-template <int RG>
+template <int I, int RG>
 __device__ __forceinline__ void scatter_phase_a(const ScatterStage& si, const uint8_t* st, const KillConst& kc, int tid,
-                                                Rec (&a)[kItems], uint32_t (&nb)[kItems], uint32_t (&dk)[kItems], Acc& acc,
+                                                Rec (&a)[I], uint32_t (&nb)[I], uint32_t (&dk)[I], Acc& acc,
                                                 uint32_t& tilebad) {
+  SAMPO_TILE_CONSTANTS(I);
   const int warp = tid >> 5;
   const float* c_age = (const float*)(st + 0 * kColBytes);
   const float* c_his = (const float*)(st + 1 * kColBytes);
@@ -988,7 +1024,9 @@ __device__ __forceinline__ void scatter_phase_a(const ScatterStage& si, const ui
 // has read its inputs, then writes every survivor straight to its slot in the
 // next buffer: the survivors of one next state are contiguous within a warp,
 // so the stores coalesce.
-__global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(KParams p) {
+template <int I>
+__global__ void __launch_bounds__(kScatterThreads, scatter_min_blocks(I)) k_scatter(KParams p) {
+  SAMPO_TILE_CONSTANTS(I);
   extern __shared__ __align__(128) uint8_t dsm[];
   __shared__ ScatterStage s_si[kDescSlots];
   __shared__ ModelConst s_mc;
@@ -1107,7 +1145,7 @@ __global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(
       if (lane == 0) {
         if (si.kind == TK_OLD) {
           fence_proxy_async();  // the stage was last read through the generic proxy
-          issue_scatter_tile(si.src, si.pre + (size_t)(si.lo / kTile) * kPreWords, dsm + s * kScatterStage, &full[s], si.lo,
+          issue_scatter_tile<I>(si.src, si.pre + (size_t)(si.lo / kTile) * kPreWords, dsm + s * kScatterStage, &full[s], si.lo,
                              min((uint32_t)kTile, si.end - si.lo));
         } else {
           mbar_arrive(&full[s]);
@@ -1194,15 +1232,15 @@ __global__ void __launch_bounds__(kScatterThreads, kScatterMinBlocks) k_scatter(
       uint32_t dk[kItems];
       if (kind == TK_OLD) {
         switch (si.urg) {  // CTA-uniform: a tile inside one range runs that state's code only
-          case EGG: scatter_phase_a<EGG>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case LARVA: scatter_phase_a<LARVA>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case PUPA: scatter_phase_a<PUPA>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case IMMATURE: scatter_phase_a<IMMATURE>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case MATESEEKING: scatter_phase_a<MATESEEKING>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case BMS: scatter_phase_a<BMS>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case BMD: scatter_phase_a<BMD>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          case GRAVID: scatter_phase_a<GRAVID>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
-          default: scatter_phase_a<-1>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case EGG: scatter_phase_a<I, EGG>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case LARVA: scatter_phase_a<I, LARVA>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case PUPA: scatter_phase_a<I, PUPA>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case IMMATURE: scatter_phase_a<I, IMMATURE>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case MATESEEKING: scatter_phase_a<I, MATESEEKING>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case BMS: scatter_phase_a<I, BMS>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case BMD: scatter_phase_a<I, BMD>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          case GRAVID: scatter_phase_a<I, GRAVID>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
+          default: scatter_phase_a<I, -1>(si, st, mc.kill, tid, a, nb, dk, acc, tilebad); break;
         }
       }
       if (kind != TK_END) mbar_arrive(&empty[s]);  // this thread is done with the stage's inputs

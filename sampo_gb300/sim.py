@@ -205,6 +205,15 @@ class Simulation:
         """Fix the grid sizes (CTAs per SM of the two passes) without tuning."""
         self._check(self.lib.sampo_set_grids(self.h, count_ctas_per_sm, scatter_ctas_per_sm))
 
+    def set_items_per_thread(self, items: int):
+        """Slots per thread of the count and update/scatter passes (2 or 4)."""
+        self._check(self.lib.sampo_set_items_per_thread(self.h, items))
+
+    def items_per_thread(self) -> int:
+        v = C.c_uint32()
+        self._check(self.lib.sampo_items_per_thread(self.h, C.byref(v)))
+        return v.value
+
     def set_small_step(self, max_tiles: int | None = None):
         """Pools of at most max_tiles 1024-slot tiles take the one-launch
         step in day graphs (None: one tile per CTA of its largest grid; 0: never)."""

@@ -1,6 +1,7 @@
-"""The grid autotuner times the step kernels on the coming step and keeps the
-fastest grid sizes; a run tuned half-way must equal the untuned run bit for bit
-(plain and batched)."""
+"""The autotuner times the step kernels on the coming step and keeps the
+fastest tile size (slots per thread) and grid sizes; a run tuned half-way must
+equal the untuned run bit for bit (plain and batched), and so must runs with
+either tile size."""
 import numpy as np
 import pytest
 
@@ -79,3 +80,59 @@ def test_set_grids_pins_the_choice(gpu_ready, tmp_path):
             with pytest.raises(SampoError):
                 sim.set_grids(1, 64)
     assert out[1] == out[0] and out[2] == out[0]
+
+
+@pytest.mark.gpu
+def test_tile_size_does_not_change_results(gpu_ready, oracle_mod):
+    """512- and 1024-slot tiles (2 or 4 slots per thread) through the
+    three-kernel step: the same rows and pools; the autotuner's pick is one of
+    them and keeps the run unchanged."""
+    from sampo_gb300 import inputs
+    from sampo_gb300.population import make_pool
+    from sampo_gb300.sim import Simulation, seed_stream
+    n = 144
+    T = np.full(n, 27.5, np.float32)
+    env = np.zeros(n, dtype=inputs.ENV_DTYPE)
+    env["bloodmealSuccess"] = 0.25
+    env["carryingCapacity"] = 40000.0
+    ranges, arrays = make_pool((30000, 20000, 8000, 12000), T[0], seed=9)
+    _, seeds = seed_stream(9, n)
+    out = []
+    for items in (4, 2, "tuned"):
+        with Simulation(capacity=1 << 19, carrying_capacity=40000.0, max_steps=n + 1) as sim:
+            sim.set_small_step(0)  # the three-kernel step every hour
+            if items != "tuned":
+                sim.set_items_per_thread(items)
+                assert sim.items_per_thread() == items
+            sim.set_inputs(T, env)
+            sim.set_seeds(0, seeds)
+            sim.load_pool(ranges, arrays)
+            rows = [sim.run(48)]
+            if items == "tuned":
+                sim.autotune()
+                assert sim.items_per_thread() in (2, 4)
+            rows.append(sim.run(n - 48))
+            pop, pool = sim.read_pool()
+            assert sim.device_status() == 0
+        out.append((np.concatenate(rows).tobytes(), oracle_mod.pool_hash(pop["ranges"], pool)))
+    assert out[1] == out[0] and out[2] == out[0]
+
+
+@pytest.mark.gpu
+def test_batch_tile_size_does_not_change_replicates(gpu_ready):
+    from sampo_gb300.batch import Batch, admit
+    from tests.test_batch import SPECS, compare
+    for items in (2, 4):
+        with Batch(max_replicates=4, ring_steps=80) as b:
+            b.set_items_per_thread(items)
+            assert b.items_per_thread() == items
+            slots = [admit(b, s, 72) for s in SPECS[:3]]
+            b.run(72)
+            for slot, spec in zip(slots, SPECS[:3]):
+                compare(b, slot, spec, 72, f"replicate {spec.seed}, {items} slots per thread")
+
+
+def test_items_per_thread_arguments(sampo_lib):
+    """Only 2 and 4 slots per thread exist (checked without a device)."""
+    assert sampo_lib.sampo_set_items_per_thread(None, 4) == -1
+    assert sampo_lib.sampo_batch_set_items_per_thread(None, 2) == -1
