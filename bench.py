@@ -375,9 +375,11 @@ def ensemble_arm(args):
     setup_batch = time.perf_counter() - t_all
     b.run(24 * args.warmup)
     tuned = b.autotune()
+    launches0 = b.launches()
     with ClockSampler(0) as clk:
         b.run(24 * args.steps)
     dev_batch = b.last_run_ms() / 1e3
+    gpu_launches = b.launches() - launches0
     rows_b, bits_b = [], []
     for slot in slots:
         b._check(b.lib.sampo_batch_rows(b.h, slot, 0, nsteps + 1, hR.p))
@@ -436,7 +438,7 @@ def ensemble_arm(args):
         "e2e": {"value": n * days / wall_e2e, "unit": "replicate-days/s",
                 "h2d_bytes_per_step": n * 24 * (4 + 24 + 4), "d2h_bytes_per_step": n * 24 * 92,
                 "window": f"the whole batched run: setup, days 0..{days}, grid tuning, rows read back"},
-        "gpu_launches": 1 + 73 * args.steps,
+        "gpu_launches": gpu_launches,
         "clocks": clk.summary(),
     }
 
@@ -457,6 +459,7 @@ def ensemble_year_arm(args):
         t0 = time.perf_counter()
         res = srv.serve(reqs)
         wall = time.perf_counter() - t0
+    gpu_launches = srv.batch.launches()
     srv.close()
     agent_days = sum(float(live_counts(r.rows[:-1]).sum()) for r in res) / 24.0
     sample = list(range(0, n, args.plain_every))
@@ -494,6 +497,9 @@ def ensemble_year_arm(args):
         "e2e": {"value": value, "unit": "replicate-days/s", "h2d_bytes_per_step": n * 24 * (4 + 24 + 4),
                 "d2h_bytes_per_step": n * 24 * 92,
                 "note": "value is already end to end: wall clock through sampo_gb300.serve.Server, inputs up and rows down"},
+        "gpu_launches": gpu_launches,
+        "gpu_launches_counts": "step kernels (day graphs' kernel nodes + one constants refresh per run call); "
+                               "pool set-up and growth copies not counted",
         "clocks": clk.summary(),
     }
 
@@ -512,6 +518,7 @@ def served_arm(args):
         t0 = time.perf_counter()
         res = srv.serve(reqs)
         makespan = max(r.completed for r in res) - min(r.arrival for r in res)
+        launches = srv.batch.launches()
         srv.close()
         if plain is None:  # service times do not depend on the arrival rate
             plain = {p["rid"]: p for p in one_at_a_time(reqs)}
@@ -541,7 +548,7 @@ def served_arm(args):
             "bit_exact": f"{exact}/{len(res)}", "peak_resident": srv.peak_resident,
             "peak_hbm_gb": srv.peak_bytes / 1e9, "days_stepped": srv.days_run, "pool_growths": srv.grows,
             "growths_after_a_pause": srv.pauses, "growths_over_budget": srv.over_budget,
-            "days_admission_held": srv.held_days, "wall_s": time.perf_counter() - t0}
+            "days_admission_held": srv.held_days, "gpu_launches": launches, "wall_s": time.perf_counter() - t0}
     first = per_rate[str(rates[0])]
     # host traffic per request (the line's step): its inputs up at admission
     # (temperature, environment row, world time per hourly step) and its stats
@@ -557,7 +564,8 @@ def served_arm(args):
                 "per_rate": per_rate,
                 "e2e": {"value": first["sims_per_s"], "unit": "sims/s", "h2d_bytes_per_step": float(hours.mean() * (4 + 24 + 4)),
                         "d2h_bytes_per_step": float((hours.mean() + 1) * 92 + 400),
-                        "note": "value is already end to end: wall clock through sampo_gb300.serve.Server"}})
+                        "note": "value is already end to end: wall clock through sampo_gb300.serve.Server"},
+                "gpu_launches": first["gpu_launches"]})
     return out
 
 

@@ -426,6 +426,9 @@ int sampo_batch_checkpoint_save(sampo_batch* b, uint32_t slot, const char* path)
 int sampo_batch_checkpoint_load(sampo_batch* b, uint32_t slot, const char* path);
 /* Device time of the last sampo_batch_run, in milliseconds (after sync). */
 int sampo_batch_last_run_ms(sampo_batch* b, double* ms);
+/* Kernels sampo_batch_run has launched since creation (a day graph's
+ * replay counts its kernel nodes). */
+int sampo_batch_launches(sampo_batch* b, uint64_t* launches);
 
 /* Library version and build information. */
 int sampo_abi_version(void);

@@ -182,6 +182,7 @@ SIGNATURES = {
     "sampo_batch_histogram": (C.c_int, [_P, C.c_uint32, _P]),
     "sampo_batch_read_pool": (C.c_int, [_P, C.c_uint32, C.POINTER(Population), C.POINTER(PoolView)]),
     "sampo_batch_last_run_ms": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "sampo_batch_launches": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
 }
 
 _lib = None

@@ -178,6 +178,12 @@ class Batch:
         self._check(self.lib.sampo_batch_last_run_ms(self.h, C.byref(v)))
         return v.value
 
+    def launches(self) -> int:
+        """Kernels run() has launched since creation."""
+        n = C.c_uint64()
+        self._check(self.lib.sampo_batch_launches(self.h, C.byref(n)))
+        return n.value
+
 
 # ---------------------------------------------------------------------------
 # Replicate descriptions (the ensemble and served workloads)

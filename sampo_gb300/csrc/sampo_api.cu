@@ -439,16 +439,8 @@ static int build_day_graph(sampo_sim* s) {
   if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(s, e, "capture launch"); }
   if (e2 != cudaSuccess) return cuda_fail(s, e2, "end capture");
   // the launches a replay makes: the kernel nodes the capture recorded
-  size_t nn = 0;
-  e = cudaGraphGetNodes(g, nullptr, &nn);
-  std::vector<cudaGraphNode_t> nodes(nn);
-  if (e == cudaSuccess && nn) e = cudaGraphGetNodes(g, nodes.data(), &nn);
   uint32_t kernels = 0;
-  for (size_t i = 0; i < nn && e == cudaSuccess; i++) {
-    cudaGraphNodeType t;
-    e = cudaGraphNodeGetType(nodes[i], &t);
-    kernels += t == cudaGraphNodeTypeKernel ? 1u : 0u;
-  }
+  e = graph_kernel_nodes(g, &kernels);
   if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_fail(s, e, "graph nodes"); }
   s->day_graph_kernels = kernels;
   e = cudaGraphInstantiate(&s->day_graph, g, 0);

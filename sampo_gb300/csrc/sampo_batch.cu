@@ -78,6 +78,8 @@ struct sampo_batch {
   int grid_count = 0, grid_scatter = 0;
   int items = kItems;                // slots per thread of the count and update/scatter passes (2 or 4)
   cudaGraphExec_t day_graph = nullptr;
+  uint32_t day_graph_kernels = 0;    // kernel nodes of day_graph
+  uint64_t launches = 0;             // kernels sampo_batch_run launched
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool timed = false;
   std::string err;
@@ -540,6 +542,13 @@ static int build_batch_graph(sampo_batch* b) {
     return bfail(b, SAMPO_ERR_CUDA, std::string("capture launch: ") + cudaGetErrorString(e));
   }
   if (e2 != cudaSuccess) return bfail(b, SAMPO_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
+  uint32_t kernels = 0;
+  e = graph_kernel_nodes(g, &kernels);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return bfail(b, SAMPO_ERR_CUDA, std::string("graph nodes: ") + cudaGetErrorString(e));
+  }
+  b->day_graph_kernels = kernels;
   e = cudaGraphInstantiate(&b->day_graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
@@ -567,13 +576,20 @@ extern "C" int sampo_batch_run(sampo_batch* b, uint32_t nsteps, int wait) {
   const KParams p = all_params(b);
   BCK(cudaEventRecord(b->ev0, b->stream), "event");
   BCK(launch_publish(p, PUB_REFRESH, b->stream), "step constants");  // inputs may postdate the last publish
+  b->launches += 1;
   uint32_t i = 0;
   if (nsteps >= 24) {
     const int rc = build_batch_graph(b);
     if (rc) return rc;
-    for (; i + 24 <= nsteps; i += 24) BCK(cudaGraphLaunch(b->day_graph, b->stream), "day graph");
+    for (; i + 24 <= nsteps; i += 24) {
+      BCK(cudaGraphLaunch(b->day_graph, b->stream), "day graph");
+      b->launches += b->day_graph_kernels;
+    }
   }
-  for (; i < nsteps; i++) BCK(launch_batch_step(b, p), "step kernels");
+  for (; i < nsteps; i++) {
+    BCK(launch_batch_step(b, p), "step kernels");
+    b->launches += 3;
+  }
   BCK(cudaEventRecord(b->ev1, b->stream), "event");
   b->timed = true;
   for (auto& r : b->reps) {
@@ -585,6 +601,12 @@ extern "C" int sampo_batch_run(sampo_batch* b, uint32_t nsteps, int wait) {
     BCK(cudaStreamSynchronize(b->stream), "batch run");
     return refresh_mirrors(b);
   }
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_batch_launches(sampo_batch* b, uint64_t* launches) {
+  if (!b || !launches) return SAMPO_ERR_ARG;
+  *launches = b->launches;
   return SAMPO_OK;
 }
 

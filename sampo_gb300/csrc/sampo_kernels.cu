@@ -2,6 +2,7 @@
 // and the grid autotuner. The device code is in sampo_step_kernels.cuh.
 #include <cuda_runtime.h>
 #include <mutex>
+#include <vector>
 #include "sampo_step_kernels.cuh"
 #include "sampo_small_step.cuh"
 
@@ -232,6 +233,22 @@ int grid_blocks_small() {
   }
   return sm_count() * per;
 }
+
+cudaError_t graph_kernel_nodes(cudaGraph_t g, uint32_t* kernels) {
+  size_t nn = 0;
+  cudaError_t e = cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (e == cudaSuccess && nn) e = cudaGraphGetNodes(g, nodes.data(), &nn);
+  uint32_t k = 0;
+  for (size_t i = 0; i < nn && e == cudaSuccess; i++) {
+    cudaGraphNodeType t;
+    e = cudaGraphNodeGetType(nodes[i], &t);
+    k += t == cudaGraphNodeTypeKernel ? 1u : 0u;
+  }
+  *kernels = k;
+  return e;
+}
+
 cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st) {
   KParams q = p;
   void* args[] = {&q, &nsteps};

@@ -210,6 +210,8 @@ cudaError_t launch_init_eggs(const KParams& p, uint32_t n, float T0, const sampo
 cudaError_t launch_publish_start(const KParams& p, cudaStream_t st);
 cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t st);
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
+// Kernel nodes in a captured graph (the launches one replay makes).
+cudaError_t graph_kernel_nodes(cudaGraph_t g, uint32_t* kernels);
 // The one-launch steps of a single simulation (sampo_small_step.cuh): the
 // largest grid (CTAs resident on all SMs, 0 if it cannot run) and a launch
 // of `nsteps` hourly steps (a cooperative launch when `cooperative`) on

@@ -60,6 +60,8 @@ def test_batch_replicates_equal_plain_runs(gpu_ready):
         b.run(48)          # two day graphs
         b.run(24, wait=False)
         b.sync()
+        # a refresh per call, then count + update/scatter + publish per hour
+        assert b.launches() == 2 + 3 * 72
         for s, spec, st in zip(slots, SPECS, steps):
             compare(b, s, spec, st, f"replicate {spec.seed}")
 
