@@ -167,11 +167,13 @@ def gpu_arm(args, wl, rank, world, device):
     # the profiler would mislead the tuner)
     fresh()
     sim.set_small_step(None if args.small_step == "auto" else 0 if args.small_step == "off" else int(args.small_step))
+    sim.set_small_step_items(args.small_items)
     if args.ctas_per_sm:
         tuned = tuple(int(x) for x in args.ctas_per_sm.split(","))
         sim.set_grids(*tuned)
     else:
         tuned = sim.autotune()
+    items = sim.items_per_thread()
     # ---- value: device-resident inputs, day graphs, L2 flushed between days ----
     fresh()
     sim.flush_l2()
@@ -261,7 +263,7 @@ def gpu_arm(args, wl, rank, world, device):
     return dict(agent_days=agent_days, ms=ms, wall=wall, live=live, rows=rows, clocks=clk.summary(), passes=passes,
                 gpu_launches=gpu_launches, scatter_ms=scatter_ms, count_ms=count_ms, publish_ms=publish_ms, achieved=achieved, peak=peak,
                 peak_kind=peak_kind, traffic=traffic, e2e_agent_days=e2e_live / 24.0, e2e_wall=e2e_wall,
-                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned, small=small, small0=small0)
+                count_gbs=count_bytes.mean() / (count_ms * 1e-3) / 1e9, days=days, tuned=tuned, items=items, small=small, small0=small0)
 
 
 def cpu_reference(wl, seconds: float, first_steps: int | None = None, warmup: int = 0):
@@ -375,6 +377,7 @@ def ensemble_arm(args):
     setup_batch = time.perf_counter() - t_all
     b.run(24 * args.warmup)
     tuned = b.autotune()
+    batch_items = b.items_per_thread()
     launches0 = b.launches()
     with ClockSampler(0) as clk:
         b.run(24 * args.steps)
@@ -425,6 +428,7 @@ def ensemble_arm(args):
                             "one at a time: uploaded",
                    "initial_agents_total": int(sizes.sum()), "agent_days_timed": live_sum / 24.0,
                    "ctas_per_sm": {"count": tuned[0], "scatter": tuned[1], "picked_by": "sampo_batch_autotune"},
+                   "slots_per_thread": batch_items,
                    "l2": "pools far larger than L2"},
         "batched": {"replicate_days_per_s": value, "sims_per_s_365d_equiv": value / 365.0,
                     "agent_days_per_s": live_sum / 24.0 / dev_batch, "device_s": dev_batch,
@@ -582,6 +586,8 @@ def main():
     ap.add_argument("--small-step", default="auto",
                     help="plain-path workloads: 'auto' (one-launch step for pools of up to one tile per CTA of its "
                          "grid), 'off' (the three-kernel step every hour) or a largest pool in 1024-slot tiles")
+    ap.add_argument("--small-items", type=int, default=0, choices=(0, 2, 4),
+                    help="plain-path workloads: slots per thread of the one-launch step (0: by pool size)")
     ap.add_argument("--replicates", type=int, default=512, help="ensemble: replicates")
     ap.add_argument("--requests", type=int, default=200, help="served: requests per rate")
     ap.add_argument("--plain-every", type=int, default=8, help="ensemble-year: the one-at-a-time arm's sample stride")
@@ -648,10 +654,12 @@ def main():
                "pool_bytes": [float(pool_bytes.min()), float(pool_bytes.max())], "parallelism": f"replicas x{world}",
                "ctas_per_sm": {"count": r["tuned"][0], "scatter": r["tuned"][1],
                                "picked_by": "--ctas-per-sm" if args.ctas_per_sm else "sampo_autotune"},
+               "slots_per_thread": r["items"],
                "small_step": {"largest_grid_ctas": r["small"]["grid"], "max_tiles": r["small"]["max_tiles"],
                               "timed_days_one_launch": r["small"]["days_one_launch"] - r["small0"]["days_one_launch"],
                               "timed_days_three_kernel": r["small"]["days_three_kernel"] - r["small0"]["days_three_kernel"],
-                              "one_launch_kind": {0: "-", 1: "-", 2: "cooperative launch", 3: "plain launch of a co-resident grid"}[r["small"]["last_day"]]}}
+                              "one_launch_kind": {0: "-", 1: "-", 2: "cooperative launch", 3: "plain launch of a co-resident grid"}[r["small"]["last_day"]],
+                              "slots_per_thread": args.small_items or "by pool size (2 up to 228 512-slot tiles, else 4)"}}
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,

@@ -194,17 +194,22 @@ int sampo_items_per_thread(sampo_sim* s, uint32_t* items);
  * launch sequence of src/abms.c:502-529 that the three-kernel step already
  * shortens). sampo_run picks each day's graph from the pool size it last
  * saw (it learns the size after each day, one day behind the queued work):
- * a pool of at most max_tiles 1024-slot tiles takes 24 launches of one
- * cooperative kernel (update, scan and compaction with one grid barrier,
- * publish by its last CTA) on a grid sized to the pool, a larger one the
- * count, update/scatter and publish kernels. Both give the same results at
- * any size. SAMPO_SMALL_STEP_DEFAULT: the largest co-resident grid of the
- * one-launch kernel, one tile per CTA (the default); 0: never.
- * sampo_run_async picks by the size seen at its call; sampo_step, runs with
- * timing on and a run-time species (sampo_set_species) always take the
- * three-kernel step. */
+ * a pool of at most max_tiles 1024-slot tiles takes one launch of a
+ * cooperative kernel that runs the day's 24 hourly steps (update, scan and
+ * compaction with two bounded grid barriers per hour) on a grid sized to the
+ * pool, a larger one the count, update/scatter and publish kernels every
+ * hour. Both give the same results at any size. SAMPO_SMALL_STEP_DEFAULT:
+ * the largest co-resident grid of the one-launch kernel, one tile per CTA
+ * (the default); 0: never. sampo_run_async picks by the size seen at its
+ * call; sampo_step, runs with timing on and a run-time species
+ * (sampo_set_species) always take the three-kernel step. */
 #define SAMPO_SMALL_STEP_DEFAULT 0xffffffffu
 int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles);
+/* Slots per thread of the one-launch step: 0 (the default) takes 512-slot
+ * tiles (2) while the pool leaves the largest grid room for them and
+ * 1024-slot tiles (4) above that; 2 or 4 fix it. The results do not depend
+ * on it. */
+int sampo_set_small_step_items(sampo_sim* s, uint32_t items);
 /* The one-launch step's largest grid (CTAs; 0 when it cannot run here), the
  * current max_tiles, the kind of the last day launched (0 none yet, 1
  * three-kernel steps, 2 one-launch steps launched cooperatively, 3 the same

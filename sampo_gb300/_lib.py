@@ -142,6 +142,7 @@ SIGNATURES = {
     "sampo_autotune": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "sampo_set_grids": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "sampo_set_small_step": (C.c_int, [_P, C.c_uint32]),
+    "sampo_set_small_step_items": (C.c_int, [_P, C.c_uint32]),
     "sampo_set_items_per_thread": (C.c_int, [_P, C.c_uint32]),
     "sampo_items_per_thread": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "sampo_batch_set_items_per_thread": (C.c_int, [_P, C.c_uint32]),

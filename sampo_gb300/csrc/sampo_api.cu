@@ -61,9 +61,10 @@ struct sampo_sim {
   // grids sized to the pool (kSmallBuckets sizes up to small_grid), picked
   // per day from the pool end the host last saw (known_end).
   int small_grid = 0;                  // largest grid of the one-launch step (0: it cannot run on this device)
-  uint32_t small_tiles = 0;            // largest pool in tiles that takes the one-launch step (0: never)
-  cudaGraphExec_t small_graph[8] = {};
-  int small_graph_kind[8] = {};        // DG_* of each
+  uint32_t small_tiles = 0;            // largest pool in 1024-slot tiles that takes the one-launch step (0: never)
+  int small_items = 0;                 // its slots per thread: 2, 4, or 0 (by pool size)
+  cudaGraphExec_t small_graph[2][8] = {};  // [512-slot tiles, 1024-slot tiles][grid bucket]
+  int small_graph_kind[2][8] = {};     // DG_* of each
   uint32_t known_end = 0;              // pool end at the start of the coming day, as last seen by the host
   uint32_t* end_pinned = nullptr;      // pool end after a day, copied back one day behind the queue
   cudaEvent_t ev_day[2] = {nullptr, nullptr};
@@ -151,7 +152,8 @@ extern "C" int sampo_destroy(sampo_sim* s) {
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->day_graph) cudaGraphExecDestroy(s->day_graph);
-  for (auto& g : s->small_graph) if (g) cudaGraphExecDestroy(g);
+  for (auto& row : s->small_graph)
+    for (auto& g : row) if (g) cudaGraphExecDestroy(g);
   for (auto& e : s->ev_day) if (e) cudaEventDestroy(e);
   if (s->end_pinned) cudaFreeHost(s->end_pinned);
   for (auto& e : s->ev) if (e) cudaEventDestroy(e);
@@ -236,7 +238,7 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     }
     s->grid_count = grid_blocks_count(1);
     s->grid_scatter = grid_blocks_scatter(1);
-    s->small_grid = grid_blocks_small();
+    s->small_grid = std::min(grid_blocks_small(2), grid_blocks_small(4));
     s->small_tiles = s->small_grid > 0 ? (uint32_t)s->small_grid : 0u;  // one tile per CTA
     if ((e = cudaMallocHost(&s->end_pinned, 2 * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(s, e, "pinned"); break; }
     for (auto& ev : s->ev_day) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -459,24 +461,25 @@ static void drop_day_graph(sampo_sim* s) {
 // A day on grid bucket b: one launch of 24 one-launch steps, cooperative
 // where a graph takes a cooperative launch, else a plain launch of the same
 // co-resident grid (its grid barriers are bounded either way).
-static cudaError_t build_small_graph(sampo_sim* s, int b) {
+static cudaError_t build_small_graph(sampo_sim* s, int items, int b) {
   const KParams p = make_params(s);
   const int grid = (int)small_bucket_grid(s, b);
+  const int ti = items == 2 ? 0 : 1;
   cudaError_t e = cudaErrorUnknown;
   for (int kind : {DG_SMALL_COOP, DG_SMALL}) {
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) break;
-    e = launch_small(p, grid, kind == DG_SMALL_COOP, 24u, s->stream);
+    e = launch_small(p, grid, kind == DG_SMALL_COOP, 24u, s->stream, items);
     const cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
     if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->small_graph[b], g, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->small_graph[ti][b], g, 0);
     if (g) cudaGraphDestroy(g);
     if (e == cudaSuccess) {
-      s->small_graph_kind[b] = kind;
+      s->small_graph_kind[ti][b] = kind;
       return cudaSuccess;
     }
-    s->small_graph[b] = nullptr;
+    s->small_graph[ti][b] = nullptr;
     (void)cudaGetLastError();
   }
   return e;
@@ -484,19 +487,25 @@ static cudaError_t build_small_graph(sampo_sim* s, int b) {
 
 // The graph of the coming day and its kernel launches: the one-launch step
 // (grid of at least kSmallGrowth CTAs per tile of the pool end last seen)
-// when that pool has at most small_tiles tiles, else the three-kernel step.
-// Either gives the same results at any size: a pool that outgrew its pick
-// is stepped by the one-launch kernel's extra-tile route.
+// when that pool has at most small_tiles 1024-slot tiles, else the
+// three-kernel step. The one-launch step takes 512-slot tiles (half the
+// chain of updates per thread) while the largest grid has room for them,
+// else 1024-slot tiles. Any pick gives the same results at any size: a pool
+// that outgrew its pick is stepped by the one-launch kernel's extra-tile route.
 static int day_graph_for(sampo_sim* s, cudaGraphExec_t* gx, uint32_t* kernels, int* kind) {
-  const uint32_t tiles = (s->known_end + kTile - 1) / kTile;
-  if (!s->species && s->small_grid > 0 && s->small_tiles > 0 && tiles <= s->small_tiles) {
+  const uint32_t t4 = (s->known_end + kTile - 1) / kTile, t2 = (s->known_end + kTileMin - 1) / kTileMin;
+  if (!s->species && s->small_grid > 0 && s->small_tiles > 0 && t4 <= s->small_tiles) {
+    int items = s->small_items;
+    if (items == 0) items = (uint64_t)(t2 ? t2 : 1u) * kSmallGrowth <= (uint64_t)s->small_grid ? 2 : 4;
+    const uint32_t tiles = items == 2 ? t2 : t4;
     const uint64_t want = (uint64_t)(tiles ? tiles : 1u) * kSmallGrowth;
+    const int ti = items == 2 ? 0 : 1;
     int b = 0;
     while (b + 1 < kSmallBuckets && small_bucket_grid(s, b) < want) b++;
-    if (s->small_graph[b] || build_small_graph(s, b) == cudaSuccess) {
-      *gx = s->small_graph[b];
+    if (s->small_graph[ti][b] || build_small_graph(s, items, b) == cudaSuccess) {
+      *gx = s->small_graph[ti][b];
       *kernels = 1;
-      *kind = s->small_graph_kind[b];
+      *kind = s->small_graph_kind[ti][b];
       return SAMPO_OK;
     }
   }
@@ -513,6 +522,14 @@ extern "C" int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles) {
   SETTLE(s);
   if (max_tiles == SAMPO_SMALL_STEP_DEFAULT) max_tiles = s->small_grid > 0 ? (uint32_t)s->small_grid : 0u;
   s->small_tiles = max_tiles;
+  return SAMPO_OK;
+}
+
+extern "C" int sampo_set_small_step_items(sampo_sim* s, uint32_t items) {
+  if (!s) return SAMPO_ERR_ARG;
+  if (items != 0 && items != 2 && items != 4) return fail(s, SAMPO_ERR_ARG, "slots per thread of the one-launch step: 0, 2 or 4");
+  SETTLE(s);
+  s->small_items = (int)items;
   return SAMPO_OK;
 }
 

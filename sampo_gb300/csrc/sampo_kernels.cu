@@ -123,6 +123,12 @@ static cudaError_t launch_trial_reset(const KParams& p, cudaStream_t st) {
   void* args[] = {&q};
   return launch(p, KID_TRIAL_RESET, (const void*)k_trial_reset, (int)((p.nrep + 255) / 256), 256, 0, st, args);
 }
+// The built-in kernels only: a run-time species is tuned at one tile size.
+static cudaError_t launch_clear_lookback(const KParams& p, cudaStream_t st) {
+  KParams q = p;
+  void* args[] = {&q};
+  return cudaLaunchKernel((const void*)k_clear_lookback, sm_count() * 4, 256, args, 0, st);
+}
 // The grid tuner of one tile size: see tune_grids.
 static cudaError_t tune_grids_items(const KParams& p, cudaStream_t st, int items, cudaEvent_t* ev, int* grid_count,
                                     int* grid_scatter, double* best_ms) {
@@ -207,7 +213,8 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
     if (e != cudaSuccess || (it != kItems && p.ks)) break;
     int gc = 0, gs = 0;
     double ms = 1e30;
-    e = tune_grids_items(p, st, it, ev, &gc, &gs, &ms);
+    if (!p.ks) e = launch_clear_lookback(p, st);  // the other tile size's trial prefixes
+    if (e == cudaSuccess) e = tune_grids_items(p, st, it, ev, &gc, &gs, &ms);
     if (e == cudaSuccess && ms < best) {
       best = ms;
       bi = it;
@@ -216,6 +223,7 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
     }
   }
   if (e == cudaSuccess) e = launch_trial_reset(p, st);
+  if (e == cudaSuccess && !p.ks) e = launch_clear_lookback(p, st);  // the step may run at either tile size
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   for (int i = 0; i < 3; i++)
     if (ev[i]) cudaEventDestroy(ev[i]);
@@ -225,9 +233,12 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
   if (best_ms) *best_ms = best;
   return e;
 }
-int grid_blocks_small() {
+static const void* small_fn(int items) {
+  return items == 2 ? (const void*)k_step_small<2> : (const void*)k_step_small<4>;
+}
+int grid_blocks_small(int items) {
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_small, kSmallThreads, kSmallStage) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, small_fn(items), kSmallThreads, small_stage(items)) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;
   }
@@ -249,20 +260,20 @@ cudaError_t graph_kernel_nodes(cudaGraph_t g, uint32_t* kernels) {
   return e;
 }
 
-cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st) {
+cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st, int items) {
   KParams q = p;
   void* args[] = {&q, &nsteps};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kSmallThreads);
-  cfg.dynamicSmemBytes = kSmallStage;
+  cfg.dynamicSmemBytes = small_stage(items);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = cooperative ? 1 : 0;
-  return cudaLaunchKernelExC(&cfg, (const void*)k_step_small, args);
+  return cudaLaunchKernelExC(&cfg, small_fn(items), args);
 }
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st) {
   k_eval_math<<<sm_count() * 2, 256, 0, st>>>(fn, x, y, out, n);

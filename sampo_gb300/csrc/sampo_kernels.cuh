@@ -212,12 +212,13 @@ cudaError_t launch_histogram(const KParams& p, uint32_t* hist_dev, cudaStream_t 
 cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t st);
 // Kernel nodes in a captured graph (the launches one replay makes).
 cudaError_t graph_kernel_nodes(cudaGraph_t g, uint32_t* kernels);
-// The one-launch steps of a single simulation (sampo_small_step.cuh): the
-// largest grid (CTAs resident on all SMs, 0 if it cannot run) and a launch
-// of `nsteps` hourly steps (a cooperative launch when `cooperative`) on
-// `grid` CTAs.
-int grid_blocks_small();
-cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st);
+// The one-launch steps of a single simulation (sampo_small_step.cuh) with
+// tiles of kBlock * items slots (items 2 or 4): the largest grid (CTAs
+// resident on all SMs, 0 if it cannot run) and a launch of `nsteps` hourly
+// steps (a cooperative launch when `cooperative`) on `grid` CTAs.
+int grid_blocks_small(int items = kItems);
+cudaError_t launch_small(const KParams& p, int grid, bool cooperative, uint32_t nsteps, cudaStream_t st,
+                         int items = kItems);
 // Times count + scatter of the coming step for each tile size (4 and, for
 // the built-in species, 2 slots per thread) at every (count, scatter) number
 // of CTAs per SM the occupancy allows, and returns the fastest tile size and

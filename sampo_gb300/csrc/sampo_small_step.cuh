@@ -11,17 +11,18 @@
 //           CTA's shared memory with their next state in the flag byte; the
 //           CTA builds the tile's prefix table over its (round, warp) chunks
 //           in shared memory and publishes the tile's survivors per next
-//           state and its eggs laid to global memory.
+//           state, its eggs laid and its share of the next pool's statistics
+//           (calcL1de.cl, calcGender.cl) to global memory.
 //  barrier  a grid barrier with a bounded wait.
 //  phase 2  every CTA sums the per-tile counts: the totals give the next
 //           layout (kernel/oldToNewAgents.cl:57-95), the tiles before its own
 //           the tile's first slot in each next-state range. It writes its
-//           survivors from shared memory to their slots in the next buffer,
-//           the new eggs of its egg tiles at [0, newEggs)
-//           (kernel/initAgents.cl:26-65), and adds its share of the next
-//           pool's statistics (calcL1de.cl, calcGender.cl).
-//  publish  the last CTA to finish publishes the next step (the k_publish
-//           code).
+//           survivors from shared memory to their slots in the next buffer
+//           and the new eggs of its egg tiles at [0, newEggs)
+//           (kernel/initAgents.cl:26-65), then computes the next step's
+//           state from the totals (the k_publish code); the last CTA also
+//           stores it for the host.
+//  barrier  a second grid barrier; the next hour's tile copies go out.
 //
 // Pools with more tiles than CTAs are still stepped correctly: CTA b also
 // takes tiles b + G, b + 2G, ... (G CTAs); their decisions are counted in
@@ -34,12 +35,17 @@
 
 namespace sampo {
 
-constexpr int kSmallThreads = kBlock;      // eight warps, kItems slots per thread
+constexpr int kSmallThreads = kBlock;      // eight warps, I slots per thread (tiles of kBlock * I slots)
 constexpr int kSmallMinBlocks = 3;         // resident CTAs per SM the registers are sized for
-constexpr uint32_t kSmallStage = kPreOff;  // the ten columns of one tile
+__host__ __device__ constexpr uint32_t small_stage(int items) { return 9 * kBlock * items * 4 + kBlock * items; }  // ten columns
 constexpr uint32_t kSmallRows = 9;         // per-tile counts: survivors by next state, eggs laid
 constexpr uint8_t kGone = 0xffu;           // flag byte of a slot without a survivor
-static_assert(kSmallRows <= kPreWords, "the per-tile count rows fit the prefix-table array");
+constexpr uint32_t kSmallHours = 24;       // hours whose inputs a CTA holds in shared memory
+// Per-CTA statistics of the next pool (CTA b's column, b < the tiles):
+// L1de, females, infective, cycles, sum of cycles, bites, infective bites
+// (sums) and the min and max larva age in days.
+enum : uint32_t { SA_L1 = 0, SA_FEM, SA_INF, SA_CYC, SA_SUMCYC, SA_BITES, SA_IBITES, SA_DMIN, SA_DMAX, kSmallStats };
+static_assert(kSmallRows + kSmallStats <= kPreWordsMin, "the per-tile rows fit the prefix-table array");
 
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   uint32_t v;
@@ -82,9 +88,10 @@ struct SmallAcc {
 // next state go to s_ent. EGGS / STATS: the eggs laid / the update's
 // counters and the next pool's statistics go to sa (a tile updated twice
 // counts its eggs the first time and the rest the second).
-template <bool KEEP, bool EGGS, bool STATS>
+template <int I, bool KEEP, bool EGGS, bool STATS>
 __device__ __forceinline__ void small_update_tile(const StepCtx& c, const ModelConst& mc, const sampo_population& pop,
                                                   uint8_t* st, uint32_t lo, uint32_t end, uint2* s_ent, SmallAcc& sa) {
+  SAMPO_TILE_CONSTANTS(I);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float* c_age = (float*)(st + 0 * kColBytes);
   float* c_his = (float*)(st + 1 * kColBytes);
@@ -155,7 +162,9 @@ __device__ __forceinline__ void small_update_tile(const StepCtx& c, const ModelC
 // Warp 0, after the tile's chunk counts are in s_ent: the tile's prefix table
 // (the same 16-bit packed entries as the count pass's) into s_tab, and the
 // tile's survivors of next state `lane` to lanes 0..7.
+template <int I>
 __device__ __forceinline__ uint32_t small_build_table(const uint2* s_ent, uint32_t* s_tab) {
+  SAMPO_TILE_CONSTANTS(I);
   const int lane = threadIdx.x & 31;
   const uint2 e = lane < (int)kChunks ? s_ent[lane] : make_uint2(0u, 0u);
   uint32_t w[5], x[5];
@@ -196,8 +205,10 @@ __device__ __forceinline__ uint32_t small_build_table(const uint2* s_ent, uint32
 // buffer: the tile's first slot of the state (s_d0) + the survivors of that
 // state in earlier chunks (s_tab) + the rank within the chunk. A survivor
 // whose slot falls outside its chunk's run sets tilebad and is not stored.
+template <int I>
 __device__ __forceinline__ void small_scatter_tile(const uint8_t* st, const uint32_t* s_tab, const uint32_t* s_d0,
                                                    const DevPool& dst, uint32_t& tilebad) {
+  SAMPO_TILE_CONSTANTS(I);
   const int tid = threadIdx.x, warp = tid >> 5;
   const float* c_age = (const float*)(st + 0 * kColBytes);
   const float* c_his = (const float*)(st + 1 * kColBytes);
@@ -234,27 +245,100 @@ __device__ __forceinline__ void small_scatter_tile(const uint8_t* st, const uint
   }
 }
 
-// Phase 2, warps 0..7 (row w; warp 0 also row 8): the sums over the per-tile
-// counts of tiles [0, t) into s_ex and, with `totals`, over all nold tiles
-// into s_tot. Rows are state-major: rows[row * stride + tile], read through L2.
+// Phase 2, all threads: over the per-tile counts (rows 0..8), the sums of
+// tiles [0, t) into s_ex and, with `totals`, of all nold tiles into s_tot,
+// followed by the statistics rows over the columns of the CTAs that held
+// tiles (min(nold, G); sums, min and max) into s_tot[kSmallRows ..]. Thread
+// i takes columns i, i + blockDim.x, ...: every row of a column is loaded at
+// once, so one round trip to L2 serves them all. Rows are state-major:
+// rows[row * stride + column], read through L2. Ends synchronised.
+constexpr uint32_t kSumWords = 2 * kSmallRows + kSmallStats;  // ex, tot, statistics
 __device__ __forceinline__ void small_sum_rows(const uint32_t* rows, uint32_t stride, uint32_t nold, uint32_t t,
-                                               bool totals, uint32_t* s_ex, uint32_t* s_tot) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int row = warp; row < (int)kSmallRows; row += kWarps) {
-    const uint32_t* r = rows + (size_t)row * stride;
-    const uint32_t lim = totals ? nold : t;
-    uint32_t ex = 0, tot = 0;
-    for (uint32_t j = lane; j < lim; j += 32) {
-      const uint32_t v = __ldcg(r + j);
-      tot += v;
-      ex += j < t ? v : 0u;
+                                               bool totals, uint32_t* s_ex, uint32_t* s_tot,
+                                               uint32_t (*s_part)[kSumWords]) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t ex[kSmallRows], tot[kSmallRows], st[kSmallStats];
+#pragma unroll
+  for (int r = 0; r < (int)kSmallRows; r++) ex[r] = tot[r] = 0;
+#pragma unroll
+  for (int k = 0; k < (int)kSmallStats; k++) st[k] = k == (int)SA_DMIN ? 0xffffffffu : 0u;
+  const uint32_t lim = totals ? nold : t;
+  for (uint32_t j = tid; j < lim; j += blockDim.x) {
+    uint32_t v[kSmallRows];
+#pragma unroll
+    for (int r = 0; r < (int)kSmallRows; r++) v[r] = __ldcg(rows + (size_t)r * stride + j);
+#pragma unroll
+    for (int r = 0; r < (int)kSmallRows; r++) {
+      tot[r] += v[r];
+      ex[r] += j < t ? v[r] : 0u;
     }
-    ex = __reduce_add_sync(0xffffffffu, ex);
-    tot = __reduce_add_sync(0xffffffffu, tot);
-    if (lane == 0) {
-      s_ex[row] = ex;
-      if (totals) s_tot[row] = tot;
+  }
+  if (totals) {
+    const uint32_t cols = min(nold, gridDim.x);  // one column per CTA with tiles
+    for (uint32_t j = tid; j < cols; j += blockDim.x) {
+      uint32_t v[kSmallStats];
+#pragma unroll
+      for (int k = 0; k < (int)kSmallStats; k++) v[k] = __ldcg(rows + (size_t)(kSmallRows + k) * stride + j);
+#pragma unroll
+      for (int k = 0; k < (int)kSmallStats; k++)
+        st[k] = k == (int)SA_DMIN ? min(st[k], v[k]) : k == (int)SA_DMAX ? max(st[k], v[k]) : st[k] + v[k];
     }
+  }
+#pragma unroll
+  for (int r = 0; r < (int)kSmallRows; r++) {
+    ex[r] = __reduce_add_sync(0xffffffffu, ex[r]);
+    tot[r] = __reduce_add_sync(0xffffffffu, tot[r]);
+  }
+#pragma unroll
+  for (int k = 0; k < (int)kSmallStats; k++)
+    st[k] = k == (int)SA_DMIN ? __reduce_min_sync(0xffffffffu, st[k])
+          : k == (int)SA_DMAX ? __reduce_max_sync(0xffffffffu, st[k]) : __reduce_add_sync(0xffffffffu, st[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int r = 0; r < (int)kSmallRows; r++) {
+      s_part[warp][r] = ex[r];
+      s_part[warp][kSmallRows + r] = tot[r];
+    }
+#pragma unroll
+    for (int k = 0; k < (int)kSmallStats; k++) s_part[warp][2 * kSmallRows + k] = st[k];
+  }
+  __syncthreads();
+  if (tid < (int)kSumWords) {
+    const int k = tid - 2 * (int)kSmallRows;  // statistic, for the last kSmallStats words
+    uint32_t x = s_part[0][tid];
+    for (int w = 1; w < kWarps; w++) {
+      const uint32_t y = s_part[w][tid];
+      x = k == (int)SA_DMIN ? min(x, y) : k == (int)SA_DMAX ? max(x, y) : x + y;
+    }
+    if (tid < (int)kSmallRows) s_ex[tid] = x;
+    else if (totals) s_tot[tid - kSmallRows] = x;
+  }
+  __syncthreads();
+}
+
+// Phase 1's end: the CTA's statistics of the next pool (its tiles) to its
+// column of the statistics rows. All threads.
+__device__ __forceinline__ void small_put_stats(const SmallAcc& sa, uint32_t* rows, uint32_t stride, uint32_t b,
+                                                uint32_t (*s_red)[kSmallStats]) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t v[kSmallStats] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
+                             sa.dmin, sa.dmax};
+#pragma unroll
+  for (int j = 0; j < (int)SA_DMIN; j++) v[j] = __reduce_add_sync(0xffffffffu, v[j]);
+  v[SA_DMIN] = __reduce_min_sync(0xffffffffu, v[SA_DMIN]);
+  v[SA_DMAX] = __reduce_max_sync(0xffffffffu, v[SA_DMAX]);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < (int)kSmallStats; j++) s_red[warp][j] = v[j];
+  }
+  __syncthreads();
+  if (tid < (int)kSmallStats) {
+    uint32_t x = s_red[0][tid];
+    for (int w = 1; w < kWarps; w++) {
+      const uint32_t y = s_red[w][tid];
+      x = tid == (int)SA_DMIN ? min(x, y) : tid == (int)SA_DMAX ? max(x, y) : x + y;
+    }
+    __stcg(rows + (size_t)(kSmallRows + tid) * stride + b, x);
   }
 }
 
@@ -266,7 +350,9 @@ __device__ __forceinline__ bool small_wait_stage(uint64_t* bar, uint32_t& phase)
   return __syncthreads_and(ok) != 0;
 }
 
+template <int I>
 __device__ __forceinline__ void small_issue_tile(const DevPool& src, uint8_t* st, uint64_t* bar, uint32_t lo, uint32_t n) {
+  SAMPO_TILE_CONSTANTS(I);
   const uint32_t b4 = (n * 4 + 15) & ~15u, b1 = (n + 15) & ~15u;
   mbar_arrive_tx(bar, 9 * b4 + b1);
   bulk_load(st + 0 * kColBytes, src.age + lo, b4, bar);
@@ -283,38 +369,35 @@ __device__ __forceinline__ void small_issue_tile(const DevPool& src, uint8_t* st
 
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
-// Per-hour statistics of the next pool, accumulated by every CTA with
-// atomics (words: L1de, females, infective, cycles, sum of cycles, bites,
-// infective bites, min and max larva age in days). Two sets alternate by
-// hour, so that one is cleared while the other is read.
-constexpr uint32_t kSmallAcc = 16;
-enum : uint32_t { SA_L1 = 0, SA_FEM, SA_INF, SA_CYC, SA_SUMCYC, SA_BITES, SA_IBITES, SA_DMIN, SA_DMAX };
-
 // The one-launch steps of p.reps[0] (a single simulation without a device
 // seed stream): `nsteps` hourly steps in one cooperative launch (a day graph
-// launches it once with 24). Per hour: the update (phase 1), a grid barrier,
-// the scatter (phase 2) and the statistics, a second grid barrier; then
-// every CTA computes the next hour's layout, statistics row, step constants
-// and larval table itself from the same totals (the k_publish arithmetic),
-// while the next hour's tile is already on its way, and the last CTA (the
-// one least likely to hold a tile) writes them to the replicate's state for
-// the host. The per-tile count rows and the two
-// sets of hourly statistics use the replicate's prefix-table array (tilePre:
-// kPreWords words per tile; the rows take kSmallRows per tile, the
-// statistics 2 x kSmallAcc words after them), which the three-kernel step
-// rewrites before it reads it. The pool the scatter wrote with ordinary
-// stores is read by the next hour's bulk copies after proxy fences.
+// launches it once with 24). Per hour: the update (phase 1), whose per-tile
+// counts and per-CTA statistics of the next pool go to rows in global
+// memory; a grid barrier; the scatter (phase 2), after which every CTA
+// computes the next hour's layout, statistics row, step constants and larval
+// table itself from the same totals (the k_publish arithmetic; the last CTA,
+// the one least likely to hold a tile, also writes them to the replicate's
+// state for the host); a second grid barrier, after which the next hour's
+// tile copies go out. The step inputs of the launch's hours are read into
+// shared memory at its start (the host writes them before the launch). The
+// rows use the replicate's prefix-table array (tilePre: kSmallRows +
+// kSmallStats words per tile), which the three-kernel step rewrites before it
+// reads it. The pool the scatter wrote with ordinary stores is read by the
+// next hour's bulk copies after proxy fences.
+template <int I>
 __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(KParams p, uint32_t nsteps) {
+  SAMPO_TILE_CONSTANTS(I);
   extern __shared__ __align__(128) uint8_t stage[];
   __shared__ StepCtx s_c;
   __shared__ ModelConst s_mc;
   __shared__ float s_hmr[100];
   __shared__ sampo_population s_pop;
+  __shared__ CtxInputs s_in[kSmallHours];
   __shared__ __align__(8) uint64_t s_mbar;
   __shared__ uint2 s_ent[kChunks];
   __shared__ __align__(16) uint32_t s_tab[(kChunks + 1) * kPreEntryWords];
-  __shared__ uint32_t s_ex[kSmallRows], s_tot[kSmallRows], s_d0[8], s_ne[kWarps];
-  __shared__ uint32_t s_red[kWarps][10], s_acc[kSmallAcc];
+  __shared__ uint32_t s_ex[kSmallRows], s_tot[kSmallRows + kSmallStats], s_d0[8], s_ne[kWarps];
+  __shared__ uint32_t s_red[kWarps][kSmallStats], s_part[kWarps][kSumWords];
   __shared__ uint32_t s_flag, s_ok, s_last;
   __shared__ uint32_t s_active, s_end, s_nold, s_cur, s_cap, s_step, s_epoch, s_stop;
   __shared__ float s_cc;
@@ -325,8 +408,7 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
   uint32_t phase = 0, barriers = 0;
   bool met = true, ok = true;
   const uint32_t stride = rp.maxTiles;
-  uint32_t* rows = rp.tilePre;                       // [kSmallRows][stride]
-  uint32_t* accs = rows + (size_t)kSmallRows * stride;  // [2][kSmallAcc]
+  uint32_t* rows = rp.tilePre;  // [kSmallRows + kSmallStats][stride]
 
   // ---- the replicate's state at the launch (the previous kernel wrote it) ----
   if (tid == 0) {
@@ -345,10 +427,7 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     s_cc = sim->cc;
     if (b < s_nold) {
       const uint32_t lo = b * kTile;
-      small_issue_tile(rp.pool[s_cur], stage, &s_mbar, lo, min((uint32_t)kTile, s_end - lo));
-    }
-    if (b == G - 1u) {  // both sets of hourly statistics start cleared
-      for (uint32_t k = 0; k < 2 * kSmallAcc; k++) accs[k] = (k % kSmallAcc) == SA_DMIN ? 0xffffffffu : 0u;
+      small_issue_tile<I>(rp.pool[s_cur], stage, &s_mbar, lo, min((uint32_t)kTile, s_end - lo));
     }
   }
   copy16(&s_c, &sim->ctx, (int)sizeof(StepCtx), tid, blockDim.x);
@@ -356,12 +435,13 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
   load_model_const(p.mc, s_mc);
   __syncthreads();
   if (tid == 0) s_c.larvaHMR = s_hmr;
+  // the inputs of the steps that follow the launch's hours
+  for (uint32_t j = tid; j < min(nsteps, kSmallHours); j += blockDim.x) load_ctx_inputs(rp, s_step + 1u + j, s_in[j]);
   __syncthreads();
 
   for (uint32_t hour = 0; hour < nsteps; hour++) {
     if (!s_active) break;  // stopped or paused (uniform)
     const uint32_t nold = s_nold, end = s_end;
-    uint32_t* acc = accs + (hour & 1u) * kSmallAcc;
     SmallAcc sa;
     sa.acc = Acc{0, 0, 0, 0, 0, 0};
     sa.l1 = sa.fem = sa.inf = sa.dmax = sa.devoob = sa.tilebad = 0;
@@ -377,18 +457,18 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
         if (t != b) {
           if (tid == 0) {
             fence_proxy_async();
-            small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+            small_issue_tile<I>(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
           }
           ok = small_wait_stage(&s_mbar, phase);
           if (!ok) break;
         }
         const uint32_t eggs_before = sa.acc.newEggs;
-        small_update_tile<false, true, false>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
+        small_update_tile<I, false, true, true>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
         const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
         if (lane == 0) s_ne[warp] = ne;
         __syncthreads();
         if (warp == 0) {
-          const uint32_t tw = small_build_table(s_ent, s_tab);
+          const uint32_t tw = small_build_table<I>(s_ent, s_tab);
           if (lane < 8) __stcg(rows + (size_t)lane * stride + t, tw);
           uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
           e = __reduce_add_sync(0xffffffffu, e);
@@ -399,25 +479,25 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
       if (ok) {
         if (tid == 0) {
           fence_proxy_async();
-          small_issue_tile(rp.pool[s_cur], stage, &s_mbar, b * kTile, min((uint32_t)kTile, end - b * kTile));
+          small_issue_tile<I>(rp.pool[s_cur], stage, &s_mbar, b * kTile, min((uint32_t)kTile, end - b * kTile));
         }
         ok = small_wait_stage(&s_mbar, phase);
         if (ok) {
-          small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);  // eggs counted above
+          small_update_tile<I, true, false, false>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);  // counted above
           __syncthreads();
-          if (warp == 0) (void)small_build_table(s_ent, s_tab);
+          if (warp == 0) (void)small_build_table<I>(s_ent, s_tab);
         }
       }
     } else if (b < nold) {
       ok = small_wait_stage(&s_mbar, phase);
       if (ok) {
         const uint32_t eggs_before = sa.acc.newEggs;
-        small_update_tile<true, true, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);
+        small_update_tile<I, true, true, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);
         const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
         if (lane == 0) s_ne[warp] = ne;
         __syncthreads();
         if (warp == 0) {
-          const uint32_t tw = small_build_table(s_ent, s_tab);
+          const uint32_t tw = small_build_table<I>(s_ent, s_tab);
           if (lane < 8) __stcg(rows + (size_t)lane * stride + b, tw);
           uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
           e = __reduce_add_sync(0xffffffffu, e);
@@ -425,19 +505,15 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
         }
       }
     }
+    if (b < nold) small_put_stats(sa, rows, stride, b, s_red);
     if (tid == 0) s_ok = ok ? 1u : 0u;
 
-    // ---- grid barrier A: every tile's counts are published ----
+    // ---- grid barrier A: every tile's counts and every CTA's statistics are published ----
     met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
     ok = s_ok != 0;  // this CTA's copies all landed
-    if (b == G - 1u && tid == 0) {  // every CTA has read the other set of statistics (last hour's): clear it
-      uint32_t* other = accs + ((hour + 1u) & 1u) * kSmallAcc;
-      for (uint32_t k = 0; k < kSmallAcc; k++) other[k] = k == SA_DMIN ? 0xffffffffu : 0u;
-    }
 
     // ---- phase 2: totals, next layout, this tile's first slots; scatter ----
-    small_sum_rows(rows, stride, nold, b < nold ? b : nold, true, s_ex, s_tot);
-    __syncthreads();
+    small_sum_rows(rows, stride, nold, b < nold ? b : nold, true, s_ex, s_tot, s_part);
     uint32_t tot[8], base[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) tot[k] = s_tot[k];
@@ -450,26 +526,25 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     if (write && b < nold) {
       if (tid < 8) s_d0[tid] = base[tid] + s_ex[tid];
       __syncthreads();
-      small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
+      small_scatter_tile<I>(stage, s_tab, s_d0, dst, sa.tilebad);
       // more tiles than CTAs: the other tiles of this CTA, loaded and updated again
       for (uint32_t t = b + G; t < nold; t += G) {
         __syncthreads();  // the stage is read
         if (tid == 0) {
           fence_proxy_async();
-          small_issue_tile(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
+          small_issue_tile<I>(rp.pool[s_cur], stage, &s_mbar, t * kTile, min((uint32_t)kTile, end - t * kTile));
         }
         if (!small_wait_stage(&s_mbar, phase)) { ok = false; break; }
-        small_update_tile<true, false, true>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
-        small_sum_rows(rows, stride, nold, t, false, s_ex, s_tot);
-        __syncthreads();
+        small_update_tile<I, true, false, false>(s_c, s_mc, s_pop, stage, t * kTile, end, s_ent, sa);
+        small_sum_rows(rows, stride, nold, t, false, s_ex, s_tot, s_part);
         if (warp == 0) {
-          const uint32_t tw = small_build_table(s_ent, s_tab);
+          const uint32_t tw = small_build_table<I>(s_ent, s_tab);
           // the update again must give the counts of phase 1
           if (lane < 8 && tw != __ldcg(rows + (size_t)lane * stride + t)) sa.tilebad = 1;
           if (lane < 8) s_d0[lane] = base[lane] + s_ex[lane];
         }
         if (__syncthreads_or(sa.tilebad)) break;
-        small_scatter_tile(stage, s_tab, s_d0, dst, sa.tilebad);
+        small_scatter_tile<I>(stage, s_tab, s_d0, dst, sa.tilebad);
       }
     }
     if (write) {
@@ -492,40 +567,16 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     }
     fence_proxy_async_global();  // the next hour reads these stores with bulk copies
 
-    // ---- this CTA's statistics: reduced in the CTA, one atomic per counter ----
+    // ---- this CTA's error bits (the capacity bit from CTA 0 only) ----
     {
-      uint32_t v[10] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
-                        (sa.acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (sa.tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u) |
-                            (sa.devoob ? SAMPO_DEV_ERR_DEVRATES : 0u) | (ok ? 0u : SAMPO_DEV_ERR_TMA) |
-                            (met ? 0u : SAMPO_DEV_ERR_BARRIER) | (fits ? 0u : SAMPO_DEV_ERR_CAPACITY),
-                        sa.dmin, sa.dmax};
-#pragma unroll
-      for (int j = 0; j < 7; j++) v[j] = __reduce_add_sync(0xffffffffu, v[j]);
-      v[7] = __reduce_or_sync(0xffffffffu, v[7]);
-      v[8] = __reduce_min_sync(0xffffffffu, v[8]);
-      v[9] = __reduce_max_sync(0xffffffffu, v[9]);
-      if (lane == 0) {
-#pragma unroll
-        for (int j = 0; j < 10; j++) s_red[warp][j] = v[j];
-      }
-      __syncthreads();
-      if (tid < 10) {
-        uint32_t x = s_red[0][tid];
-        for (int w = 1; w < kWarps; w++) {
-          const uint32_t y = s_red[w][tid];
-          x = tid < 7 ? x + y : tid == 7 ? (x | y) : tid == 8 ? min(x, y) : max(x, y);
-        }
-        if (tid < 7) { if (x) atomicAdd(&acc[tid], x); }
-        else if (tid == 7) { if (x && (b == 0 || (x & ~SAMPO_DEV_ERR_CAPACITY))) atomicOr(&sim->error, x); }
-        else if (tid == 8) { if (x != 0xffffffffu) atomicMin(&acc[SA_DMIN], x); }
-        else { if (x) atomicMax(&acc[SA_DMAX], x); }
-      }
+      uint32_t x = (sa.acc.bad ? SAMPO_DEV_ERR_LARVATABLE : 0u) | (sa.tilebad ? SAMPO_DEV_ERR_TILECOUNT : 0u) |
+                   (sa.devoob ? SAMPO_DEV_ERR_DEVRATES : 0u) | (ok ? 0u : SAMPO_DEV_ERR_TMA) |
+                   (met ? 0u : SAMPO_DEV_ERR_BARRIER) | (fits ? 0u : SAMPO_DEV_ERR_CAPACITY);
+      x = __reduce_or_sync(0xffffffffu, x);
+      if (b != 0) x &= ~SAMPO_DEV_ERR_CAPACITY;
+      if (lane == 0 && x) atomicOr(&sim->error, x);
     }
     if (!met || !ok) break;  // the error bits are set; nothing after this hour is valid
-
-    // ---- grid barrier B: every CTA's stores and statistics are in ----
-    met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
-    if (!met) break;
     if (!fits) {
       // the next layout does not fit: the replicate pauses at this step with
       // its pool and constants (k_publish does the same for the three-kernel step)
@@ -533,47 +584,36 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
       break;
     }
 
-    // ---- the next hour's tile is on its way while every CTA computes the
-    //      next hour's state (the k_publish arithmetic, publish_rep) ----
+    // ---- the next hour's state (the k_publish arithmetic, publish_rep), by
+    //      every CTA from the same totals ----
     const uint32_t step = s_step + 1u;
     const bool active = step < s_stop;
     const uint32_t next_end = np.r[GRAVID].end, next_nold = (next_end + kTile - 1) / kTile;
-    if (tid == 0 && b < next_nold && active && hour + 1u < nsteps) {  // (no copy is left in flight at the exit)
-      fence_proxy_async_global();
-      fence_proxy_async();
-      small_issue_tile(dst, stage, &s_mbar, b * kTile, min((uint32_t)kTile, next_end - b * kTile));
-    }
-    if (tid == 0) {
-      uint32_t st[kSmallAcc];
-#pragma unroll
-      for (int k = 0; k < (int)kSmallAcc; k++) st[k] = __ldcg(&acc[k]);
-      s_acc[0] = st[SA_L1]; s_acc[1] = st[SA_FEM]; s_acc[2] = st[SA_INF]; s_acc[3] = st[SA_CYC];
-      s_acc[4] = st[SA_SUMCYC]; s_acc[5] = st[SA_BITES]; s_acc[6] = st[SA_IBITES]; s_acc[7] = st[SA_DMIN]; s_acc[8] = st[SA_DMAX];
-    }
-    __syncthreads();
+    const uint32_t* st = s_tot + kSmallRows;
     // the next pool's statistics (kernel/calcL1de.cl:259-280, calcGender.cl)
-    np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? s_acc[0] : 0u;
-    np.numFemale = s_acc[1];
-    np.numPotentiallyInfective = s_acc[2];
-    sampo_bites_cycles nbnc;
-    nbnc.numCyclesReported = s_acc[3];
-    nbnc.sumCyclesReported = s_acc[4];
-    nbnc.numBitesReported = s_acc[5];
-    nbnc.numInfectBitesReported = s_acc[6];
-    // the reference's shared empty initial ranges (src/abms.c:204-219)
-    bool shared_end = false;
-    uint32_t moved = 0;
-    for (int k = 1; k < 8; k++) {
-      shared_end |= s_pop.r[k].end == s_pop.r[k - 1].end;
-      moved += tot[k];
-    }
+    np.numLarvae1DayEquiv = (np.r[LARVA].end > np.r[LARVA].start) ? st[SA_L1] : 0u;
+    np.numFemale = st[SA_FEM];
+    np.numPotentiallyInfective = st[SA_INF];
+    __syncthreads();  // every thread is past its last read of s_c, s_hmr and s_pop
     if (tid == 0) {
-      CtxInputs in;
-      load_ctx_inputs(rp, step, in);
+      CtxInputs& in = s_in[hour % kSmallHours];
+      if (hour >= kSmallHours) load_ctx_inputs(rp, step, in);  // (its slot's hour is done)
       StepCtx c;
       make_ctx(in, sim->larvaHMR, np, c);  // the global table: the last CTA stores this one
       if (b == G - 1u) {
         // the replicate's state and the coming step's row for the host
+        sampo_bites_cycles nbnc;
+        nbnc.numCyclesReported = st[SA_CYC];
+        nbnc.sumCyclesReported = st[SA_SUMCYC];
+        nbnc.numBitesReported = st[SA_BITES];
+        nbnc.numInfectBitesReported = st[SA_IBITES];
+        // the reference's shared empty initial ranges (src/abms.c:204-219)
+        bool shared_end = false;
+        uint32_t moved = 0;
+        for (int k = 1; k < 8; k++) {
+          shared_end |= s_pop.r[k].end == s_pop.r[k - 1].end;
+          moved += s_tot[k];
+        }
         if (shared_end && moved) sim->warn = __ldcg(&sim->warn) | SAMPO_DEV_WARN_REF_LAYOUT;
         sim->ctx = c;
         sim->pop = np;
@@ -589,17 +629,6 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
       }
       c.larvaHMR = s_hmr;
       s_c = c;
-    }
-    {  // the next hour's larval table (every CTA; the last one also stores it)
-      const uint32_t dmin = s_acc[7], dmax = s_acc[8], l1 = np.numLarvae1DayEquiv;
-      for (int d = tid - 32; d >= 0 && d < 100; d += blockDim.x - 32) {
-        const float h = larva_hmr_entry((uint32_t)d, dmin, dmax, l1, s_cc);
-        s_hmr[d] = h;
-        if (b == G - 1u) sim->larvaHMR[d] = h;
-      }
-    }
-    __syncthreads();  // s_acc, s_c, s_hmr are read and written
-    if (tid == 0) {
       s_pop = np;
       s_step = step;
       s_epoch += 1u;
@@ -608,7 +637,24 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
       s_nold = next_nold;
       s_active = active;
     }
-    __syncthreads();
+    {  // the next hour's larval table (every CTA; the last one also stores it)
+      const uint32_t dmin = st[SA_DMIN], dmax = st[SA_DMAX], l1 = np.numLarvae1DayEquiv;
+      for (int d = tid - 32; d >= 0 && d < 100; d += blockDim.x - 32) {
+        const float h = larva_hmr_entry((uint32_t)d, dmin, dmax, l1, s_cc);
+        s_hmr[d] = h;
+        if (b == G - 1u) sim->larvaHMR[d] = h;
+      }
+    }
+    if (hour + 1u == nsteps || !active) break;  // (no copy is in flight)
+
+    // ---- grid barrier B: every CTA's stores are in; the next hour's tile ----
+    met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
+    if (!met) break;
+    if (tid == 0 && b < next_nold) {
+      fence_proxy_async_global();
+      fence_proxy_async();
+      small_issue_tile<I>(dst, stage, &s_mbar, b * kTile, min((uint32_t)kTile, next_end - b * kTile));
+    }
   }
   if (!met && tid == 0) atomicOr(&sim->error, SAMPO_DEV_ERR_BARRIER);
   // a copy that did not land in time may still be in flight: let it land

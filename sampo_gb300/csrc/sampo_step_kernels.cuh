@@ -1364,7 +1364,8 @@ __global__ void k_init_eggs(KParams p, uint32_t n, float T0, const sampo_seeds* 
 // Before and after a timing trial of the step kernels: zero what they add to
 // (survivor counts, eggs laid, next-pool statistics, tickets). Their other
 // writes - the next buffer, and tile counts and prefixes equal to the ones
-// the real step computes - leave the simulation's course unchanged.
+// the real step computes at the same tile size (k_clear_lookback clears the
+// prefixes between tile sizes) - leave the simulation's course unchanged.
 __global__ void k_trial_reset(KParams p) {
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < p.nrep; r += gridDim.x * blockDim.x) {
     SimDev* sim = p.reps[r].sim;
@@ -1378,6 +1379,20 @@ __global__ void k_trial_reset(KParams p) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     p.bat->ticket1 = 0;
     p.bat->ticket2 = 0;
+  }
+}
+
+// Between timing trials of different tile sizes, and after them: every
+// replicate's inclusive prefixes to zero. A trial leaves prefixes tagged with
+// the coming step's epoch; at another tile size they sum other slots, and the
+// look-back would take them as published. Zero epochs match no step (epochs
+// start at 1).
+__global__ void k_clear_lookback(KParams p) {
+  const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+  for (uint32_t r = 0; r < p.nrep; r++) {
+    unsigned long long* incl = p.reps[r].tileIncl;
+    const size_t n = (size_t)p.reps[r].maxTiles * 8;
+    for (size_t i = i0; i < n; i += stride) incl[i] = 0ull;
   }
 }
 

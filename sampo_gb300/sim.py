@@ -219,6 +219,10 @@ class Simulation:
         step in day graphs (None: one tile per CTA of its largest grid; 0: never)."""
         self._check(self.lib.sampo_set_small_step(self.h, 0xFFFFFFFF if max_tiles is None else max_tiles))
 
+    def set_small_step_items(self, items: int = 0):
+        """Slots per thread of the one-launch step: 0 by pool size, 2 or 4 fixed."""
+        self._check(self.lib.sampo_set_small_step_items(self.h, items))
+
     def small_step_info(self) -> dict:
         """The one-launch step's largest grid, its current max_tiles, the
         kind of the last day launched (0 none, 1 three-kernel steps, 2
