@@ -1,7 +1,7 @@
-"""The one-launch step for small pools (k_step_small) against the three-kernel
-step: day graphs that pick each hour's path on the device give the same rows
-and pools as either path forced for every hour, across the size threshold and
-beyond the one-launch grid (more tiles than CTAs)."""
+"""The one-launch day for small pools (k_step_small) against the three-kernel
+step: day graphs picked per day on the host, at either tile size, give the
+same rows and pools as the three-kernel step every hour, across the size
+threshold and beyond the one-launch grid (more tiles than CTAs)."""
 import numpy as np
 import pytest
 
