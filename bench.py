@@ -667,8 +667,9 @@ def main():
         "data": "synthetic", "config": cfg, "details": details,
         "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": r["peak"], "unit": "GB/s",
                      "frac": r["achieved"] / r["peak"], "traffic": r["traffic"], "kernel": "k_scatter (update + stable scatter)",
-                     "traffic_from": "scaled: DRAM bytes per live agent of one ncu capture of k_scatter on the 5e6-agent "
-                                     "roofline mix (profiles/k_scatter_dram.json) x this run's mean live pool",
+                     "traffic_from": "scaled: DRAM bytes per live agent of a single-pass ncu capture of k_scatter on the "
+                                     "roofline workload at 5.7e7 live agents (profiles/k_scatter_dram.json: 0.998 of the "
+                                     "algorithmic bytes) x this run's mean live pool",
                      "peak_kind": r["peak_kind"], "scatter_ms_per_launch": r["scatter_ms"], "count_ms_per_launch": r["count_ms"],
                      "publish_and_gaps_ms_per_step": r["publish_ms"],
                      "count_pass_gbs": r["count_gbs"],
