@@ -144,7 +144,6 @@ inline void fill_constant_tables(ModelConst& h) {
   for (uint32_t k = 0; k < kEggBatchTable; k++) h.eggBatchScale[k] = egg_batch_scale(k);
 }
 
-// Initial device state of a simulation (before its pool is published).
 // The tile arrays of a pool of max_tiles tiles of kTileMin slots at base
 // (16-byte aligned, for the bulk copies of the prefix tables): the prefix
 // tables (tile_pre_words words, indexed by the running tile size's table
@@ -172,6 +171,7 @@ inline const char* ranges_error(const sampo_population& pop, uint64_t capacity) 
   return nullptr;
 }
 
+// Initial device state of a simulation (before its pool is published).
 inline SimDev initial_sim_state(uint32_t capacity, float cc) {
   SimDev h;
   memset(&h, 0, sizeof(h));
