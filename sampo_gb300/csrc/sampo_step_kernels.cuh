@@ -469,10 +469,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
   auto claim = [&](uint32_t sidx) {
     CountStage& cs = s_cs[sidx];
     uint32_t t = 0;
-    if (lane == 0) {
-      t = s_tnext;
-      s_tnext = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket1, 1u);
-    }
+    if (lane == 0) t = s_tnext;
     t = __shfl_sync(0xffffffffu, t, 0);
     const uint32_t tile = total - 1u - t;
     const uint32_t r = t < total ? find_rep(s_pre, p.nrep, tile) : kNoRep;
@@ -509,6 +506,9 @@ __global__ void __launch_bounds__(kBlock, 5) k_count(KParams p) {
         cs.urg = (u >= 0 && lo + n <= cs.pop.r[u].end) ? u : -1;
         fence_proxy_async();  // the stage was last read through the generic proxy
         issue_count_tile<I>(cs.src, dsm + sidx * kCountStage, &bars[sidx], cs.pop, lo, n, cs.larv != 0);
+        // the ticket of the claim after this one, drawn once the copies are
+        // on their way (its round trip stays off the stage's refill)
+        s_tnext = one_each ? 0xffffffffu : atomicAdd(&p.bat->ticket1, 1u);
       }
     }
   };
