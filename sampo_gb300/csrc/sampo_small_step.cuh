@@ -53,17 +53,20 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   return v;
 }
 
-// All CTAs of the grid (co-resident: a cooperative launch) wait until the
-// arrival counter reaches `target` (the grid size times the barriers passed
-// so far in the launch). The CTA's writes are ordered before its arrival by
-// the CTA barrier and the release of the arrival; the acquire of the counter
-// orders the reads that follow. Bounded: false when the others did not
-// arrive within the limit. Every thread calls it; every thread gets the same
-// answer.
-__device__ bool small_grid_barrier(uint32_t* bar, uint32_t target, uint32_t* s_flag) {
+// A grid barrier in two halves. small_grid_arrive (every thread): the CTA's
+// writes so far are ordered before its arrival by the CTA barrier and the
+// release of the arrival. small_grid_wait (every thread): all CTAs of the
+// grid (co-resident: a cooperative launch) wait until the arrival counter
+// reaches `target` (the grid size times the barriers passed so far in the
+// launch); the acquire of the counter orders the reads that follow. Bounded:
+// false when the others did not arrive within the limit; every thread gets
+// the same answer. Work that needs no other CTA can go between the halves.
+__device__ __forceinline__ void small_grid_arrive(uint32_t* bar) {
   __syncthreads();
+  if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+}
+__device__ bool small_grid_wait(uint32_t* bar, uint32_t target, uint32_t* s_flag) {
   if (threadIdx.x == 0) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
     uint32_t ok = 0;
     for (uint32_t i = 0; i < kWaitLimit; i++) {
       if (ld_acquire_u32(bar) >= target) { ok = 1; break; }
@@ -73,6 +76,10 @@ __device__ bool small_grid_barrier(uint32_t* bar, uint32_t target, uint32_t* s_f
   }
   __syncthreads();
   return *s_flag != 0;
+}
+__device__ bool small_grid_barrier(uint32_t* bar, uint32_t target, uint32_t* s_flag) {
+  small_grid_arrive(bar);
+  return small_grid_wait(bar, target, s_flag);
 }
 
 struct SmallAcc {
@@ -585,9 +592,12 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
     }
 
     // ---- the next hour's state (the k_publish arithmetic, publish_rep), by
-    //      every CTA from the same totals ----
+    //      every CTA from the same totals, between its arrival at the grid
+    //      barrier (its stores are in) and its wait there ----
     const uint32_t step = s_step + 1u;
     const bool active = step < s_stop;
+    const bool more = hour + 1u < nsteps && active;  // another hour in this launch
+    if (more) small_grid_arrive(&p.bat->bar);
     const uint32_t next_end = np.r[GRAVID].end, next_nold = (next_end + kTile - 1) / kTile;
     const uint32_t* st = s_tot + kSmallRows;
     // the next pool's statistics (kernel/calcL1de.cl:259-280, calcGender.cl)
@@ -645,10 +655,10 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
         if (b == G - 1u) sim->larvaHMR[d] = h;
       }
     }
-    if (hour + 1u == nsteps || !active) break;  // (no copy is in flight)
+    if (!more) break;  // (no copy is in flight)
 
-    // ---- grid barrier B: every CTA's stores are in; the next hour's tile ----
-    met = small_grid_barrier(&p.bat->bar, G * ++barriers, &s_flag);
+    // ---- the grid barrier's wait: every CTA's stores are in; the next hour's tile ----
+    met = small_grid_wait(&p.bat->bar, G * ++barriers, &s_flag);
     if (!met) break;
     if (tid == 0 && b < next_nold) {
       fence_proxy_async_global();
