@@ -586,7 +586,7 @@ def main():
     ap.add_argument("--small-step", default="auto",
                     help="plain-path workloads: 'auto' (one-launch step for pools of up to one tile per CTA of its "
                          "grid), 'off' (the three-kernel step every hour) or a largest pool in 1024-slot tiles")
-    ap.add_argument("--small-items", type=int, default=0, choices=(0, 2, 4),
+    ap.add_argument("--small-items", type=int, default=0, choices=(0, 1, 2, 4),
                     help="plain-path workloads: slots per thread of the one-launch step (0: by pool size)")
     ap.add_argument("--replicates", type=int, default=512, help="ensemble: replicates")
     ap.add_argument("--requests", type=int, default=200, help="served: requests per rate")
@@ -659,7 +659,7 @@ def main():
                               "timed_days_one_launch": r["small"]["days_one_launch"] - r["small0"]["days_one_launch"],
                               "timed_days_three_kernel": r["small"]["days_three_kernel"] - r["small0"]["days_three_kernel"],
                               "one_launch_kind": {0: "-", 1: "-", 2: "cooperative launch", 3: "plain launch of a co-resident grid"}[r["small"]["last_day"]],
-                              "slots_per_thread": args.small_items or "by pool size (2 up to 228 512-slot tiles, else 4)"}}
+                              "slots_per_thread": args.small_items or "by pool size (the smallest tiles, of 256, 512 or 1024 slots, that fit two per CTA of the largest grid)"}}
     line = {
         "metric": "agent-days/s", "value": job_rate(tot_days, tmax), "unit": "agent-days/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,

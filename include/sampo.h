@@ -205,10 +205,10 @@ int sampo_items_per_thread(sampo_sim* s, uint32_t* items);
  * (sampo_set_species) always take the three-kernel step. */
 #define SAMPO_SMALL_STEP_DEFAULT 0xffffffffu
 int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles);
-/* Slots per thread of the one-launch step: 0 (the default) takes 512-slot
- * tiles (2) while the pool leaves the largest grid room for them and
- * 1024-slot tiles (4) above that; 2 or 4 fix it. The results do not depend
- * on it. */
+/* Slots per thread of the one-launch step: 0 (the default) takes the
+ * smallest tiles, 256 (1), 512 (2) or 1024 slots (4), that the pool leaves
+ * the largest grid room for; 1, 2 or 4 fix it. The results do not depend on
+ * it. */
 int sampo_set_small_step_items(sampo_sim* s, uint32_t items);
 /* The one-launch step's largest grid (CTAs; 0 when it cannot run here), the
  * current max_tiles, the kind of the last day launched (0 none yet, 1

@@ -62,9 +62,9 @@ struct sampo_sim {
   // per day from the pool end the host last saw (known_end).
   int small_grid = 0;                  // largest grid of the one-launch step (0: it cannot run on this device)
   uint32_t small_tiles = 0;            // largest pool in 1024-slot tiles that takes the one-launch step (0: never)
-  int small_items = 0;                 // its slots per thread: 2, 4, or 0 (by pool size)
-  cudaGraphExec_t small_graph[2][8] = {};  // [512-slot tiles, 1024-slot tiles][grid bucket]
-  int small_graph_kind[2][8] = {};     // DG_* of each
+  int small_items = 0;                 // its slots per thread: 1, 2, 4, or 0 (by pool size)
+  cudaGraphExec_t small_graph[3][8] = {};  // [256-, 512-, 1024-slot tiles][grid bucket]
+  int small_graph_kind[3][8] = {};     // DG_* of each
   uint32_t known_end = 0;              // pool end at the start of the coming day, as last seen by the host
   uint32_t* end_pinned = nullptr;      // pool end after a day, copied back one day behind the queue
   cudaEvent_t ev_day[2] = {nullptr, nullptr};
@@ -238,7 +238,7 @@ extern "C" int sampo_create(const sampo_config* cfg, sampo_sim** out) {
     }
     s->grid_count = grid_blocks_count(1);
     s->grid_scatter = grid_blocks_scatter(1);
-    s->small_grid = std::min(grid_blocks_small(2), grid_blocks_small(4));
+    s->small_grid = std::min(grid_blocks_small(1), std::min(grid_blocks_small(2), grid_blocks_small(4)));
     s->small_tiles = s->small_grid > 0 ? (uint32_t)s->small_grid : 0u;  // one tile per CTA
     if ((e = cudaMallocHost(&s->end_pinned, 2 * sizeof(uint32_t))) != cudaSuccess) { rc = cuda_fail(s, e, "pinned"); break; }
     for (auto& ev : s->ev_day) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -464,7 +464,7 @@ static void drop_day_graph(sampo_sim* s) {
 static cudaError_t build_small_graph(sampo_sim* s, int items, int b) {
   const KParams p = make_params(s);
   const int grid = (int)small_bucket_grid(s, b);
-  const int ti = items == 2 ? 0 : 1;
+  const int ti = items == 1 ? 0 : items == 2 ? 1 : 2;
   cudaError_t e = cudaErrorUnknown;
   for (int kind : {DG_SMALL_COOP, DG_SMALL}) {
     cudaGraph_t g = nullptr;
@@ -488,18 +488,24 @@ static cudaError_t build_small_graph(sampo_sim* s, int items, int b) {
 // The graph of the coming day and its kernel launches: the one-launch step
 // (grid of at least kSmallGrowth CTAs per tile of the pool end last seen)
 // when that pool has at most small_tiles 1024-slot tiles, else the
-// three-kernel step. The one-launch step takes 512-slot tiles (half the
-// chain of updates per thread) while the largest grid has room for them,
-// else 1024-slot tiles. Any pick gives the same results at any size: a pool
-// that outgrew its pick is stepped by the one-launch kernel's extra-tile route.
+// three-kernel step. The one-launch step takes the smallest tiles (the
+// shortest chain of updates per thread: 256, then 512, then 1024 slots) the
+// largest grid has room for. Any pick gives the same results at any size: a
+// pool that outgrew its pick is stepped by the one-launch kernel's
+// extra-tile route.
 static int day_graph_for(sampo_sim* s, cudaGraphExec_t* gx, uint32_t* kernels, int* kind) {
-  const uint32_t t4 = (s->known_end + kTile - 1) / kTile, t2 = (s->known_end + kTileMin - 1) / kTileMin;
+  const uint32_t end = s->known_end;
+  const uint32_t t4 = (end + kTile - 1) / kTile;
   if (!s->species && s->small_grid > 0 && s->small_tiles > 0 && t4 <= s->small_tiles) {
+    auto tiles_of = [&](int items) { const uint32_t t = (end + kBlock * items - 1) / (kBlock * items); return t ? t : 1u; };
     int items = s->small_items;
-    if (items == 0) items = (uint64_t)(t2 ? t2 : 1u) * kSmallGrowth <= (uint64_t)s->small_grid ? 2 : 4;
-    const uint32_t tiles = items == 2 ? t2 : t4;
-    const uint64_t want = (uint64_t)(tiles ? tiles : 1u) * kSmallGrowth;
-    const int ti = items == 2 ? 0 : 1;
+    if (items == 0) {
+      items = 4;
+      for (int i : {2, 1})
+        if ((uint64_t)tiles_of(i) * kSmallGrowth <= (uint64_t)s->small_grid) items = i;
+    }
+    const uint64_t want = (uint64_t)tiles_of(items) * kSmallGrowth;
+    const int ti = items == 1 ? 0 : items == 2 ? 1 : 2;
     int b = 0;
     while (b + 1 < kSmallBuckets && small_bucket_grid(s, b) < want) b++;
     if (s->small_graph[ti][b] || build_small_graph(s, items, b) == cudaSuccess) {
@@ -527,7 +533,8 @@ extern "C" int sampo_set_small_step(sampo_sim* s, uint32_t max_tiles) {
 
 extern "C" int sampo_set_small_step_items(sampo_sim* s, uint32_t items) {
   if (!s) return SAMPO_ERR_ARG;
-  if (items != 0 && items != 2 && items != 4) return fail(s, SAMPO_ERR_ARG, "slots per thread of the one-launch step: 0, 2 or 4");
+  if (items != 0 && items != 1 && items != 2 && items != 4)
+    return fail(s, SAMPO_ERR_ARG, "slots per thread of the one-launch step: 0, 1, 2 or 4");
   SETTLE(s);
   s->small_items = (int)items;
   return SAMPO_OK;

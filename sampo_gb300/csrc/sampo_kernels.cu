@@ -234,7 +234,7 @@ cudaError_t tune_grids(const KParams& p, cudaStream_t st, int* grid_count, int* 
   return e;
 }
 static const void* small_fn(int items) {
-  return items == 2 ? (const void*)k_step_small<2> : (const void*)k_step_small<4>;
+  return items == 1 ? (const void*)k_step_small<1> : items == 2 ? (const void*)k_step_small<2> : (const void*)k_step_small<4>;
 }
 int grid_blocks_small(int items) {
   int per = 0;

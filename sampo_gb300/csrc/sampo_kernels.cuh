@@ -213,7 +213,7 @@ cudaError_t launch_eval_math(int fn, const float* x, const float* y, float* out,
 // Kernel nodes in a captured graph (the launches one replay makes).
 cudaError_t graph_kernel_nodes(cudaGraph_t g, uint32_t* kernels);
 // The one-launch steps of a single simulation (sampo_small_step.cuh) with
-// tiles of kBlock * items slots (items 2 or 4): the largest grid (CTAs
+// tiles of kBlock * items slots (items 1, 2 or 4): the largest grid (CTAs
 // resident on all SMs, 0 if it cannot run) and a launch of `nsteps` hourly
 // steps (a cooperative launch when `cooperative`) on `grid` CTAs.
 int grid_blocks_small(int items = kItems);

@@ -35,7 +35,7 @@
 
 namespace sampo {
 
-constexpr int kSmallThreads = kBlock;      // eight warps, I slots per thread (tiles of kBlock * I slots)
+constexpr int kSmallThreads = kBlock;      // eight warps, I slots per thread (tiles of kBlock * I slots: I = 1, 2 or 4)
 constexpr int kSmallMinBlocks = 3;         // resident CTAs per SM the registers are sized for
 __host__ __device__ constexpr uint32_t small_stage(int items) { return 9 * kBlock * items * 4 + kBlock * items; }  // ten columns
 constexpr uint32_t kSmallRows = 9;         // per-tile counts: survivors by next state, eggs laid
@@ -45,7 +45,9 @@ constexpr uint32_t kSmallHours = 24;       // hours whose inputs a CTA holds in 
 // L1de, females, infective, cycles, sum of cycles, bites, infective bites
 // (sums) and the min and max larva age in days.
 enum : uint32_t { SA_L1 = 0, SA_FEM, SA_INF, SA_CYC, SA_SUMCYC, SA_BITES, SA_IBITES, SA_DMIN, SA_DMAX, kSmallStats };
-static_assert(kSmallRows + kSmallStats <= kPreWordsMin, "the per-tile rows fit the prefix-table array");
+// The rows' stride is twice the pool's count of 512-slot tiles (room for
+// 256-slot tiles): they fit the prefix-table array.
+static_assert(2 * (kSmallRows + kSmallStats) <= kPreWordsMin, "the per-tile rows fit the prefix-table array");
 
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   uint32_t v;
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
   const uint32_t G = gridDim.x, b = blockIdx.x;
   uint32_t phase = 0, barriers = 0;
   bool met = true, ok = true;
-  const uint32_t stride = rp.maxTiles;
+  const uint32_t stride = 2u * rp.maxTiles;  // >= the tiles of any pool that fits, at 256-slot tiles
   uint32_t* rows = rp.tilePre;  // [kSmallRows + kSmallStats][stride]
 
   // ---- the replicate's state at the launch (the previous kernel wrote it) ----

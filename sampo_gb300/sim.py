@@ -220,7 +220,7 @@ class Simulation:
         self._check(self.lib.sampo_set_small_step(self.h, 0xFFFFFFFF if max_tiles is None else max_tiles))
 
     def set_small_step_items(self, items: int = 0):
-        """Slots per thread of the one-launch step: 0 by pool size, 2 or 4 fixed."""
+        """Slots per thread of the one-launch step: 0 by pool size, 1, 2 or 4 fixed."""
         self._check(self.lib.sampo_set_small_step_items(self.h, items))
 
     def small_step_info(self) -> dict:

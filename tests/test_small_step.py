@@ -48,7 +48,7 @@ def test_paths_agree(gpu_ready, oracle_mod, sizes, n, cc):
     identical rows, pools, histograms. The second pool grows from 489 to
     about 2,500 tiles, more than the one-launch grid has CTAs, so 'always'
     takes the route that visits a CTA's extra tiles twice. The one-launch
-    step's 512- and 1024-slot tiles are also forced on their own."""
+    step's 256-, 512- and 1024-slot tiles are also forced on their own."""
     ranges, arrays, T, env, seeds = _workload(sizes, n, cc, seed=11)
     cap = 1 << 22
     ref = _run(ranges, arrays, T, env, seeds, cc, n, 0, cap)
@@ -56,7 +56,7 @@ def test_paths_agree(gpu_ready, oracle_mod, sizes, n, cc):
     tiles = (ref[0]["ranges"][:, 7, 1].astype(np.int64) + 1023) // 1024
     mid = int(np.median(tiles))
     # (max_tiles, slots per thread of the one-launch step: 0 by pool size)
-    for max_tiles, items in ((1 << 30, 0), (None, 0), (mid, 0), (1 << 30, 2), (1 << 30, 4)):
+    for max_tiles, items in ((1 << 30, 0), (None, 0), (mid, 0), (1 << 30, 1), (1 << 30, 2), (1 << 30, 4)):
         got = _run(ranges, arrays, T, env, seeds, cc, n, max_tiles, cap, items)
         assert got[4] == 0, f"max_tiles={max_tiles}, items={items}: device status {got[4]:#x}"
         info = got[5]
@@ -102,7 +102,7 @@ def test_small_step_matches_oracle(gpu_ready, oracle_mod):
     assert np.array_equal(hist, orc.histogram())
 
 
-@pytest.mark.parametrize("items", [2, 4])
+@pytest.mark.parametrize("items", [1, 2, 4])
 def test_pool_outgrowing_its_grid_matches_golden(gpu_ready, tmp_path, items):
     """The golden interventions case (a few thousand agents, 40 days): each
     day's grid is picked from the pool end seen two days earlier, so on some
