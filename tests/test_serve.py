@@ -72,3 +72,76 @@ def test_served_pools_grow_and_match_solo_runs(gpu_ready, grow_at):
         assert res.rows.tobytes() == rows.tobytes(), f"request {res.rid}: rows differ from its solo run"
         assert np.array_equal(res.histogram, hist)
         assert res.status == status == 0
+
+
+class _FakeBatch:
+    """The two calls the growth policy makes, on fixed slot states."""
+
+    def __init__(self, states):
+        self.st = states
+        self.grown = []
+
+    def states(self):
+        return self.st
+
+    def grow(self, slot, capacity):
+        self.grown.append((slot, capacity))
+        self.st[slot]["capacity"] = capacity
+
+
+def _policy_server(states, steps, budget, used_extra=0, grow_at=2, grow_to=3):
+    """A Server whose batch is a fake: only the growth policy (_grow) runs."""
+    from types import SimpleNamespace
+    from sampo_gb300.batch import Batch
+    from sampo_gb300.serve import Server
+    srv = Server.__new__(Server)
+    srv.grow_at, srv.grow_to, srv.ring = grow_at, grow_to, 25
+    srv.batch = _FakeBatch(states)
+    srv.resident = {}
+    srv.used = used_extra
+    for slot, st in states.items():
+        nbytes = Batch.replicate_bytes(st["capacity"], srv.ring)
+        srv.resident[slot] = (SimpleNamespace(spec=SimpleNamespace(steps=steps[slot])), None, nbytes)
+        srv.used += nbytes
+    srv.budget = budget
+    srv.grows = srv.pauses = srv.over_budget = srv.peak_bytes = 0
+    srv.held = False
+    return srv
+
+
+def _state(step, active, status, end, capacity):
+    return {"step": step, "active": active, "status": status, "end": end, "capacity": capacity}
+
+
+def test_growth_policy_without_gpu(sampo_lib):
+    """Which pools the server grows between days, and when it holds
+    admissions (host logic only: a fake batch stands for the GPU)."""
+    from sampo_gb300.batch import Batch
+    from sampo_gb300.serve import CAPACITY_BIT
+    ring = 25
+    cost = lambda cap: Batch.replicate_bytes(cap, ring)
+    # a paused replicate, a running one past half its capacity, one below it,
+    # one finished: the first two grow, paused first, to 3 x end + 65536
+    states = {0: _state(40, 0, CAPACITY_BIT, 90000, 100000), 1: _state(40, 1, 0, 60000, 100000),
+              2: _state(40, 1, 0, 40000, 100000), 3: _state(48, 0, 0, 99000, 100000)}
+    srv = _policy_server(states, {0: 48, 1: 48, 2: 48, 3: 48}, budget=1 << 40)
+    srv._grow()
+    assert srv.batch.grown == [(0, 3 * 90000 + 65536), (1, 3 * 60000 + 65536)]
+    assert (srv.grows, srv.pauses, srv.over_budget, srv.held) == (2, 1, 0, False)
+    # grow_at = 0: only paused pools grow
+    states = {0: _state(40, 0, CAPACITY_BIT, 90000, 100000), 1: _state(40, 1, 0, 60000, 100000)}
+    srv = _policy_server(states, {0: 48, 1: 48}, budget=1 << 40, grow_at=0)
+    srv._grow()
+    assert srv.batch.grown == [(0, 3 * 90000 + 65536)]
+    # a paused pool that does not fit while another runs: admissions are held
+    states = {0: _state(40, 0, CAPACITY_BIT, 90000, 100000), 1: _state(40, 1, 0, 10000, 100000)}
+    base = 2 * cost(100000)
+    srv = _policy_server(states, {0: 48, 1: 48}, budget=base + 1000)
+    srv._grow()
+    assert srv.batch.grown == [] and srv.held
+    # nothing runs: the smallest paused growth goes ahead over the budget
+    states = {0: _state(40, 0, CAPACITY_BIT, 90000, 100000), 1: _state(40, 0, CAPACITY_BIT, 50000, 100000)}
+    srv = _policy_server(states, {0: 48, 1: 48}, budget=base + 1000)
+    srv._grow()
+    assert srv.batch.grown == [(1, 3 * 50000 + 65536)]
+    assert srv.over_budget == 1 and srv.used == base + cost(3 * 50000 + 65536) - cost(100000)
