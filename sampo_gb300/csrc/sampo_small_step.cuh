@@ -382,17 +382,18 @@ __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence
 // seed stream): `nsteps` hourly steps in one cooperative launch (a day graph
 // launches it once with 24). Per hour: the update (phase 1), whose per-tile
 // counts and per-CTA statistics of the next pool go to rows in global
-// memory; a grid barrier; the scatter (phase 2), after which every CTA
-// computes the next hour's layout, statistics row, step constants and larval
-// table itself from the same totals (the k_publish arithmetic; the last CTA,
-// the one least likely to hold a tile, also writes them to the replicate's
-// state for the host); a second grid barrier, after which the next hour's
-// tile copies go out. The step inputs of the launch's hours are read into
-// shared memory at its start (the host writes them before the launch). The
-// rows use the replicate's prefix-table array (tilePre: kSmallRows +
-// kSmallStats words per tile), which the three-kernel step rewrites before it
-// reads it. The pool the scatter wrote with ordinary stores is read by the
-// next hour's bulk copies after proxy fences.
+// memory; a grid barrier; the scatter (phase 2) and the arrival at a second
+// grid barrier, after which every CTA computes the next hour's layout,
+// statistics row, step constants and larval table itself from the same
+// totals (the k_publish arithmetic; the last CTA, the one least likely to
+// hold a tile, also writes them to the replicate's state for the host) before
+// it waits there; then the next hour's tile copies go out. The step inputs of
+// the launch's hours are read into shared memory at its start (the host
+// writes them before the launch). The rows use the replicate's prefix-table
+// array (tilePre: kSmallRows + kSmallStats words per column, at a stride of
+// twice its count of 512-slot tiles), which the three-kernel step rewrites
+// before it reads it. The pool the scatter wrote with ordinary stores is
+// read by the next hour's bulk copies after proxy fences.
 template <int I>
 __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(KParams p, uint32_t nsteps) {
   SAMPO_TILE_CONSTANTS(I);
