@@ -326,10 +326,11 @@ __device__ __forceinline__ void small_sum_rows(const uint32_t* rows, uint32_t st
 }
 
 // Phase 1's end: the CTA's statistics of the next pool (its tiles) to its
-// column of the statistics rows. All threads.
-__device__ __forceinline__ void small_put_stats(const SmallAcc& sa, uint32_t* rows, uint32_t stride, uint32_t b,
-                                                uint32_t (*s_red)[kSmallStats]) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// column of the statistics rows, in two halves around a CTA barrier: each
+// warp's totals into s_red (every thread), then the CTA's totals out by the
+// threads of warp `w` (the other warps may do other work meanwhile).
+__device__ __forceinline__ void small_stats_warps(const SmallAcc& sa, uint32_t (*s_red)[kSmallStats]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t v[kSmallStats] = {sa.l1, sa.fem, sa.inf, sa.acc.cycles, sa.acc.sumCycles, sa.acc.bites, sa.acc.infectBites,
                              sa.dmin, sa.dmax};
 #pragma unroll
@@ -340,14 +341,17 @@ __device__ __forceinline__ void small_put_stats(const SmallAcc& sa, uint32_t* ro
 #pragma unroll
     for (int j = 0; j < (int)kSmallStats; j++) s_red[warp][j] = v[j];
   }
-  __syncthreads();
-  if (tid < (int)kSmallStats) {
-    uint32_t x = s_red[0][tid];
-    for (int w = 1; w < kWarps; w++) {
-      const uint32_t y = s_red[w][tid];
-      x = tid == (int)SA_DMIN ? min(x, y) : tid == (int)SA_DMAX ? max(x, y) : x + y;
+}
+__device__ __forceinline__ void small_stats_store(uint32_t* rows, uint32_t stride, uint32_t b,
+                                                  const uint32_t (*s_red)[kSmallStats], int w) {
+  const int k = (int)threadIdx.x - 32 * w;
+  if (k >= 0 && k < (int)kSmallStats) {
+    uint32_t x = s_red[0][k];
+    for (int i = 1; i < kWarps; i++) {
+      const uint32_t y = s_red[i][k];
+      x = k == (int)SA_DMIN ? min(x, y) : k == (int)SA_DMAX ? max(x, y) : x + y;
     }
-    __stcg(rows + (size_t)(kSmallRows + tid) * stride + b, x);
+    __stcg(rows + (size_t)(kSmallRows + k) * stride + b, x);
   }
 }
 
@@ -494,8 +498,10 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
         ok = small_wait_stage(&s_mbar, phase);
         if (ok) {
           small_update_tile<I, true, false, false>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);  // counted above
+          small_stats_warps(sa, s_red);
           __syncthreads();
           if (warp == 0) (void)small_build_table<I>(s_ent, s_tab);
+          else if (warp == 1) small_stats_store(rows, stride, b, s_red, 1);
         }
       }
     } else if (b < nold) {
@@ -505,17 +511,19 @@ __global__ void __launch_bounds__(kSmallThreads, kSmallMinBlocks) k_step_small(K
         small_update_tile<I, true, true, true>(s_c, s_mc, s_pop, stage, b * kTile, end, s_ent, sa);
         const uint32_t ne = __reduce_add_sync(0xffffffffu, sa.acc.newEggs - eggs_before);
         if (lane == 0) s_ne[warp] = ne;
+        small_stats_warps(sa, s_red);
         __syncthreads();
-        if (warp == 0) {
+        if (warp == 0) {  // the tile's table and counts
           const uint32_t tw = small_build_table<I>(s_ent, s_tab);
           if (lane < 8) __stcg(rows + (size_t)lane * stride + b, tw);
           uint32_t e = lane < kWarps ? s_ne[lane] : 0u;
           e = __reduce_add_sync(0xffffffffu, e);
           if (lane == 0) __stcg(rows + (size_t)8 * stride + b, e);
+        } else if (warp == 1) {  // meanwhile the CTA's statistics
+          small_stats_store(rows, stride, b, s_red, 1);
         }
       }
     }
-    if (b < nold) small_put_stats(sa, rows, stride, b, s_red);
     if (tid == 0) s_ok = ok ? 1u : 0u;
 
     // ---- grid barrier A: every tile's counts and every CTA's statistics are published ----
